@@ -1,0 +1,395 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 sieve path: (p,n) pairs tested per second.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--workload combined|factorial|primorial]
+
+Workload (default): the combined factorial + compositorial search (-! -c) over
+n in [101, 200000) and p in [10^9, 10^9 + 10^8): about 4.8e6 candidate primes
+x 199,899 n = 9.7e11 pairs per step.  Inputs are the scalar search bounds; the
+tables live in HBM from job creation on.
+
+One step = candidate generation + setup + iterate over the whole n range +
+check + hit read-back, through the C ABI stage calls on the context stream.
+`value` is pairs per second over K steps timed with CUDA events on that
+stream; the candidate state (16 B x 4.8e6) is smaller than L2, so a 256 MB
+buffer is overwritten on the same stream before every step (inside the timed
+region).  `e2e` is the same metric through pfcsieve_gb300.sieve(), the call a
+user makes: table build and upload, all segments, hit drain, CPU
+re-verification of every hit, 2-PRP filter and checksum, timed on the host.
+
+The roofline object covers the iterate kernel (the dominant one): achieved =
+algorithmic 32-bit multiply operations (4 per class-32 Montgomery
+multiplication, 16 per class-64 one) / kernel time; peak = 32-bit IMAD
+throughput measured in this run by pfc_bench_int_peak.
+
+--impl reference times the reference algorithm's CPU form (the oracle port of
+the reference kernels, OpenMP over all host threads) on a bounded sample of
+the same workload.  Under torchrun each rank runs its own p range (weak
+scaling) and rank 0 prints the JSON line.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "(p,n) pairs tested/s"
+UNIT = "pairs/s"
+
+WORKLOADS = {
+    # configs of the reference benchmark description: -! -c, -!, -#
+    "combined": dict(mode=5, nmin=101, nmax=200000, pmin=10**9, pmax=10**9 + 10**8,
+                     desc="-! -c n=[101,200000) p=[1e9,1.1e9)"),
+    "factorial": dict(mode=1, nmin=101, nmax=20000, pmin=10**7, pmax=10**7 + 10**6,
+                      desc="-! n=[101,20000) p=[1e7,1.1e7)"),
+    "primorial": dict(mode=2, nmin=101, nmax=10**6, pmin=2**62, pmax=2**62 + 5 * 10**7,
+                      desc="-# n=[101,1e6) p=[2^62,2^62+5e7)"),
+}
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="combined", choices=sorted(WORKLOADS))
+    ap.add_argument("--e2e-steps", type=int, default=2)
+    ap.add_argument("--cpu-sample", type=int, default=0,
+                    help="candidates in the CPU baseline sample (0 = auto)")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+# ------------------------------------------------------------ distributed
+
+def dist_env():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def dist_init(world):
+    if world <= 1:
+        return None
+    import torch.distributed as dist
+    backend = "nccl" if _cuda_available() else "gloo"
+    dist.init_process_group(backend=backend)
+    return dist
+
+
+def _cuda_available():
+    try:
+        import torch
+        return torch.cuda.is_available()
+    except Exception:
+        return False
+
+
+def shard(wl, rank):
+    """Weak scaling: rank r sieves the p range of the same length after rank r-1's."""
+    span = wl["pmax"] - wl["pmin"]
+    lo = wl["pmin"] + rank * span
+    return lo, lo + span
+
+
+def barrier_max(dist, x):
+    if dist is None:
+        return x
+    import torch
+    dev = "cuda" if _cuda_available() else "cpu"
+    t = torch.tensor([float(x)], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+# ------------------------------------------------------------------ clocks
+
+class ClockSampler:
+    """nvidia-smi samples every 200 ms while the timed region runs."""
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.rows = []
+        self.proc = None
+        self.thr = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.Q,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+            return
+        self.thr = threading.Thread(target=self._read, daemon=True)
+        self.thr.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            f = [x.strip() for x in line.split(",")]
+            if len(f) >= 7:
+                self.rows.append(f)
+
+    def stop(self):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+        if self.thr is not None:
+            self.thr.join(timeout=2)
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        sm, mx, reasons = [], [], set()
+        for r in self.rows:
+            try:
+                sm.append(float(r[0]))
+                mx.append(float(r[1]))
+            except ValueError:
+                continue
+            for k, name in enumerate(names):
+                if r[3 + k].lower().startswith("active"):
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx),
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ------------------------------------------------------- CPU baseline (oracle)
+
+def cpu_sample_run(wl, ncands, offset=0):
+    """Time the oracle (the reference algorithm on the CPU) on `ncands`
+    candidates of the workload's p range, all host threads."""
+    from oracle import oracle as o
+    o.build()
+    # candidates of a short range at the bottom of the workload's p range
+    lo = wl["pmin"] + offset
+    span = max(int(ncands * np.log(float(lo)) * 1.3), 1000)
+    cands = o.candidates(lo, lo + span)[:ncands]
+    threads = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    o.sieve(wl["mode"], wl["nmin"], wl["nmax"], cands, threads)
+    dt = time.perf_counter() - t0
+    pairs = len(cands) * (wl["nmax"] - wl["nmin"])
+    return pairs / dt, dict(cores=threads, seconds=dt, cands=len(cands), pairs=pairs)
+
+
+def auto_sample(wl):
+    # about 10-20 s of CPU work on 16 cores at ~1e8 mulmods/s/core
+    per_cand = (wl["nmax"] - wl["nmin"]) * (2 if wl["mode"] == 5 else 1)
+    if wl["mode"] == 2:
+        per_cand = (wl["nmax"] - wl["nmin"]) / 12 * 2 * 5   # primes only, 64-bit, 2 mulmods
+    budget = 1.6e9 * 12 * (os.cpu_count() or 1) / 16
+    return int(max(64, min(200000, budget / per_cand)))
+
+
+# -------------------------------------------------------------- reference
+
+def run_reference(args, wl, world, rank):
+    if rank != 0:
+        return
+    n = args.cpu_sample or max(16, auto_sample(wl) // 4)
+    rates = []
+    info = None
+    for s in range(args.warmup + args.steps):
+        rate, info = cpu_sample_run(wl, n, offset=s * 1000)
+        if s >= args.warmup:
+            rates.append(rate)
+    value = float(np.mean(rates))
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT,
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": info["seconds"] * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "u64", "data": "synthetic (deterministic search bounds)",
+        "config": {"workload": wl["desc"], "sample": "%d candidates x full n range per step" % n,
+                   "l2": "n/a (CPU)"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": info["cores"], "kind": "port",
+                         "sample": "%d candidates from the bottom of the p range x all n" % n},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+# -------------------------------------------------------------------- ours
+
+def n_composites(nmin, nmax):
+    sieve = np.ones(nmax, dtype=bool)
+    sieve[:2] = False
+    for i in range(2, int(nmax ** 0.5) + 1):
+        if sieve[i]:
+            sieve[i * i::i] = False
+    seg = sieve[nmin:nmax]
+    return int(len(seg) - seg.sum()), int(seg.sum())
+
+
+def run_ours(args, wl, world, rank, local, dist):
+    import torch
+
+    import pfcsieve_gb300 as pfc
+
+    torch.cuda.set_device(local)
+    lo, hi = shard(wl, rank)
+    ctx = pfc.Context(local)
+    name, sms = ctx.device_info()
+    stream = torch.cuda.ExternalStream(ctx.stream, device=torch.device("cuda", local))
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    job = pfc.Job(ctx, wl["mode"], wl["nmin"], wl["nmax"], lo, hi)
+
+    ncomp, nprime = n_composites(wl["nmin"], wl["nmax"])
+    it_ms = []
+
+    def step():
+        with torch.cuda.stream(stream):
+            flush.zero_()
+        job.gen(lo, hi)
+        job.setup()
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        job.iterate(wl["nmin"], wl["nmax"])
+        b.record(stream)
+        job.check()
+        job.drain_hits()
+        return a, b
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    barrier(dist)
+    launches0 = ctx.launches
+    pairs0 = job.pairs
+    clk = ClockSampler(local)
+    clk.start()
+    t0 = torch.cuda.Event(enable_timing=True)
+    t1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    t0.record(stream)
+    evs = [step() for _ in range(args.steps)]
+    t1.record(stream)
+    torch.cuda.synchronize()
+    clocks = clk.stop()
+    barrier(dist)
+    ms = t0.elapsed_time(t1)
+    it_ms = [a.elapsed_time(b) for a, b in evs]
+    launches = ctx.launches - launches0
+    pairs = job.pairs - pairs0
+    ms_max = barrier_max(dist, ms)
+    pairs_total = pairs * world
+    value = pairs_total / (ms_max * 1e-3)
+
+    termsum, _ = job.totals()
+    cands_per_step = pairs // args.steps // (wl["nmax"] - wl["nmin"])
+    job.close()
+
+    # roofline of the iterate kernel: algorithmic 32-bit multiply ops / time
+    mode = wl["mode"]
+    if mode == 2:
+        steps_per_cand = nprime
+    elif mode == 5:
+        steps_per_cand = (wl["nmax"] - wl["nmin"]) + ncomp
+    elif mode == 4:
+        steps_per_cand = ncomp
+    else:
+        steps_per_cand = wl["nmax"] - wl["nmin"]
+    cls32 = hi <= 2**32
+    ops_per_mulmod = 4 if cls32 else 16
+    alg_ops = cands_per_step * steps_per_cand * ops_per_mulmod
+    it_s = float(np.mean(it_ms)) * 1e-3
+    peak = pfc.int_peak(local, 0)
+    achieved = alg_ops / it_s
+    traffic = None
+    tfile = os.path.join(ROOT, "profiles", "iterate_traffic.json")
+    if os.path.exists(tfile):
+        try:
+            t = json.load(open(tfile))
+            if t.get("workload") == wl["desc"]:
+                traffic = t.get("dram_bytes_per_step")
+        except Exception:
+            traffic = None
+
+    # end to end through the public call
+    e2e = None
+    if rank == 0 and args.e2e_steps > 0:
+        h2d0, d2h0 = ctx.transfer_bytes()
+        walls = []
+        res = None
+        for _ in range(args.e2e_steps):
+            t = time.perf_counter()
+            res = pfc.sieve(mode, wl["nmin"], wl["nmax"], lo, hi, threads=os.cpu_count() or 1,
+                            ctx=ctx)
+            walls.append(time.perf_counter() - t)
+        h2d1, d2h1 = ctx.transfer_bytes()
+        e2e = {"value": res.pairs / float(np.mean(walls)), "unit": UNIT,
+               "h2d_bytes_per_step": (h2d1 - h2d0) // args.e2e_steps,
+               "d2h_bytes_per_step": (d2h1 - d2h0) // args.e2e_steps,
+               "seconds_per_step": float(np.mean(walls)),
+               "factors": int(res.factorcount), "checksum": res.checksum_hex()}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        n = args.cpu_sample or auto_sample(wl)
+        rate, info = cpu_sample_run(wl, n)
+        cpu = {"value": rate, "unit": UNIT, "cores": info["cores"], "kind": "port",
+               "sample": "%d candidates from the bottom of the p range x all %d n (%.1f s)"
+                         % (info["cands"], wl["nmax"] - wl["nmin"], info["seconds"])}
+    ctx.close()
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_max / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "u32" if cls32 else "u64",
+            "data": "synthetic (deterministic search bounds, as the reference's CLI takes them)",
+            "config": {"workload": wl["desc"], "candidates_per_gpu": int(cands_per_step),
+                       "pairs_per_step": int(pairs_total // args.steps),
+                       "l2": "256 MB buffer overwritten before each step (candidate state < L2)",
+                       "parallelism": "p-range shards, one per GPU" if world > 1 else "1 GPU",
+                       "device": name, "sms": sms},
+            "roofline": {"bound": "int (IMAD pipe)", "achieved": achieved / 1e12, "peak": peak / 1e12,
+                         "unit": "Tops/s (32-bit integer multiply-add)", "frac": achieved / peak,
+                         "traffic": traffic, "kernel": "iterate_kernel<%s,%d>" % ("Cls32" if cls32 else "Cls64", mode),
+                         "kernel_ms_per_step": it_s * 1e3,
+                         "peak_source": "measured in this run (pfc_bench_int_peak, 32-bit IMAD chains)"},
+            "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(launches), "clocks": clocks,
+            "checksum_terms": "%016X" % termsum,
+        }
+        print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    wl = WORKLOADS[args.workload]
+    world, rank, local = dist_env()
+    dist = dist_init(world)
+    if args.impl == "reference":
+        run_reference(args, wl, world, rank)
+    else:
+        run_ours(args, wl, world, rank, local, dist)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

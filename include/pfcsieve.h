@@ -1,0 +1,201 @@
+/*
+ * pfcsieve.h -- C ABI of the GB300 (sm_103a) PFCSieve sieve path.
+ *
+ * This is the drop-in boundary between a host program (the pfcsieve CLI, a
+ * BOINC wrapper, Python via ctypes) and the CUDA kernels.  Plain C types and
+ * pointers only.  Every call returns PFC_OK (0) or a negative PFC_ERR_* code;
+ * nothing in the library calls exit().
+ *
+ * Ownership: the context owns all device memory and its CUDA stream; the
+ * caller owns every host buffer it passes (pointer + capacity).  One host
+ * thread per context.
+ *
+ * The reference (mfl0p/PFCSieve 1.4, OpenCL) has no library API: its host
+ * loop cl_sieve() (cl_sieve.cpp:1328-1761) binds OpenCL kernels by name and
+ * sets positional arguments.  Each entry point below names the reference code
+ * it replaces.
+ */
+#ifndef PFCSIEVE_H
+#define PFCSIEVE_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------- status codes */
+#define PFC_OK                 0
+#define PFC_ERR_ARG          (-1)  /* invalid argument (setupSearch checks, cl_sieve.cpp:600-641) */
+#define PFC_ERR_CUDA         (-2)  /* a CUDA runtime call failed */
+#define PFC_ERR_NOMEM        (-3)  /* allocation failed or the memory budget is exceeded */
+#define PFC_ERR_HIT_OVERFLOW (-4)  /* more hits than the caller's buffer holds */
+#define PFC_ERR_VALIDATION   (-5)  /* the n-counter check failed (kernels/check.cl:61-73) */
+#define PFC_ERR_VERIFY       (-6)  /* CPU re-verification of a factor failed (cl_sieve.cpp:515-529) */
+#define PFC_ERR_STATE        (-7)  /* call out of order (e.g. iterate before setup) */
+#define PFC_ERR_CAND_OVERFLOW (-8) /* candidate buffer overflow (cl_sieve.cpp:462-472) */
+#define PFC_ERR_NO_DEVICE    (-9)  /* no CUDA device, or not an sm_103 device */
+#define PFC_ERR_IO          (-10)  /* file I/O (factors file, checkpoint) */
+
+/* ------------------------------------------------------------------- modes */
+/* Mode bits; PFC_FACTORIAL | PFC_COMPOSITORIAL is the combined search
+ * (-! -c), every other combination except single bits is rejected
+ * (cl_sieve.cpp:600-617). */
+#define PFC_FACTORIAL     1u
+#define PFC_PRIMORIAL     2u
+#define PFC_COMPOSITORIAL 4u
+
+/* factor types in pfc_factor.type (cl_sieve.h:4-6) */
+#define PFC_TYPE_FACTORIAL     0
+#define PFC_TYPE_PRIMORIAL     1
+#define PFC_TYPE_COMPOSITORIAL 2
+
+/* One hit: p divides n!-1, n#-1 or n!/n#-1 when nc = -n, and the +1 form
+ * when nc = +n.  Same 16-byte layout as the reference `factor`
+ * (cl_sieve.h:8-12). */
+typedef struct {
+    uint64_t p;
+    int32_t nc;
+    int32_t type;
+} pfc_factor;
+
+typedef struct pfc_ctx pfc_ctx;
+typedef struct pfc_job pfc_job;
+
+/* ----------------------------------------------------------------- context */
+
+/* Select `device`, create the context's stream and its device buffers.
+ * `mem_budget` caps the device memory the context may hold (0 = 90% of free
+ * memory).  Replaces the OpenCL platform/context/queue set-up of main.cpp:
+ * 245-297 and the buffer creation of cl_sieve.cpp:1339-1350,1508-1519. */
+int pfc_ctx_create(int device, uint64_t mem_budget, pfc_ctx **out);
+
+/* Free everything the context owns (cleanup(), cl_sieve.cpp:77-103). */
+int pfc_ctx_destroy(pfc_ctx *ctx);
+
+/* The context's cudaStream_t (as void*), for callers that time the stages
+ * with CUDA events on the launching stream. */
+void *pfc_ctx_stream(pfc_ctx *ctx);
+
+/* Number of kernels this context has launched so far. */
+uint64_t pfc_ctx_launch_count(pfc_ctx *ctx);
+
+/* Bytes this context has copied host->device and device->host so far. */
+int pfc_ctx_transfer_bytes(pfc_ctx *ctx, uint64_t *h2d, uint64_t *d2h);
+
+/* Device name and SM count, for logs (main.cpp:299-335). */
+int pfc_ctx_device_info(pfc_ctx *ctx, char *name, size_t name_cap, int *sm_count);
+
+/* --------------------------------------------------------------------- job */
+
+/* Validate a search and build its host tables: the factorial power table,
+ * primorial and compositorial products and the prime lists of the n range
+ * (setupSearch cl_sieve.cpp:596-665; setupPowerTable :842-984;
+ * setupPrimeProducts :987-1148; setupCompositeProducts :1151-1326; prime list
+ * :1494-1499), and upload them.  Range rules are the CLI's: 3 <= pmin < pmax,
+ * 101 <= nmin < nmax < 2^31 (main.cpp:58-72). */
+int pfc_job_create(pfc_ctx *ctx, unsigned mode, uint32_t nmin, uint32_t nmax,
+                   uint64_t pmin, uint64_t pmax, pfc_job **out);
+int pfc_job_destroy(pfc_job *job);
+
+/* Suggest the end of the next p-segment starting at p_lo, sized to the
+ * device budget (profileGPU's range, cl_sieve.cpp:669-769). */
+int pfc_job_segment_end(pfc_job *job, uint64_t p_lo, uint64_t *p_hi);
+
+/* ---- stage calls: enqueue on the context stream for the current p-segment */
+
+/* Generate the candidate primes of [p_lo, p_hi): 3..113 and every base-2
+ * strong probable prime with no factor <= 113.  Resets the segment state.
+ * Replaces clearn + addsmallprimes + getsegprimes (cl_sieve.cpp:1572,
+ * 1598-1615; kernels/addsmallprimes.cl, kernels/getsegprimes.cl). */
+int pfc_gen_candidates(pfc_job *job, uint64_t p_lo, uint64_t p_hi);
+
+/* Starting residues (nmin-1)!, (nmin-1)#, (nmin-1)!/(nmin-1)# mod p for every
+ * candidate (the setup chunk loop cl_sieve.cpp:1655-1672; kernels/setup.cl). */
+int pfc_setup(pfc_job *job);
+
+/* Advance every candidate over n in [n_lo, n_hi) (primorial: over the primes
+ * in that range), appending hits.  Calls must cover [nmin, nmax) in order
+ * (the iterate chunk loop cl_sieve.cpp:1696-1719; kernels/iterate.cl). */
+int pfc_iterate(pfc_job *job, uint32_t n_lo, uint32_t n_hi);
+
+/* Fold the segment's checksum terms and candidate count into the job totals
+ * and run the n-counter check (kernels/check.cl; cl_sieve.cpp:1722). */
+int pfc_check(pfc_job *job);
+
+/* gen + setup + iterate over the whole n range (in launches of bounded
+ * length) + check for [p_lo, p_hi), enqueued on the context stream; grows the
+ * buffers and re-runs on candidate or hit buffer overflow.  Synchronises.
+ * The body of the reference's main loop, cl_sieve.cpp:1563-1726. */
+int pfc_segment(pfc_job *job, uint64_t p_lo, uint64_t p_hi);
+
+/* Wait for the context stream (waitOnEvent/sleepCPU, cl_sieve.cpp:248-365). */
+int pfc_sync(pfc_job *job);
+
+/* Copy the hits found since the last drain to `buf` (unsorted) and clear the
+ * device hit list.  *n receives the number of hits; if it exceeds cap, only
+ * cap are copied, nothing is cleared and PFC_ERR_HIT_OVERFLOW is returned
+ * (the factor read-back of getResults, cl_sieve.cpp:479-494). */
+int pfc_drain_hits(pfc_job *job, pfc_factor *buf, size_t cap, size_t *n);
+
+/* Totals over all checked segments: the wrapping 64-bit sum of the
+ * per-candidate checksum terms (kernels/check.cl:59,115,161) and the candidate
+ * count (cl_sieve.cpp:452-460).  Factor terms are added by
+ * pfc_finalize_factors. */
+int pfc_job_totals(pfc_job *job, uint64_t *term_checksum, uint64_t *primecount);
+
+/* Whole job [pmin, pmax) in segments; hits are drained into `buf` (capacity
+ * cap, *n receives the total).  Returns PFC_ERR_HIT_OVERFLOW with *n set when
+ * cap is too small (the caller re-runs with a larger buffer). */
+int pfc_job_run(pfc_job *job, pfc_factor *buf, size_t cap, size_t *n);
+
+/* Copy the current segment's candidates (class p < 2^32 first, then the
+ * rest) with their residues in the reference's representation, Montgomery
+ * with R = 2^64: s0 = the .s6 residue (factorial, primorial or compositorial),
+ * s1 = the combined search's compositorial residue (.s4).  For inspection and
+ * parity tests; synchronises.  Has no counterpart in the reference, whose
+ * records stay on the device (cl_sieve.h:25-35). */
+int pfc_segment_state(pfc_job *job, uint64_t *p, uint64_t *s0, uint64_t *s1, size_t cap, size_t *n);
+
+/* (p, n) pairs of all checked segments: candidates x (nmax - nmin). */
+uint64_t pfc_job_pairs(pfc_job *job);
+
+/* Multiplications per candidate of the setup programs (class p < 2^32 when
+ * cls64 = 0, else p >= 2^32), excluding the final correction. */
+uint64_t pfc_job_setup_mulmods(pfc_job *job, int cls64);
+
+/* ------------------------------------------------- host-side post-processing */
+
+/* Sort hits by (p, |n|, type), re-verify each on the CPU with naive products
+ * when `verify` is set (verifyprime.cpp:199-268, OpenMP with `threads`),
+ * drop hits whose p is not prime (7-base Miller-Rabin, verifyprime.cpp:
+ * 157-195) and add n+c of every kept factor to *checksum
+ * (cl_sieve.cpp:496-589).  Kept factors are compacted to the front of f;
+ * *kept receives their count. */
+int pfc_finalize_factors(unsigned mode, uint32_t nmax, pfc_factor *f, size_t n,
+                         int threads, int verify, size_t *kept, uint64_t *checksum);
+
+/* Deterministic primality for 64-bit p (verifyprime.cpp:157-195). */
+int pfc_is_prime(uint64_t p);
+
+/* Format one factor line as factors.txt holds it (cl_sieve.cpp:565-581);
+ * returns the length written (without NUL), or a negative code. */
+int pfc_format_factor(const pfc_factor *f, char *buf, size_t cap);
+
+/* ------------------------------------------------------------ measurement */
+
+/* Throughput of the integer pipes on `device`, in operations per second:
+ * variant 0 = 32-bit multiply-add (IMAD), 1 = 32-bit multiply-high,
+ * 2 = 32x32->64 multiply-add, 3 = 32-bit add/xor.  The roofline denominator
+ * for the sieve kernels, which are integer-multiply bound.  No counterpart
+ * in the reference. */
+int pfc_bench_int_peak(int device, int variant, double *ops_per_s);
+
+/* Static description of a status code. */
+const char *pfc_status_string(int status);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PFCSIEVE_H */

@@ -636,7 +636,7 @@ static int sieve_all(unsigned mode, uint32_t nmin, uint32_t nmax,
     {
         hitbuf_t hb = {0, 0, 0};
         uint64_t local = 0;
-#pragma omp for schedule(dynamic, 64)
+#pragma omp for schedule(dynamic, 8)
         for (uint64_t i = 0; i < ncand; ++i) {
             uint64_t st[3];
             uint64_t term = sieve_one(&pl, cands[i], &hb, st);

@@ -1,0 +1,312 @@
+"""pfcsieve_gb300 -- GB300-native (sm_103a) PFCSieve sieve path.
+
+Finds 64-bit primes p dividing n!+-1, n#+-1 or n!/n#+-1 for n in [nmin, nmax)
+and p in [pmin, pmax), with the reference's candidate rule, factor list and
+checksum.  This module is a thin ctypes binding over the C ABI in
+include/pfcsieve.h (libpfcsieve.so, built in-tree by pfcsieve_gb300/build.py).
+There is no CPU fallback: without the library or a GB300 every call raises.
+
+    import pfcsieve_gb300 as pfc
+    r = pfc.sieve(pfc.FACTORIAL, nmin=101, nmax=20000, pmin=10**7, pmax=11*10**6)
+    r.factorcount, r.primecount, r.checksum, r.factors
+
+`sieve()` follows the reference's cl_sieve() (cl_sieve.cpp:1328-1761): the
+p range is walked in segments, hits are drained, re-verified on the CPU,
+2-PRP factors are dropped and n+-1 of every kept factor joins the checksum.
+"""
+import ctypes
+import os
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import build as _build
+
+FACTORIAL, PRIMORIAL, COMPOSITORIAL = 1, 2, 4
+TYPE_FACTORIAL, TYPE_PRIMORIAL, TYPE_COMPOSITORIAL = 0, 1, 2
+FACTOR_DTYPE = np.dtype([("p", "<u8"), ("nc", "<i4"), ("type", "<i4")])
+
+PFC_OK = 0
+PFC_ERR_HIT_OVERFLOW = -4
+PFC_ERR_NO_DEVICE = -9
+
+LIB_PATH = _build.LIB
+
+
+class PFCError(RuntimeError):
+    def __init__(self, code, where=""):
+        self.code = code
+        super().__init__("%s: %s (%d)" % (where, status_string(code), code))
+
+
+_lib = None
+
+
+def lib():
+    """Load libpfcsieve.so (raises if it has not been built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError("libpfcsieve.so not built: run pfcsieve_gb300.build.build() "
+                              "(or __graft_entry__.build())")
+        L = ctypes.CDLL(LIB_PATH)
+        u64, u32, i32, vp, sz = (ctypes.c_uint64, ctypes.c_uint32, ctypes.c_int32,
+                                 ctypes.c_void_p, ctypes.c_size_t)
+        P = ctypes.POINTER
+        sig = {
+            "pfc_ctx_create": (ctypes.c_int, [ctypes.c_int, u64, P(vp)]),
+            "pfc_ctx_destroy": (ctypes.c_int, [vp]),
+            "pfc_ctx_stream": (vp, [vp]),
+            "pfc_ctx_launch_count": (u64, [vp]),
+            "pfc_ctx_transfer_bytes": (ctypes.c_int, [vp, P(u64), P(u64)]),
+            "pfc_ctx_device_info": (ctypes.c_int, [vp, ctypes.c_char_p, sz, P(ctypes.c_int)]),
+            "pfc_job_create": (ctypes.c_int, [vp, ctypes.c_uint, u32, u32, u64, u64, P(vp)]),
+            "pfc_job_destroy": (ctypes.c_int, [vp]),
+            "pfc_job_segment_end": (ctypes.c_int, [vp, u64, P(u64)]),
+            "pfc_gen_candidates": (ctypes.c_int, [vp, u64, u64]),
+            "pfc_setup": (ctypes.c_int, [vp]),
+            "pfc_iterate": (ctypes.c_int, [vp, u32, u32]),
+            "pfc_check": (ctypes.c_int, [vp]),
+            "pfc_segment": (ctypes.c_int, [vp, u64, u64]),
+            "pfc_sync": (ctypes.c_int, [vp]),
+            "pfc_drain_hits": (ctypes.c_int, [vp, vp, sz, P(sz)]),
+            "pfc_job_totals": (ctypes.c_int, [vp, P(u64), P(u64)]),
+            "pfc_job_run": (ctypes.c_int, [vp, vp, sz, P(sz)]),
+            "pfc_segment_state": (ctypes.c_int, [vp, vp, vp, vp, sz, P(sz)]),
+            "pfc_job_pairs": (u64, [vp]),
+            "pfc_job_setup_mulmods": (u64, [vp, ctypes.c_int]),
+            "pfc_finalize_factors": (ctypes.c_int, [ctypes.c_uint, u32, vp, sz, ctypes.c_int,
+                                                    ctypes.c_int, P(sz), P(u64)]),
+            "pfc_is_prime": (ctypes.c_int, [u64]),
+            "pfc_format_factor": (ctypes.c_int, [vp, ctypes.c_char_p, sz]),
+            "pfc_status_string": (ctypes.c_char_p, [ctypes.c_int]),
+            "pfc_bench_int_peak": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, P(ctypes.c_double)]),
+        }
+        for name, (res, args) in sig.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib
+
+
+def status_string(code):
+    return lib().pfc_status_string(code).decode()
+
+
+def _ck(code, where):
+    if code != PFC_OK:
+        raise PFCError(code, where)
+
+
+class Context:
+    """One GPU, one stream, a device-memory budget (pfc_ctx_create)."""
+
+    def __init__(self, device=0, budget=0):
+        self.h = ctypes.c_void_p()
+        _ck(lib().pfc_ctx_create(device, budget, ctypes.byref(self.h)), "pfc_ctx_create")
+
+    def close(self):
+        if self.h:
+            lib().pfc_ctx_destroy(self.h)
+            self.h = ctypes.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def stream(self):
+        """cudaStream_t of the context, as an integer."""
+        return lib().pfc_ctx_stream(self.h) or 0
+
+    @property
+    def launches(self):
+        return lib().pfc_ctx_launch_count(self.h)
+
+    def transfer_bytes(self):
+        """(host->device, device->host) bytes copied so far."""
+        a, b = ctypes.c_uint64(0), ctypes.c_uint64(0)
+        _ck(lib().pfc_ctx_transfer_bytes(self.h, ctypes.byref(a), ctypes.byref(b)), "transfer_bytes")
+        return a.value, b.value
+
+    def device_info(self):
+        buf = ctypes.create_string_buffer(256)
+        sms = ctypes.c_int(0)
+        _ck(lib().pfc_ctx_device_info(self.h, buf, 256, ctypes.byref(sms)), "device_info")
+        return buf.value.decode(), sms.value
+
+
+class Job:
+    """One search (mode, [nmin, nmax), [pmin, pmax)); see include/pfcsieve.h."""
+
+    def __init__(self, ctx, mode, nmin, nmax, pmin, pmax):
+        self.ctx = ctx
+        self.mode, self.nmin, self.nmax, self.pmin, self.pmax = mode, nmin, nmax, pmin, pmax
+        self.h = ctypes.c_void_p()
+        _ck(lib().pfc_job_create(ctx.h, mode, nmin, nmax, pmin, pmax, ctypes.byref(self.h)),
+            "pfc_job_create")
+
+    def close(self):
+        if self.h:
+            lib().pfc_job_destroy(self.h)
+            self.h = ctypes.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # stage calls
+    def gen(self, lo, hi):
+        _ck(lib().pfc_gen_candidates(self.h, lo, hi), "pfc_gen_candidates")
+
+    def setup(self):
+        _ck(lib().pfc_setup(self.h), "pfc_setup")
+
+    def iterate(self, lo, hi):
+        _ck(lib().pfc_iterate(self.h, lo, hi), "pfc_iterate")
+
+    def check(self):
+        _ck(lib().pfc_check(self.h), "pfc_check")
+
+    def segment(self, lo, hi):
+        _ck(lib().pfc_segment(self.h, lo, hi), "pfc_segment")
+
+    def segment_end(self, lo):
+        hi = ctypes.c_uint64(0)
+        _ck(lib().pfc_job_segment_end(self.h, lo, ctypes.byref(hi)), "pfc_job_segment_end")
+        return hi.value
+
+    def sync(self):
+        _ck(lib().pfc_sync(self.h), "pfc_sync")
+
+    def drain_hits(self):
+        n = ctypes.c_size_t(0)
+        cap = 1 << 16
+        while True:
+            buf = np.zeros(cap, dtype=FACTOR_DTYPE)
+            rc = lib().pfc_drain_hits(self.h, buf.ctypes.data, cap, ctypes.byref(n))
+            if rc == PFC_ERR_HIT_OVERFLOW and n.value > cap:
+                cap = n.value
+                continue
+            _ck(rc, "pfc_drain_hits")
+            return buf[: n.value]
+
+    def totals(self):
+        t, c = ctypes.c_uint64(0), ctypes.c_uint64(0)
+        _ck(lib().pfc_job_totals(self.h, ctypes.byref(t), ctypes.byref(c)), "pfc_job_totals")
+        return t.value, c.value
+
+    def run(self, cap=1 << 20):
+        """Whole p range; returns the raw hits (unsorted)."""
+        while True:
+            buf = np.zeros(max(cap, 1), dtype=FACTOR_DTYPE)
+            n = ctypes.c_size_t(0)
+            rc = lib().pfc_job_run(self.h, buf.ctypes.data, cap, ctypes.byref(n))
+            if rc == PFC_ERR_HIT_OVERFLOW:
+                raise PFCError(rc, "pfc_job_run: %d hits do not fit %d; rerun with cap=%d"
+                               % (n.value, cap, n.value))
+            _ck(rc, "pfc_job_run")
+            return buf[: n.value]
+
+    def segment_state(self):
+        """(p, s0, s1) of the current segment in the reference's R = 2^64 form."""
+        n = ctypes.c_size_t(0)
+        rc = lib().pfc_segment_state(self.h, None, None, None, 0, ctypes.byref(n))
+        if rc not in (PFC_OK, -1):
+            _ck(rc, "pfc_segment_state")
+        cap = n.value
+        p = np.zeros(max(cap, 1), dtype=np.uint64)
+        s0 = np.zeros_like(p)
+        s1 = np.zeros_like(p)
+        _ck(lib().pfc_segment_state(self.h, p.ctypes.data, s0.ctypes.data, s1.ctypes.data, cap,
+                                    ctypes.byref(n)), "pfc_segment_state")
+        return p[: n.value], s0[: n.value], s1[: n.value]
+
+    @property
+    def pairs(self):
+        return lib().pfc_job_pairs(self.h)
+
+    def setup_mulmods(self, cls64):
+        return lib().pfc_job_setup_mulmods(self.h, int(cls64))
+
+
+def finalize(mode, nmax, hits, threads=2, verify=True):
+    """Sort, re-verify, drop 2-PRP p and fold n+-1 (cl_sieve.cpp:496-589).
+
+    Returns (kept factors sorted by (p, |n|, type), checksum addend)."""
+    f = np.ascontiguousarray(hits, dtype=FACTOR_DTYPE).copy()
+    kept = ctypes.c_size_t(0)
+    add = ctypes.c_uint64(0)
+    _ck(lib().pfc_finalize_factors(mode, nmax, f.ctypes.data if len(f) else None, len(f), threads,
+                                   int(bool(verify)), ctypes.byref(kept), ctypes.byref(add)),
+        "pfc_finalize_factors")
+    return f[: kept.value], add.value
+
+
+def int_peak(device=0, variant=0):
+    """Measured integer-pipe throughput in ops/s (see pfc_bench_int_peak)."""
+    v = ctypes.c_double(0)
+    _ck(lib().pfc_bench_int_peak(device, variant, ctypes.byref(v)), "pfc_bench_int_peak")
+    return v.value
+
+
+def is_prime(p):
+    return bool(lib().pfc_is_prime(int(p)))
+
+
+def format_factor(f):
+    a = np.zeros(1, dtype=FACTOR_DTYPE)
+    a[0] = f
+    buf = ctypes.create_string_buffer(96)
+    n = lib().pfc_format_factor(a.ctypes.data, buf, 96)
+    if n < 0:
+        raise PFCError(n, "pfc_format_factor")
+    return buf.value.decode()
+
+
+@dataclass
+class SieveResult:
+    factorcount: int
+    primecount: int
+    checksum: int
+    pairs: int
+    factors: np.ndarray = field(repr=False)
+    hits: int = 0
+
+    def checksum_hex(self):
+        return "%016X" % self.checksum
+
+
+def sieve(mode, nmin, nmax, pmin, pmax, device=0, threads=2, verify=True, ctx=None):
+    """One complete search, as the reference's cl_sieve() runs it."""
+    own = ctx is None
+    ctx = ctx or Context(device)
+    try:
+        with Job(ctx, mode, nmin, nmax, pmin, pmax) as job:
+            hits = job.run()
+            termsum, primecount = job.totals()
+            pairs = job.pairs
+        kept, add = finalize(mode, nmax, hits, threads=threads, verify=verify)
+        return SieveResult(factorcount=len(kept), primecount=primecount,
+                           checksum=(termsum + add) & 0xFFFFFFFFFFFFFFFF, pairs=pairs,
+                           factors=kept, hits=len(hits))
+    finally:
+        if own:
+            ctx.close()

@@ -1,0 +1,714 @@
+// api.cu -- C ABI implementation (include/pfcsieve.h): context, job tables,
+// stage calls and the segment driver.
+//
+// Device memory of a job (all owned by the context budget):
+//   class-32 candidates: p, s0, s1 (u32) and nnext (u32)   16 B / candidate
+//   class-64 candidates: p, s0, s1 (u64) and nnext (u32)   28 B / candidate
+//   hit list pfc_factor[hitcap] + 64-bit counter
+//   setup programs (u32 and u64 words), prime flags of [nmin, nmax) (1 bit per
+//   n) or the prime list of [nmin, nmax) for the primorial walk
+//   per-segment accumulators: counts[2], termsum, flags
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include "host.hpp"
+#include "kernels.cuh"
+#include "pfcsieve.h"
+
+using namespace pfc;
+
+struct pfc_ctx {
+    int device = 0;
+    cudaStream_t st = nullptr;
+    int sms = 0;
+    char name[256] = {0};
+    uint64_t budget = 0, used = 0;
+    uint64_t launches = 0;
+    uint64_t h2d = 0, d2h = 0;   // bytes copied by this context
+    uint64_t *d_pat = nullptr;
+};
+
+namespace {
+
+cudaError_t dalloc_bytes(pfc_ctx *c, void **p, size_t bytes) {
+    *p = nullptr;
+    if (bytes == 0) return cudaSuccess;
+    if (c->used + bytes > c->budget) return cudaErrorMemoryAllocation;
+    cudaError_t e = cudaMalloc(p, bytes);
+    if (e == cudaSuccess) c->used += bytes;
+    return e;
+}
+
+template <class T>
+struct DArr {
+    T *p = nullptr;
+    size_t n = 0;
+    cudaError_t alloc(pfc_ctx *c, size_t count) {
+        release(c);
+        cudaError_t e = dalloc_bytes(c, (void **)&p, count * sizeof(T));
+        if (e == cudaSuccess) n = count;
+        return e;
+    }
+    cudaError_t upload(pfc_ctx *c, const std::vector<T> &v) {
+        cudaError_t e = alloc(c, std::max<size_t>(v.size(), 1));
+        if (e != cudaSuccess) return e;
+        if (v.empty()) return cudaMemsetAsync(p, 0, sizeof(T), c->st);
+        c->h2d += v.size() * sizeof(T);
+        return cudaMemcpyAsync(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, c->st);
+    }
+    void release(pfc_ctx *c) {
+        if (p) {
+            cudaFree(p);
+            c->used -= n * sizeof(T);
+        }
+        p = nullptr;
+        n = 0;
+    }
+};
+
+template <class W>
+struct DevProg {
+    DArr<W> words;
+    DArr<uint32_t> groups;
+    Prog<W> view{};
+    cudaError_t upload(pfc_ctx *c, const HostProg<W> &h) {
+        cudaError_t e = words.upload(c, h.words);
+        if (e == cudaSuccess) e = groups.upload(c, h.groups);
+        view.words = words.p;
+        view.groups = groups.p;
+        view.ngroups = (uint32_t)(h.groups.size() / 3);
+        view.final_sq = h.final_sq;
+        view.corr = h.corr;
+        return e;
+    }
+    void release(pfc_ctx *c) {
+        words.release(c);
+        groups.release(c);
+    }
+};
+
+template <class W>
+struct DevClass {
+    DArr<W> p, s0, s1;
+    DArr<uint32_t> nnext;
+    uint32_t cap = 0;
+    cudaError_t ensure(pfc_ctx *c, uint32_t want) {
+        if (want <= cap && p.p) return cudaSuccess;
+        release(c);
+        const size_t n = std::max<uint32_t>(want, 256);
+        cudaError_t e = p.alloc(c, n);
+        if (e == cudaSuccess) e = s0.alloc(c, n);
+        if (e == cudaSuccess) e = s1.alloc(c, n);
+        if (e == cudaSuccess) e = nnext.alloc(c, n);
+        if (e == cudaSuccess) cap = (uint32_t)n;
+        return e;
+    }
+    void release(pfc_ctx *c) {
+        p.release(c);
+        s0.release(c);
+        s1.release(c);
+        nnext.release(c);
+        cap = 0;
+    }
+    ClassBuf<W> view(const uint32_t *count) const {
+        ClassBuf<W> b;
+        b.p = p.p;
+        b.s0 = s0.p;
+        b.s1 = s1.p;
+        b.nnext = nnext.p;
+        b.cap = cap;
+        b.count = count;
+        return b;
+    }
+};
+
+// small per-segment read-back block (pinned host mirror)
+struct SegStats {
+    uint32_t counts[2];
+    uint32_t flags;
+    uint32_t pad;
+    unsigned long long termsum;
+    unsigned long long hits;
+};
+
+}  // namespace
+
+struct pfc_job {
+    pfc_ctx *ctx = nullptr;
+    unsigned mode = 0;
+    uint32_t nmin = 0, nmax = 0;
+    uint64_t pmin = 0, pmax = 0;
+
+    DevProg<uint32_t> a32, b32;
+    DevProg<uint64_t> a64, b64;
+    uint64_t setup_mulmods32 = 0, setup_mulmods64 = 0;
+    DArr<uint32_t> primebits;
+    DArr<uint32_t> qlist;
+    std::vector<uint32_t> h_qlist;
+
+    DevClass<uint32_t> c32;
+    DevClass<uint64_t> c64;
+    DArr<pfc_factor> hits;
+    DArr<SegStats> stats;       // device copy of SegStats
+    SegStats *h_stats = nullptr;  // pinned
+
+    uint64_t termsum = 0, primecount = 0;
+    int stage = 0;              // 0 idle, 1 generated, 2 set up, 3 checked
+    uint32_t next_it = 0;       // next n (or prime index) for pfc_iterate
+    uint64_t seg_lo = 0, seg_hi = 0;
+    uint64_t pairs = 0;
+};
+
+// ------------------------------------------------------------------ helpers
+
+static int cuda_fail(cudaError_t e) {
+    if (e == cudaErrorMemoryAllocation) return PFC_ERR_NOMEM;
+    return e == cudaSuccess ? PFC_OK : PFC_ERR_CUDA;
+}
+#define CK(x)                                    \
+    do {                                         \
+        cudaError_t e_ = (x);                    \
+        if (e_ != cudaSuccess) return cuda_fail(e_); \
+    } while (0)
+
+static uint32_t* counts_ptr(pfc_job *j) { return &j->stats.p->counts[0]; }
+
+static unsigned long long *hitcount_ptr(pfc_job *j) { return &j->stats.p->hits; }
+
+static uint32_t iter_end(const pfc_job *j) {
+    return j->mode == PFC_PRIMORIAL ? (uint32_t)j->h_qlist.size() : j->nmax;
+}
+static uint32_t iter_begin(const pfc_job *j) { return j->mode == PFC_PRIMORIAL ? 0u : j->nmin; }
+
+// expected candidates in [lo, hi) (an over-estimate: density 1/ln x falls)
+static double est_cands(uint64_t lo, uint64_t hi) {
+    if (hi <= lo) return 0;
+    const double a = (double)std::max<uint64_t>(lo, 114);
+    return (double)(hi - lo) / std::log(a) * 1.25 + 30.0;
+}
+
+// ----------------------------------------------------------------- context
+
+extern "C" int pfc_ctx_create(int device, uint64_t mem_budget, pfc_ctx **out) {
+    if (!out) return PFC_ERR_ARG;
+    *out = nullptr;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= device || device < 0) return PFC_ERR_NO_DEVICE;
+    cudaDeviceProp prop;
+    CK(cudaGetDeviceProperties(&prop, device));
+    if (prop.major != 10 || prop.minor != 3) return PFC_ERR_NO_DEVICE;  // kernels are built for sm_103a only
+    CK(cudaSetDevice(device));
+    pfc_ctx *c = new (std::nothrow) pfc_ctx();
+    if (!c) return PFC_ERR_NOMEM;
+    c->device = device;
+    c->sms = prop.multiProcessorCount;
+    snprintf(c->name, sizeof(c->name), "%s", prop.name);
+    size_t fr = 0, tot = 0;
+    cudaMemGetInfo(&fr, &tot);
+    c->budget = mem_budget ? mem_budget : (uint64_t)(0.9 * (double)fr);
+    cudaError_t e = cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = dalloc_bytes(c, (void **)&c->d_pat, kPatEntries * sizeof(uint64_t));
+    if (e == cudaSuccess) {
+        std::vector<uint64_t> pat(kPatEntries);
+        uint32_t pr[kSmallPrimes];
+        build_pattern_table(pat.data(), pr);
+        e = cudaMemcpy(c->d_pat, pat.data(), pat.size() * sizeof(uint64_t), cudaMemcpyHostToDevice);
+    }
+    if (e != cudaSuccess) {
+        pfc_ctx_destroy(c);
+        return cuda_fail(e);
+    }
+    *out = c;
+    return PFC_OK;
+}
+
+extern "C" int pfc_ctx_destroy(pfc_ctx *c) {
+    if (!c) return PFC_ERR_ARG;
+    cudaSetDevice(c->device);
+    if (c->st) cudaStreamSynchronize(c->st);
+    if (c->d_pat) cudaFree(c->d_pat);
+    if (c->st) cudaStreamDestroy(c->st);
+    delete c;
+    return PFC_OK;
+}
+
+extern "C" void *pfc_ctx_stream(pfc_ctx *c) { return c ? (void *)c->st : nullptr; }
+
+extern "C" uint64_t pfc_ctx_launch_count(pfc_ctx *c) { return c ? c->launches : 0; }
+
+extern "C" int pfc_ctx_transfer_bytes(pfc_ctx *c, uint64_t *h2d, uint64_t *d2h) {
+    if (!c) return PFC_ERR_ARG;
+    if (h2d) *h2d = c->h2d;
+    if (d2h) *d2h = c->d2h;
+    return PFC_OK;
+}
+
+extern "C" int pfc_ctx_device_info(pfc_ctx *c, char *name, size_t cap, int *sms) {
+    if (!c) return PFC_ERR_ARG;
+    if (name && cap) snprintf(name, cap, "%s", c->name);
+    if (sms) *sms = c->sms;
+    return PFC_OK;
+}
+
+// --------------------------------------------------------------------- job
+
+static int job_release(pfc_job *j) {
+    pfc_ctx *c = j->ctx;
+    cudaSetDevice(c->device);
+    cudaStreamSynchronize(c->st);
+    j->a32.release(c);
+    j->b32.release(c);
+    j->a64.release(c);
+    j->b64.release(c);
+    j->primebits.release(c);
+    j->qlist.release(c);
+    j->c32.release(c);
+    j->c64.release(c);
+    j->hits.release(c);
+    j->stats.release(c);
+    if (j->h_stats) cudaFreeHost(j->h_stats);
+    j->h_stats = nullptr;
+    return PFC_OK;
+}
+
+extern "C" int pfc_job_create(pfc_ctx *c, unsigned mode, uint32_t nmin, uint32_t nmax, uint64_t pmin,
+                              uint64_t pmax, pfc_job **out) {
+    if (!c || !out) return PFC_ERR_ARG;
+    *out = nullptr;
+    // setupSearch (cl_sieve.cpp:600-641) and the CLI ranges (main.cpp:58-72)
+    const bool valid_mode = mode == PFC_FACTORIAL || mode == PFC_PRIMORIAL || mode == PFC_COMPOSITORIAL ||
+                            mode == (PFC_FACTORIAL | PFC_COMPOSITORIAL);
+    if (!valid_mode) return PFC_ERR_ARG;
+    if (pmin < 3 || pmax <= pmin) return PFC_ERR_ARG;
+    if (nmin < 101 || nmax <= nmin || nmax > 0x7FFFFFFFu) return PFC_ERR_ARG;
+    CK(cudaSetDevice(c->device));
+    pfc_job *j = new (std::nothrow) pfc_job();
+    if (!j) return PFC_ERR_NOMEM;
+    j->ctx = c;
+    j->mode = mode;
+    j->nmin = nmin;
+    j->nmax = nmax;
+    j->pmin = pmin;
+    j->pmax = pmax;
+
+    const uint32_t startN = nmin - 1;
+    const uint32_t plim = (mode & PFC_COMPOSITORIAL) ? nmax : std::max(startN, nmax - 1);
+    const std::vector<uint32_t> primes = primes_between(2, plim);
+    const std::vector<uint32_t> below(primes.begin(), std::upper_bound(primes.begin(), primes.end(), startN));
+    HostProg<uint32_t> a32, b32;
+    HostProg<uint64_t> a64, b64;
+    bool ok = true;
+    if (mode == PFC_FACTORIAL) {
+        ok = build_power_prog(startN, 0, primes, a32) && build_power_prog(startN, 0, primes, a64);
+    } else if (mode == PFC_COMPOSITORIAL) {
+        ok = build_power_prog(startN, 1, primes, a32) && build_power_prog(startN, 1, primes, a64);
+    } else if (mode == PFC_PRIMORIAL) {
+        ok = build_product_prog(below, a32) && build_product_prog(below, a64);
+    } else {
+        ok = build_power_prog(startN, 1, primes, a32) && build_power_prog(startN, 1, primes, a64) &&
+             build_product_prog(below, b32) && build_product_prog(below, b64);
+    }
+    if (!ok) {
+        delete j;
+        return PFC_ERR_ARG;
+    }
+    j->setup_mulmods32 = a32.mulmods() + b32.mulmods();
+    j->setup_mulmods64 = a64.mulmods() + b64.mulmods();
+
+    cudaError_t e = j->a32.upload(c, a32);
+    if (e == cudaSuccess) e = j->a64.upload(c, a64);
+    if (e == cudaSuccess) e = j->b32.upload(c, b32);
+    if (e == cudaSuccess) e = j->b64.upload(c, b64);
+    if (e == cudaSuccess && (mode & PFC_COMPOSITORIAL)) e = j->primebits.upload(c, prime_bitmap(nmin, nmax, primes));
+    if (e == cudaSuccess && mode == PFC_PRIMORIAL) {
+        auto lo = std::lower_bound(primes.begin(), primes.end(), nmin);
+        auto hi = std::lower_bound(primes.begin(), primes.end(), nmax);
+        j->h_qlist.assign(lo, hi);
+        std::vector<uint32_t> padded = j->h_qlist;
+        padded.resize(padded.size() + 32, 1u);
+        e = j->qlist.upload(c, padded);
+    }
+    if (e == cudaSuccess) e = j->stats.alloc(c, 1);
+    if (e == cudaSuccess) e = cudaMemsetAsync(j->stats.p, 0, sizeof(SegStats), c->st);
+    if (e == cudaSuccess) e = cudaMallocHost((void **)&j->h_stats, sizeof(SegStats));
+    if (e == cudaSuccess) e = j->hits.alloc(c, 1u << 20);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->st);
+    if (e != cudaSuccess) {
+        job_release(j);
+        delete j;
+        return cuda_fail(e);
+    }
+    *out = j;
+    return PFC_OK;
+}
+
+extern "C" int pfc_job_destroy(pfc_job *j) {
+    if (!j) return PFC_ERR_ARG;
+    job_release(j);
+    delete j;
+    return PFC_OK;
+}
+
+extern "C" int pfc_job_segment_end(pfc_job *j, uint64_t p_lo, uint64_t *p_hi) {
+    if (!j || !p_hi || p_lo < j->pmin || p_lo >= j->pmax) return PFC_ERR_ARG;
+    // candidates per segment: bounded by a quarter of the budget at 28 B each
+    // and by 2^26
+    const double maxc = std::min<double>((double)(1u << 26), (double)j->ctx->budget / 4.0 / 28.0);
+    const double ln = std::log((double)std::max<uint64_t>(p_lo, 114));
+    const double span = maxc * ln * 0.75;
+    uint64_t hi = (span >= (double)(j->pmax - p_lo)) ? j->pmax : p_lo + (uint64_t)span;
+    if (hi <= p_lo) hi = std::min(j->pmax, p_lo + 1);
+    *p_hi = hi;
+    return PFC_OK;
+}
+
+// ------------------------------------------------------------- stage calls
+
+static int ensure_class_caps(pfc_job *j, uint64_t lo, uint64_t hi) {
+    const uint64_t split = 1ull << 32;
+    const double e32 = est_cands(lo, std::min(hi, split));
+    const double e64 = est_cands(std::max(lo, split), hi);
+    const double lim = 4.0e9;
+    if (e32 > lim || e64 > lim) return PFC_ERR_NOMEM;
+    CK(j->c32.ensure(j->ctx, lo < split ? (uint32_t)e32 : 0u));
+    CK(j->c64.ensure(j->ctx, hi > split ? (uint32_t)e64 : 0u));
+    return PFC_OK;
+}
+
+static int enqueue_gen(pfc_job *j, uint64_t lo, uint64_t hi) {
+    pfc_ctx *c = j->ctx;
+    CK(cudaMemsetAsync(counts_ptr(j), 0, 2 * sizeof(uint32_t), c->st));
+    GenArgs g;
+    memset(&g, 0, sizeof(g));
+    const uint64_t base = lo | 1;
+    g.base = base;
+    g.nodd = hi > base ? (hi - base + 1) / 2 : 0;
+    g.p32 = j->c32.p.p;
+    g.p64 = j->c64.p.p;
+    g.cap32 = j->c32.p.p ? j->c32.cap : 0;
+    g.cap64 = j->c64.p.p ? j->c64.cap : 0;
+    g.count = counts_ptr(j);
+    g.pat = c->d_pat;
+    static const uint32_t sp[kSmallPrimes] = {3,  5,  7,  11, 13, 17, 19, 23, 29, 31, 37,  41,  43,  47,  53,
+                                              59, 61, 67, 71, 73, 79, 83, 89, 97, 101, 103, 107, 109, 113};
+    for (int k = 0; k < kSmallPrimes; ++k) g.bmod[k] = (uint32_t)(base % sp[k]);
+    c->launches += launch_gen(g, c->sms, c->st);
+    CK(cudaGetLastError());
+    j->seg_lo = lo;
+    j->seg_hi = hi;
+    j->stage = 1;
+    return PFC_OK;
+}
+
+extern "C" int pfc_gen_candidates(pfc_job *j, uint64_t p_lo, uint64_t p_hi) {
+    if (!j || p_lo < j->pmin || p_hi > j->pmax || p_hi <= p_lo) return PFC_ERR_ARG;
+    CK(cudaSetDevice(j->ctx->device));
+    int rc = ensure_class_caps(j, p_lo, p_hi);
+    if (rc) return rc;
+    return enqueue_gen(j, p_lo, p_hi);
+}
+
+static int enqueue_setup(pfc_job *j) {
+    pfc_ctx *c = j->ctx;
+    SetupArgs<uint32_t> s32;
+    s32.mode = j->mode;
+    s32.a = j->a32.view;
+    s32.b = j->b32.view;
+    s32.nnext0 = iter_begin(j);
+    SetupArgs<uint64_t> s64;
+    s64.mode = j->mode;
+    s64.a = j->a64.view;
+    s64.b = j->b64.view;
+    s64.nnext0 = iter_begin(j);
+    if (j->c32.p.p) c->launches += launch_setup32(j->c32.view(counts_ptr(j)), s32, c->st);
+    if (j->c64.p.p) c->launches += launch_setup64(j->c64.view(counts_ptr(j) + 1), s64, c->st);
+    CK(cudaGetLastError());
+    j->stage = 2;
+    j->next_it = iter_begin(j);
+    return PFC_OK;
+}
+
+extern "C" int pfc_setup(pfc_job *j) {
+    if (!j) return PFC_ERR_ARG;
+    if (j->stage < 1) return PFC_ERR_STATE;
+    CK(cudaSetDevice(j->ctx->device));
+    return enqueue_setup(j);
+}
+
+static HitBuf hitbuf(pfc_job *j) {
+    HitBuf h;
+    h.buf = j->hits.p;
+    h.count = hitcount_ptr(j);
+    h.cap = j->hits.n;
+    return h;
+}
+
+// one iterate launch per class over [lo, hi) (n values or prime indices)
+static int enqueue_iter_range(pfc_job *j, uint32_t lo, uint32_t hi) {
+    pfc_ctx *c = j->ctx;
+    IterArgs a;
+    a.mode = j->mode;
+    a.nmin = j->nmin;
+    a.lo = lo;
+    a.hi = hi;
+    a.primebits = j->primebits.p;
+    a.qlist = j->qlist.p;
+    const HitBuf h = hitbuf(j);
+    if (j->c32.p.p) c->launches += launch_iterate32(j->c32.view(counts_ptr(j)), a, h, c->st);
+    if (j->c64.p.p) c->launches += launch_iterate64(j->c64.view(counts_ptr(j) + 1), a, h, c->st);
+    CK(cudaGetLastError());
+    return PFC_OK;
+}
+
+// chunk length so one launch covers about `budget` candidate-steps
+static uint32_t chunk_len(uint64_t count, double budget) {
+    double L = budget / (double)std::max<uint64_t>(count, 1);
+    L = std::max(16.0, std::min(L, 2147483648.0));
+    return ((uint32_t)L + 15u) & ~15u;
+}
+
+// [lo, hi) in launches of about 1.5e11 candidate-steps (class-64 steps
+// weigh 3), so no launch runs for more than a fraction of a second
+static int enqueue_iter_chunked(pfc_job *j, uint32_t lo, uint32_t hi, uint64_t n32, uint64_t n64) {
+    const uint32_t L = chunk_len(n32 + 3 * n64, 1.5e11);
+    while (lo < hi) {
+        const uint32_t e = (uint32_t)std::min<uint64_t>((uint64_t)lo + L, hi);
+        int rc = enqueue_iter_range(j, lo, e);
+        if (rc) return rc;
+        lo = e;
+    }
+    return PFC_OK;
+}
+
+extern "C" int pfc_iterate(pfc_job *j, uint32_t n_lo, uint32_t n_hi) {
+    if (!j || n_hi < n_lo) return PFC_ERR_ARG;
+    if (j->stage < 2) return PFC_ERR_STATE;
+    CK(cudaSetDevice(j->ctx->device));
+    uint32_t lo = n_lo, hi = n_hi;
+    if (j->mode == PFC_PRIMORIAL) {   // n range -> prime index range
+        lo = (uint32_t)(std::lower_bound(j->h_qlist.begin(), j->h_qlist.end(), n_lo) - j->h_qlist.begin());
+        hi = (uint32_t)(std::lower_bound(j->h_qlist.begin(), j->h_qlist.end(), n_hi) - j->h_qlist.begin());
+        if (n_lo <= j->nmin) lo = 0;
+        if (n_hi >= j->nmax) hi = (uint32_t)j->h_qlist.size();
+    }
+    if (lo != j->next_it || hi > iter_end(j)) return PFC_ERR_STATE;
+    if (hi == lo) return PFC_OK;
+    int rc = enqueue_iter_chunked(j, lo, hi, j->c32.cap, j->c64.cap);
+    if (rc) return rc;
+    j->next_it = hi;
+    return PFC_OK;
+}
+
+static int enqueue_check(pfc_job *j) {
+    pfc_ctx *c = j->ctx;
+    CheckArgs a;
+    a.mode = j->mode;
+    a.nlast = j->nmax - 1;
+    a.nend = iter_end(j);
+    a.termsum = &j->stats.p->termsum;
+    a.flags = &j->stats.p->flags;
+    if (j->c32.p.p) c->launches += launch_check32(j->c32.view(counts_ptr(j)), a, c->st);
+    if (j->c64.p.p) c->launches += launch_check64(j->c64.view(counts_ptr(j) + 1), a, c->st);
+    CK(cudaGetLastError());
+    return PFC_OK;
+}
+
+static int read_stats(pfc_job *j) {
+    j->ctx->d2h += sizeof(SegStats);
+    CK(cudaMemcpyAsync(j->h_stats, j->stats.p, sizeof(SegStats), cudaMemcpyDeviceToHost, j->ctx->st));
+    CK(cudaStreamSynchronize(j->ctx->st));
+    return PFC_OK;
+}
+
+// fold the checked segment into the job totals
+static int commit_segment(pfc_job *j) {
+    const SegStats &s = *j->h_stats;
+    if (s.counts[0] > j->c32.cap && j->c32.p.p) return PFC_ERR_CAND_OVERFLOW;
+    if (s.counts[1] > j->c64.cap && j->c64.p.p) return PFC_ERR_CAND_OVERFLOW;
+    if ((!j->c32.p.p && s.counts[0]) || (!j->c64.p.p && s.counts[1])) return PFC_ERR_CAND_OVERFLOW;
+    if (s.flags & 1u) return PFC_ERR_VALIDATION;
+    j->termsum += s.termsum;
+    j->primecount += (uint64_t)s.counts[0] + s.counts[1];
+    j->pairs += ((uint64_t)s.counts[0] + s.counts[1]) * (uint64_t)(j->nmax - j->nmin);
+    j->stage = 3;
+    return PFC_OK;
+}
+
+extern "C" int pfc_check(pfc_job *j) {
+    if (!j) return PFC_ERR_ARG;
+    if (j->stage < 2 || j->next_it != iter_end(j)) return PFC_ERR_STATE;
+    CK(cudaSetDevice(j->ctx->device));
+    CK(cudaMemsetAsync(&j->stats.p->termsum, 0, sizeof(unsigned long long), j->ctx->st));
+    CK(cudaMemsetAsync(&j->stats.p->flags, 0, sizeof(uint32_t), j->ctx->st));
+    int rc = enqueue_check(j);
+    if (rc) return rc;
+    rc = read_stats(j);
+    if (rc) return rc;
+    return commit_segment(j);
+}
+
+extern "C" int pfc_segment(pfc_job *j, uint64_t p_lo, uint64_t p_hi) {
+    if (!j || p_lo < j->pmin || p_hi > j->pmax || p_hi <= p_lo) return PFC_ERR_ARG;
+    pfc_ctx *c = j->ctx;
+    CK(cudaSetDevice(c->device));
+    int rc = ensure_class_caps(j, p_lo, p_hi);
+    if (rc) return rc;
+    // generate; grow and regenerate if a class overflowed
+    for (int attempt = 0;; ++attempt) {
+        rc = enqueue_gen(j, p_lo, p_hi);
+        if (rc) return rc;
+        CK(cudaMemcpyAsync(j->h_stats, j->stats.p, sizeof(SegStats), cudaMemcpyDeviceToHost, c->st));
+        CK(cudaStreamSynchronize(c->st));
+        const uint32_t n32 = j->h_stats->counts[0], n64 = j->h_stats->counts[1];
+        const bool over32 = n32 > (j->c32.p.p ? j->c32.cap : 0);
+        const bool over64 = n64 > (j->c64.p.p ? j->c64.cap : 0);
+        if (!over32 && !over64) break;
+        if (attempt >= 2) return PFC_ERR_CAND_OVERFLOW;
+        if (over32) CK(j->c32.ensure(c, (uint32_t)std::min<uint64_t>(4000000000ull, n32 + n32 / 8 + 1024)));
+        if (over64) CK(j->c64.ensure(c, (uint32_t)std::min<uint64_t>(4000000000ull, n64 + n64 / 8 + 1024)));
+    }
+    const uint32_t n32 = j->h_stats->counts[0], n64 = j->h_stats->counts[1];
+    const unsigned long long hit_base = j->h_stats->hits;
+    for (int attempt = 0;; ++attempt) {
+        CK(cudaMemsetAsync(&j->stats.p->termsum, 0, sizeof(unsigned long long), c->st));
+        CK(cudaMemsetAsync(&j->stats.p->flags, 0, sizeof(uint32_t), c->st));
+        rc = enqueue_setup(j);
+        if (rc) return rc;
+        rc = enqueue_iter_chunked(j, iter_begin(j), iter_end(j), n32, n64);
+        if (rc) return rc;
+        j->next_it = iter_end(j);
+        rc = enqueue_check(j);
+        if (rc) return rc;
+        rc = read_stats(j);
+        if (rc) return rc;
+        const unsigned long long nh = j->h_stats->hits;
+        if (nh <= j->hits.n) break;
+        if (attempt >= 2) return PFC_ERR_HIT_OVERFLOW;
+        // grow the hit list, keep the hits of earlier segments, redo this one
+        DArr<pfc_factor> bigger;
+        CK(bigger.alloc(c, (size_t)(nh + nh / 4 + 4096)));
+        if (hit_base) CK(cudaMemcpyAsync(bigger.p, j->hits.p, hit_base * sizeof(pfc_factor), cudaMemcpyDeviceToDevice, c->st));
+        CK(cudaStreamSynchronize(c->st));
+        j->hits.release(c);
+        j->hits = bigger;
+        CK(cudaMemcpyAsync(hitcount_ptr(j), &hit_base, sizeof(hit_base), cudaMemcpyHostToDevice, c->st));
+    }
+    return commit_segment(j);
+}
+
+extern "C" int pfc_sync(pfc_job *j) {
+    if (!j) return PFC_ERR_ARG;
+    CK(cudaSetDevice(j->ctx->device));
+    CK(cudaStreamSynchronize(j->ctx->st));
+    return PFC_OK;
+}
+
+extern "C" int pfc_drain_hits(pfc_job *j, pfc_factor *buf, size_t cap, size_t *n) {
+    if (!j || !n || (!buf && cap)) return PFC_ERR_ARG;
+    pfc_ctx *c = j->ctx;
+    CK(cudaSetDevice(c->device));
+    int rc = read_stats(j);
+    if (rc) return rc;
+    const unsigned long long nh = j->h_stats->hits;
+    *n = (size_t)nh;
+    if (nh > j->hits.n) return PFC_ERR_HIT_OVERFLOW;   // device list incomplete
+    const size_t copy = std::min<size_t>((size_t)nh, cap);
+    if (copy) {
+        c->d2h += copy * sizeof(pfc_factor);
+        CK(cudaMemcpyAsync(buf, j->hits.p, copy * sizeof(pfc_factor), cudaMemcpyDeviceToHost, c->st));
+        CK(cudaStreamSynchronize(c->st));
+    }
+    if (nh > cap) return PFC_ERR_HIT_OVERFLOW;
+    CK(cudaMemsetAsync(hitcount_ptr(j), 0, sizeof(unsigned long long), c->st));
+    CK(cudaStreamSynchronize(c->st));
+    j->h_stats->hits = 0;
+    return PFC_OK;
+}
+
+extern "C" int pfc_job_totals(pfc_job *j, uint64_t *termsum, uint64_t *primecount) {
+    if (!j) return PFC_ERR_ARG;
+    if (termsum) *termsum = j->termsum;
+    if (primecount) *primecount = j->primecount;
+    return PFC_OK;
+}
+
+extern "C" int pfc_job_run(pfc_job *j, pfc_factor *buf, size_t cap, size_t *n) {
+    if (!j || !n || (!buf && cap)) return PFC_ERR_ARG;
+    size_t total = 0;
+    bool overflow = false;
+    std::vector<pfc_factor> tmp;
+    for (uint64_t lo = j->pmin; lo < j->pmax;) {
+        uint64_t hi;
+        int rc = pfc_job_segment_end(j, lo, &hi);
+        if (rc) return rc;
+        rc = pfc_segment(j, lo, hi);
+        if (rc) return rc;
+        size_t got = 0;
+        const size_t room = overflow ? 0 : cap - total;
+        rc = pfc_drain_hits(j, overflow ? nullptr : buf + total, room, &got);
+        if (rc == PFC_ERR_HIT_OVERFLOW) {
+            overflow = true;
+            // clear the device list so later segments keep counting
+            CK(cudaMemsetAsync(hitcount_ptr(j), 0, sizeof(unsigned long long), j->ctx->st));
+            CK(cudaStreamSynchronize(j->ctx->st));
+            j->h_stats->hits = 0;
+        } else if (rc) {
+            return rc;
+        }
+        total += got;
+        lo = hi;
+    }
+    *n = total;
+    return overflow ? PFC_ERR_HIT_OVERFLOW : PFC_OK;
+}
+
+// ---------------------------------------------------------- introspection
+
+extern "C" int pfc_segment_state(pfc_job *j, uint64_t *p, uint64_t *s0, uint64_t *s1, size_t cap, size_t *n) {
+    if (!j || !n) return PFC_ERR_ARG;
+    int rc = read_stats(j);
+    if (rc) return rc;
+    const uint32_t n32 = std::min(j->h_stats->counts[0], j->c32.p.p ? j->c32.cap : 0u);
+    const uint32_t n64 = std::min(j->h_stats->counts[1], j->c64.p.p ? j->c64.cap : 0u);
+    *n = (size_t)n32 + n64;
+    if (*n > cap) return PFC_ERR_ARG;
+    std::vector<uint32_t> a(n32), b(n32), d(n32);
+    std::vector<uint64_t> e(n64), f(n64), g(n64);
+    pfc_ctx *c = j->ctx;
+    if (n32) {
+        CK(cudaMemcpy(a.data(), j->c32.p.p, n32 * 4, cudaMemcpyDeviceToHost));
+        CK(cudaMemcpy(b.data(), j->c32.s0.p, n32 * 4, cudaMemcpyDeviceToHost));
+        CK(cudaMemcpy(d.data(), j->c32.s1.p, n32 * 4, cudaMemcpyDeviceToHost));
+    }
+    if (n64) {
+        CK(cudaMemcpy(e.data(), j->c64.p.p, n64 * 8, cudaMemcpyDeviceToHost));
+        CK(cudaMemcpy(f.data(), j->c64.s0.p, n64 * 8, cudaMemcpyDeviceToHost));
+        CK(cudaMemcpy(g.data(), j->c64.s1.p, n64 * 8, cudaMemcpyDeviceToHost));
+    }
+    (void)c;
+    typedef unsigned __int128 u128;
+    for (uint32_t i = 0; i < n32; ++i) {
+        // class 32 holds x*2^32 mod p: the reference form is x*2^64 mod p
+        p[i] = a[i];
+        if (s0) s0[i] = (uint64_t)(((u128)b[i] << 32) % a[i]);
+        if (s1) s1[i] = (uint64_t)(((u128)d[i] << 32) % a[i]);
+    }
+    for (uint32_t i = 0; i < n64; ++i) {
+        p[n32 + i] = e[i];
+        if (s0) s0[n32 + i] = f[i];
+        if (s1) s1[n32 + i] = g[i];
+    }
+    return PFC_OK;
+}
+
+extern "C" uint64_t pfc_job_pairs(pfc_job *j) { return j ? j->pairs : 0; }
+
+extern "C" uint64_t pfc_job_setup_mulmods(pfc_job *j, int cls64) {
+    return j ? (cls64 ? j->setup_mulmods64 : j->setup_mulmods32) : 0;
+}

@@ -1,0 +1,189 @@
+// arith.cuh -- modular arithmetic for the sieve kernels (sm_103a).
+//
+// Two size classes of candidate prime p:
+//   class 32: p < 2^32, Montgomery with R = 2^32, one 32x32->64 product per
+//             multiplication (IMAD.WIDE) plus two IMADs for the reduction.
+//   class 64: p < 2^64, Montgomery with R = 2^64.
+//
+// The reference keeps every residue in Montgomery form with R = 2^64
+// (kernels/iterate.cl:44-50: m_mul(a,b) = a*b/2^64 mod p in [0,p)).  All
+// values here are canonical (in [0,p)), so any representation maps back to
+// the reference's by exact modular arithmetic; the checksum epilogue converts
+// class-32 residues to R = 2^64 before summing.
+//
+// "redc(a*b)" below always means a*b*R^-1 mod p for a*b < p*R; it is used
+// with one operand in plain form (n, a prime q, a table word) so that the
+// product drifts by a known power of R which the kernels track (see
+// sieve.cu).
+#pragma once
+#include <cstdint>
+
+namespace pfc {
+
+// ------------------------------------------------------------------ class 32
+
+// p^-1 mod 2^32 for odd p (Newton: x <- x(2 - p x); p*p = 1 mod 8 seeds 3 bits)
+__device__ __forceinline__ uint32_t inv32(uint32_t p) {
+    uint32_t x = p;
+    x *= 2u - p * x;
+    x *= 2u - p * x;
+    x *= 2u - p * x;
+    x *= 2u - p * x;
+    return x;
+}
+
+// a*b*2^-32 mod p, requires a*b < p*2^32; result in [0,p)
+__device__ __forceinline__ uint32_t redc32(uint32_t a, uint32_t b, uint32_t p, uint32_t pinv) {
+    uint64_t t = (uint64_t)a * b;
+    uint32_t m = (uint32_t)t * pinv;          // m*p = t (mod 2^32)
+    uint32_t u = __umulhi(m, p);
+    uint32_t th = (uint32_t)(t >> 32);
+    uint32_t r = th - u;
+    return (th < u) ? r + p : r;
+}
+
+struct Mont32 {
+    uint32_t p, pinv, one /* 2^32 mod p */, r2 /* 2^64 mod p */;
+    __device__ __forceinline__ void init(uint32_t p_) {
+        p = p_;
+        pinv = inv32(p);
+        one = (0u - p) % p;
+        r2 = (uint32_t)(((uint64_t)one * one) % p);
+    }
+    __device__ __forceinline__ uint32_t mul(uint32_t a, uint32_t b) const { return redc32(a, b, p, pinv); }
+    __device__ __forceinline__ uint32_t to_mont(uint32_t x) const { return redc32(x, r2, p, pinv); }
+    // Mont(R^e) = R^(e+1) mod p by square-and-multiply on base Mont(R) = r2
+    __device__ __forceinline__ uint32_t mont_R_pow(uint64_t e) const {
+        uint32_t acc = one, base = r2;
+        while (e) {
+            if (e & 1) acc = mul(acc, base);
+            base = mul(base, base);
+            e >>= 1;
+        }
+        return acc;
+    }
+    // value with R = 2^64 Montgomery scaling: x*2^64 mod p, from x*2^32 mod p
+    __device__ __forceinline__ uint64_t mont32_to_mont64(uint32_t xm) const { return mul(xm, r2); }
+};
+
+// ------------------------------------------------------------------ class 64
+
+__device__ __forceinline__ uint64_t inv64(uint64_t p) {
+    uint64_t x = p;
+    x *= 2u - p * x;
+    x *= 2u - p * x;
+    x *= 2u - p * x;
+    x *= 2u - p * x;
+    x *= 2u - p * x;
+    return x;
+}
+
+// a*b*2^-64 mod p, requires a*b < p*2^64; result in [0,p).  Same reduction
+// as the reference m_mul (kernels/iterate.cl:44-50).
+__device__ __forceinline__ uint64_t redc64(uint64_t a, uint64_t b, uint64_t p, uint64_t pinv) {
+    uint64_t tl = a * b;
+    uint64_t th = __umul64hi(a, b);
+    uint64_t m = tl * pinv;
+    uint64_t u = __umul64hi(m, p);
+    uint64_t r = th - u;
+    return (th < u) ? r + p : r;
+}
+
+// s*n*2^-64 mod p for a 32-bit multiplier n (s < p): the 96-bit product
+// s*n is formed with two 32x64 multiply-adds, then reduced as above.
+__device__ __forceinline__ uint64_t redc64_u32(uint64_t s, uint32_t n, uint64_t p, uint64_t pinv) {
+    uint64_t lo = (uint64_t)(uint32_t)s * n;
+    uint64_t hi = (s >> 32) * (uint64_t)n;     // < 2^64
+    uint64_t tl = lo + (hi << 32);
+    uint64_t th = (hi >> 32) + (tl < lo ? 1u : 0u);
+    uint64_t m = tl * pinv;
+    uint64_t u = __umul64hi(m, p);
+    uint64_t r = th - u;
+    return (th < u) ? r + p : r;
+}
+
+__device__ __forceinline__ uint64_t addmod64(uint64_t a, uint64_t b, uint64_t p) {
+    uint64_t c = (a >= p - b) ? p : 0;
+    return a + b - c;
+}
+
+struct Mont64 {
+    uint64_t p, pinv, one /* 2^64 mod p */, r2 /* 2^128 mod p */;
+    __device__ __forceinline__ void init(uint64_t p_) {
+        p = p_;
+        pinv = inv64(p);
+        one = (0ull - p) % p;
+        uint64_t two = addmod64(one, one, p);
+        uint64_t x = addmod64(two, two, p);         // 4*2^64
+        for (int i = 0; i < 5; ++i) x = redc64(x, x, p, pinv);  // 4^(2^5) * 2^64 = 2^128
+        r2 = x;
+    }
+    __device__ __forceinline__ uint64_t mul(uint64_t a, uint64_t b) const { return redc64(a, b, p, pinv); }
+    __device__ __forceinline__ uint64_t to_mont(uint64_t x) const { return redc64(x, r2, p, pinv); }
+    __device__ __forceinline__ uint64_t mont_R_pow(uint64_t e) const {
+        uint64_t acc = one, base = r2;
+        while (e) {
+            if (e & 1) acc = mul(acc, base);
+            base = mul(base, base);
+            e >>= 1;
+        }
+        return acc;
+    }
+};
+
+// ------------------------------------------------ base-2 strong PRP (SPRP-2)
+// Textbook strong probable-prime test to base 2 (the rule of
+// kernels/getsegprimes.cl:79-108).  Doubling replaces multiplication by the
+// base.  For odd n > 2 only.
+
+__device__ __forceinline__ bool sprp2_32(uint32_t n) {
+    Mont32 m;
+    m.p = n;
+    m.pinv = inv32(n);
+    m.one = (0u - n) % n;
+    uint32_t nmo = n - m.one;
+    int t = __ffs(n - 1) - 1;
+    uint32_t d = (n - 1) >> t;
+    uint32_t a = m.one + m.one;                    // Mont(2), may be >= n
+    if (a >= n || a < m.one) a -= n;
+    if (d > 1) {
+        int top = 31 - __clz(d);
+        for (int b = top - 1; b >= 0; --b) {
+            a = m.mul(a, a);
+            if ((d >> b) & 1) {
+                uint32_t a2 = a + a;
+                a = (a2 >= n || a2 < a) ? a2 - n : a2;
+            }
+        }
+    }
+    if (a == m.one || a == nmo) return true;
+    for (int s = 1; s < t; ++s) {
+        a = m.mul(a, a);
+        if (a == nmo) return true;
+    }
+    return false;
+}
+
+__device__ __forceinline__ bool sprp2_64(uint64_t n) {
+    uint64_t pinv = inv64(n);
+    uint64_t one = (0ull - n) % n;
+    uint64_t nmo = n - one;
+    int t = __ffsll((long long)(n - 1)) - 1;
+    uint64_t d = (n - 1) >> t;
+    uint64_t a = addmod64(one, one, n);
+    if (d > 1) {
+        int top = 63 - __clzll((long long)d);
+        for (int b = top - 1; b >= 0; --b) {
+            a = redc64(a, a, n, pinv);
+            if ((d >> b) & 1) a = addmod64(a, a, n);
+        }
+    }
+    if (a == one || a == nmo) return true;
+    for (int s = 1; s < t; ++s) {
+        a = redc64(a, a, n, pinv);
+        if (a == nmo) return true;
+    }
+    return false;
+}
+
+}  // namespace pfc

@@ -1,0 +1,373 @@
+// host.cpp -- host tables (prime lists, setup programs) and factor
+// post-processing (re-verification, 2-PRP filter, checksum fold, formatting).
+#include "host.hpp"
+
+#include <algorithm>
+#include <cinttypes>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#include "pfcsieve.h"
+
+namespace pfc {
+
+typedef unsigned __int128 u128;
+
+// ----------------------------------------------------------------- primes
+
+std::vector<uint32_t> primes_between(uint32_t lo, uint32_t hi) {
+    std::vector<uint32_t> out;
+    if (hi < 2 || hi < lo) return out;
+    if (lo <= 2) out.push_back(2);
+    const uint64_t root = (uint64_t)std::sqrt((double)hi) + 2;
+    std::vector<uint8_t> comp(root + 1, 0);
+    std::vector<uint32_t> base;
+    for (uint64_t i = 3; i <= root; i += 2) {
+        if (comp[i]) continue;
+        base.push_back((uint32_t)i);
+        for (uint64_t j = i * i; j <= root; j += 2 * i) comp[j] = 1;
+    }
+    const uint64_t first = std::max<uint64_t>(lo, 3) | 1;  // odd
+    if (first > hi) return out;
+    const uint64_t nodd = ((uint64_t)hi - first) / 2 + 1;
+    const uint64_t seg = 1u << 21;
+    const uint64_t nseg = (nodd + seg - 1) / seg;
+    std::vector<std::vector<uint32_t>> parts(nseg);
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int64_t s = 0; s < (int64_t)nseg; ++s) {
+        const uint64_t i0 = (uint64_t)s * seg;
+        const uint64_t len = std::min(seg, nodd - i0);
+        const uint64_t x0 = first + 2 * i0;  // odd, x_i = x0 + 2i
+        std::vector<uint8_t> mark(len, 0);
+        for (uint32_t q : base) {
+            const uint64_t qq = (uint64_t)q * q;
+            if (qq > x0 + 2 * (len - 1)) break;
+            uint64_t start;
+            if (qq >= x0) start = qq;
+            else {
+                start = (x0 + q - 1) / q * q;
+                if (!(start & 1)) start += q;
+            }
+            for (uint64_t x = start; x < x0 + 2 * len; x += 2 * (uint64_t)q) mark[(x - x0) / 2] = 1;
+        }
+        std::vector<uint32_t> &v = parts[s];
+        for (uint64_t i = 0; i < len; ++i)
+            if (!mark[i] && x0 + 2 * i > 1) v.push_back((uint32_t)(x0 + 2 * i));
+    }
+    for (auto &v : parts) out.insert(out.end(), v.begin(), v.end());
+    return out;
+}
+
+std::vector<uint32_t> prime_bitmap(uint32_t nmin, uint32_t nmax, const std::vector<uint32_t> &primes) {
+    const uint64_t len = nmax > nmin ? (uint64_t)nmax - nmin : 0;
+    std::vector<uint32_t> bits((len + 31) / 32 + 2, 0);
+    auto it = std::lower_bound(primes.begin(), primes.end(), nmin);
+    for (; it != primes.end() && *it < nmax; ++it) {
+        const uint64_t k = *it - nmin;
+        bits[k >> 5] |= 1u << (k & 31);
+    }
+    return bits;
+}
+
+// ------------------------------------------------------------ setup programs
+
+template <class W>
+uint64_t HostProg<W>::mulmods() const {
+    uint64_t t = final_sq + words.size();
+    for (size_t g = 0; g + 2 < groups.size(); g += 3) t += groups[g + 2];
+    return t;
+}
+
+template <class W>
+static void pack_words(const std::vector<uint32_t> &f, std::vector<W> &words) {
+    const u128 lim = (u128)(W)~(W)0;
+    size_t i = 0;
+    while (i < f.size()) {
+        u128 acc = f[i++];
+        while (i < f.size() && acc * f[i] <= lim) acc *= f[i++];
+        words.push_back((W)acc);
+    }
+}
+
+// drift bookkeeping: the device multiplies Montgomery values, so every
+// reduction of a product with a plain table word lowers the power of R by
+// one and every squaring maps d -> 2d - 1; the final correction multiplies
+// by R^(corr+1) to come back to d = 1 (Montgomery form).
+template <class W>
+static bool finish_prog(HostProg<W> &p) {
+    __int128 d = 1;
+    const __int128 lim = (__int128)1 << 62;
+    for (size_t g = 0; g + 2 < p.groups.size(); g += 3) {
+        for (uint32_t k = 0; k < p.groups[g + 2]; ++k) {
+            d = 2 * d - 1;
+            if (-d > lim) return false;
+        }
+        d -= (__int128)(p.groups[g + 1] - p.groups[g]);
+    }
+    for (uint32_t k = 0; k < p.final_sq; ++k) {
+        d = 2 * d - 1;
+        if (-d > lim) return false;
+    }
+    p.corr = (uint64_t)(1 - d);
+    return true;
+}
+
+template <class W>
+bool build_power_prog(uint32_t startN, uint32_t sub, const std::vector<uint32_t> &primes, HostProg<W> &out) {
+    out = HostProg<W>();
+    std::vector<std::vector<uint32_t>> bit(32);
+    int top = -1;
+    for (uint32_t q : primes) {
+        if (q > startN) break;
+        uint64_t e = 0;
+        for (uint64_t qk = q; qk <= startN; qk *= q) e += startN / qk;   // Legendre, cl_sieve.cpp:824-833
+        if (e < sub) continue;
+        e -= sub;
+        for (int j = 0; e; ++j, e >>= 1)
+            if (e & 1) {
+                bit[j].push_back(q);
+                top = std::max(top, j);
+            }
+    }
+    uint32_t pending = 0;
+    bool started = false;
+    for (int j = top; j >= 0; --j) {
+        if (started) ++pending;
+        if (bit[j].empty()) continue;
+        const uint32_t b = (uint32_t)out.words.size();
+        pack_words<W>(bit[j], out.words);
+        out.groups.push_back(b);
+        out.groups.push_back((uint32_t)out.words.size());
+        out.groups.push_back(pending);
+        pending = 0;
+        started = true;
+    }
+    out.final_sq = pending;
+    return finish_prog(out);
+}
+
+template <class W>
+bool build_product_prog(const std::vector<uint32_t> &factors, HostProg<W> &out) {
+    out = HostProg<W>();
+    if (!factors.empty()) {
+        pack_words<W>(factors, out.words);
+        out.groups = {0u, (uint32_t)out.words.size(), 0u};
+    }
+    return finish_prog(out);
+}
+
+template struct HostProg<uint32_t>;
+template struct HostProg<uint64_t>;
+template bool build_power_prog<uint32_t>(uint32_t, uint32_t, const std::vector<uint32_t> &, HostProg<uint32_t> &);
+template bool build_power_prog<uint64_t>(uint32_t, uint32_t, const std::vector<uint32_t> &, HostProg<uint64_t> &);
+template bool build_product_prog<uint32_t>(const std::vector<uint32_t> &, HostProg<uint32_t> &);
+template bool build_product_prog<uint64_t>(const std::vector<uint32_t> &, HostProg<uint64_t> &);
+
+// ------------------------------------------------------- host Montgomery
+
+struct HMont {
+    uint64_t p, q, one, r2;
+    explicit HMont(uint64_t p_) : p(p_) {
+        uint64_t x = p;
+        for (int i = 0; i < 6; ++i) x *= 2 - p * x;
+        q = x;
+        one = (0 - p) % p;
+        r2 = (uint64_t)(((u128)one * one) % p);
+    }
+    uint64_t mul(uint64_t a, uint64_t b) const {
+        const u128 t = (u128)a * b;
+        const uint64_t m = (uint64_t)t * q;
+        const uint64_t u = (uint64_t)(((u128)m * p) >> 64);
+        const uint64_t th = (uint64_t)(t >> 64);
+        const uint64_t r = th - u;
+        return th < u ? r + p : r;
+    }
+    uint64_t to(uint64_t x) const { return mul(x, r2); }
+    uint64_t add(uint64_t a, uint64_t b) const { return (a >= p - b) ? a + b - p : a + b; }
+};
+
+static bool sprp_base(const HMont &m, uint32_t base, int t, uint64_t d) {
+    const uint64_t nmo = m.p - m.one;
+    const uint64_t b = m.to(base);
+    uint64_t a = m.one;
+    for (int k = 63 - __builtin_clzll(d); k >= 0; --k) {
+        a = m.mul(a, a);
+        if ((d >> k) & 1) a = m.mul(a, b);
+    }
+    if (a == m.one || a == nmo) return true;
+    for (int s = 1; s < t; ++s) {
+        a = m.mul(a, a);
+        if (a == nmo) return true;
+    }
+    return false;
+}
+
+bool is_prime_u64(uint64_t p) {
+    static const uint32_t bases[7] = {2, 325, 9375, 28178, 450775, 9780504, 1795265022};
+    if (p < 2) return false;
+    if (!(p & 1)) return p == 2;
+    if (p < 9) return p > 1;
+    const HMont m(p);
+    const int t = __builtin_ctzll(p - 1);
+    const uint64_t d = (p - 1) >> t;
+    for (uint32_t b : bases) {
+        uint64_t bb = b;
+        if (bb >= p) {
+            bb %= p;
+            if (!bb) continue;
+        }
+        if (!sprp_base(m, (uint32_t)bb, t, d)) return false;
+    }
+    return true;
+}
+
+// starting products of verifyprime.cpp:205,222,241: 34!, 101#, 44!/44#
+static const u128 kStart[3] = {
+    ((u128)0xde1bc4d19efcac82ull << 64) | 0x445da75b00000000ull,
+    ((u128)0xaf2fa8f8a2d02a93ull << 64) | 0xae69c9f8987d5efeull,
+    ((u128)0x98dcc10f185c0e67ull << 64) | 0x3c93ff0000000000ull};
+
+// One walk per (p, type) over the hits of one prime (sorted by |n|):
+// the value of verifyprime.cpp:199-268 for each hit.
+static bool verify_group(const pfc_factor *h, size_t cnt, const uint32_t *list, size_t listsize) {
+    const uint64_t p = h[0].p;
+    const HMont m(p);
+    const uint64_t nmo = p - m.one;
+    for (int type = 0; type < 3; ++type) {
+        bool init = false;
+        uint64_t r = 0, nm = 0;   // r: Montgomery running product; nm: Mont(i)
+        uint64_t cur = 34;
+        size_t li = 0;
+        for (size_t k = 0; k < cnt; ++k) {
+            if (h[k].type != type) continue;
+            if (!init) {
+                r = m.to((uint64_t)(kStart[type] % p));
+                nm = m.to(cur % p);
+                init = true;
+            }
+            const uint32_t n = (uint32_t)(h[k].nc < 0 ? -h[k].nc : h[k].nc);
+            const int32_t c = h[k].nc < 0 ? -1 : 1;
+            if (type == 0) {
+                for (; cur < n; ++cur) {
+                    nm = m.add(nm, m.one);
+                    r = m.mul(r, nm);
+                }
+            } else {
+                for (; li < listsize && list[li] <= n; ++li) r = m.mul(r, m.to(list[li]));
+            }
+            if (!((r == m.one && c == -1) || (r == nmo && c == 1))) return false;
+        }
+    }
+    return true;
+}
+
+bool verify_factor(uint64_t p, uint32_t n, int32_t c, int32_t type, const uint32_t *list, size_t listsize) {
+    pfc_factor f;
+    f.p = p;
+    f.nc = c < 0 ? -(int32_t)n : (int32_t)n;
+    f.type = type;
+    return verify_group(&f, 1, list, listsize);
+}
+
+}  // namespace pfc
+
+// ==================================================================== C ABI
+
+using namespace pfc;
+
+static bool factor_less(const pfc_factor &a, const pfc_factor &b) {
+    if (a.p != b.p) return a.p < b.p;
+    const int32_t na = a.nc < 0 ? -a.nc : a.nc, nb = b.nc < 0 ? -b.nc : b.nc;
+    if (na != nb) return na < nb;
+    if (a.type != b.type) return a.type < b.type;
+    return a.nc < b.nc;
+}
+
+extern "C" int pfc_finalize_factors(unsigned mode, uint32_t nmax, pfc_factor *f, size_t n, int threads,
+                                    int verify, size_t *kept, uint64_t *checksum) {
+    if ((!f && n) || !kept || !checksum) return PFC_ERR_ARG;
+    std::sort(f, f + n, factor_less);
+    if (verify && n) {
+        // verification lists (cl_sieve.cpp:1468-1492)
+        std::vector<uint32_t> list;
+        if (mode & PFC_PRIMORIAL) {
+            list = primes_between(103, nmax);
+        } else if (mode & PFC_COMPOSITORIAL) {
+            const std::vector<uint32_t> pr = primes_between(45, nmax);
+            size_t i = 0;
+            for (uint32_t v = 45; v < nmax; ++v) {
+                if (i < pr.size() && pr[i] == v) {
+                    ++i;
+                    continue;
+                }
+                list.push_back(v);
+            }
+        }
+        std::vector<size_t> grp;
+        for (size_t i = 0; i < n; ++i)
+            if (i == 0 || f[i].p != f[i - 1].p) grp.push_back(i);
+        grp.push_back(n);
+        int bad = 0;
+#ifdef _OPENMP
+        if (threads > 0) omp_set_num_threads(threads);
+#else
+        (void)threads;
+#endif
+        const int64_t ngrp = (int64_t)grp.size() - 1;
+#pragma omp parallel for schedule(dynamic, 1)
+        for (int64_t g = 0; g < ngrp; ++g) {
+            if (!verify_group(f + grp[g], grp[g + 1] - grp[g], list.data(), list.size())) {
+#pragma omp atomic write
+                bad = 1;
+            }
+        }
+        if (bad) return PFC_ERR_VERIFY;
+    }
+    // drop 2-PRP factors, fold n+c into the checksum (cl_sieve.cpp:555-589)
+    size_t k = 0;
+    uint64_t lastgood = 0;
+    for (size_t i = 0; i < n; ++i) {
+        const uint64_t p = f[i].p;
+        if (p == lastgood || is_prime_u64(p)) {
+            lastgood = p;
+            const uint32_t fn = (uint32_t)(f[i].nc < 0 ? -f[i].nc : f[i].nc);
+            const int32_t fc = f[i].nc < 0 ? -1 : 1;
+            *checksum += (uint32_t)(fn + (uint32_t)fc);
+            f[k++] = f[i];
+        }
+    }
+    *kept = k;
+    return PFC_OK;
+}
+
+extern "C" int pfc_is_prime(uint64_t p) { return is_prime_u64(p) ? 1 : 0; }
+
+extern "C" int pfc_format_factor(const pfc_factor *f, char *buf, size_t cap) {
+    if (!f || !buf) return PFC_ERR_ARG;
+    const uint32_t fn = (uint32_t)(f->nc < 0 ? -f->nc : f->nc);
+    const int fc = f->nc < 0 ? -1 : 1;
+    const char *sym = f->type == PFC_TYPE_FACTORIAL ? "!" : f->type == PFC_TYPE_PRIMORIAL ? "#" : "!/#";
+    const int len = snprintf(buf, cap, "%" PRIu64 " | %u%s%+d", f->p, fn, sym, fc);
+    return (len < 0 || (size_t)len >= cap) ? PFC_ERR_ARG : len;
+}
+
+extern "C" const char *pfc_status_string(int s) {
+    switch (s) {
+        case PFC_OK: return "ok";
+        case PFC_ERR_ARG: return "invalid argument";
+        case PFC_ERR_CUDA: return "CUDA runtime error";
+        case PFC_ERR_NOMEM: return "out of memory or over the memory budget";
+        case PFC_ERR_HIT_OVERFLOW: return "hit buffer overflow";
+        case PFC_ERR_VALIDATION: return "gpu validation failure (n counter)";
+        case PFC_ERR_VERIFY: return "CPU factor verification failed";
+        case PFC_ERR_STATE: return "call out of order";
+        case PFC_ERR_CAND_OVERFLOW: return "candidate buffer overflow";
+        case PFC_ERR_NO_DEVICE: return "no usable CUDA device";
+        case PFC_ERR_IO: return "file I/O error";
+        default: return "unknown status";
+    }
+}

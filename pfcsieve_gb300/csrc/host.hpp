@@ -1,0 +1,44 @@
+// host.hpp -- host-side tables and post-processing for the sieve path.
+#pragma once
+#include <cstdint>
+#include <string>
+#include <vector>
+
+namespace pfc {
+
+// primes p with lo <= p <= hi (segmented odd-only sieve; replaces the
+// primesieve_generate_primes calls of cl_sieve.cpp:850,996,1000,1158,1472,
+// 1476,1498)
+std::vector<uint32_t> primes_between(uint32_t lo, uint32_t hi);
+
+// Setup program on the host: words, groups {begin, end, squarings}, final
+// squarings and the drift correction exponent (see kernels.cuh Prog).
+template <class W>
+struct HostProg {
+    std::vector<W> words;
+    std::vector<uint32_t> groups;
+    uint32_t final_sq = 0;
+    uint64_t corr = 0;
+    uint64_t mulmods() const;   // device multiplications per candidate (excl. correction)
+};
+
+// prod over primes q <= startN of q^(e_q - sub), e_q = Legendre exponent of q
+// in startN!, in Horner form over the bits of the exponent.  sub = 0 gives
+// startN!, sub = 1 gives startN!/startN# (the product of the composites).
+template <class W>
+bool build_power_prog(uint32_t startN, uint32_t sub, const std::vector<uint32_t> &primes, HostProg<W> &out);
+
+// plain product of the given factors packed into words (one group)
+template <class W>
+bool build_product_prog(const std::vector<uint32_t> &factors, HostProg<W> &out);
+
+// prime flags for n in [nmin, nmax): bit k <-> nmin + k, plus 2 zero pad words
+std::vector<uint32_t> prime_bitmap(uint32_t nmin, uint32_t nmax, const std::vector<uint32_t> &primes);
+
+// 7-base deterministic Miller-Rabin (verifyprime.cpp:157-195)
+bool is_prime_u64(uint64_t p);
+
+// CPU re-verification of one factor by naive products (verifyprime.cpp:199-268)
+bool verify_factor(uint64_t p, uint32_t n, int32_t c, int32_t type, const uint32_t *list, size_t listsize);
+
+}  // namespace pfc

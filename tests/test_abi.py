@@ -1,0 +1,99 @@
+"""C ABI checks that need no GPU: the library builds and loads, exports every
+symbol include/pfcsieve.h declares, and its host-side routines (factor
+post-processing, primality, formatting, status strings) match the oracle and
+the reference's formats."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+from oracle import oracle as o
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+@pytest.fixture(scope="module")
+def pfc():
+    from pfcsieve_gb300 import build
+    build.build()
+    import pfcsieve_gb300
+    pfcsieve_gb300.lib()
+    return pfcsieve_gb300
+
+
+def declared_symbols():
+    names = set()
+    for h in os.listdir(os.path.join(ROOT, "include")):
+        if h.endswith(".h"):
+            txt = open(os.path.join(ROOT, "include", h)).read()
+            txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+            names |= set(re.findall(r"\b(pfc_\w+)\s*\(", txt))
+    return names
+
+
+def test_exports_every_declared_symbol(pfc):
+    L = ctypes.CDLL(pfc.LIB_PATH)
+    syms = declared_symbols()
+    assert len(syms) >= 25
+    for s in sorted(syms):
+        assert hasattr(L, s), s
+
+
+def test_no_device_is_an_error_not_a_fallback(pfc):
+    try:
+        import torch
+        if torch.cuda.is_available():
+            pytest.skip("a GPU is present")
+    except ImportError:
+        pass
+    with pytest.raises(pfc.PFCError) as e:
+        pfc.Context(0)
+    assert e.value.code == pfc.PFC_ERR_NO_DEVICE
+
+
+def test_status_strings(pfc):
+    for code in range(-10, 1):
+        assert pfc.status_string(code) != "unknown status"
+
+
+def test_format_factor_lines(pfc):
+    # cl_sieve.cpp:565-581: "%llu | %u!%+d", "%llu | %u#%+d", "%llu | %u!/#%+d"
+    assert pfc.format_factor((101, -100, 0)) == "101 | 100!-1"
+    assert pfc.format_factor((1000000007, 12345, 1)) == "1000000007 | 12345#+1"
+    assert pfc.format_factor((18446744073709551557, -2147483647, 2)) == \
+        "18446744073709551557 | 2147483647!/#-1"
+
+
+def test_is_prime_matches_oracle(pfc):
+    rng = np.random.default_rng(3)
+    xs = list(range(1, 5000)) + [42799, 85489, 4294967297, 3215031751, 2152302898747,
+                                 3474749660383, 341550071728321, 3825123056546413051,
+                                 18446744073709551557, 18446744073709551615]
+    xs += [int(x) | 1 for x in rng.integers(1, 2**63, size=3000, dtype=np.uint64)]
+    for x in xs:
+        assert pfc.is_prime(x) == o.is_prime(x), x
+
+
+@pytest.mark.parametrize("mode,nmin,nmax,pmin,pmax", [
+    (1, 101, 200000, 101, 20000), (2, 101, 200000, 101, 20000),
+    (4, 101, 200000, 101, 20000), (5, 101, 50000, 3, 30000),
+])
+def test_finalize_matches_oracle_job(pfc, mode, nmin, nmax, pmin, pmax):
+    """pfc_finalize_factors on the oracle's raw hits reproduces the oracle's
+    whole-job factor list and checksum (sort, CPU verify, 2-PRP drop, fold)."""
+    cands = o.candidates(pmin, pmax)
+    hits, termsum, _ = o.sieve(mode, nmin, nmax, cands, os.cpu_count() or 1)
+    res, ofac = o.job(mode, nmin, nmax, pmin, pmax, os.cpu_count() or 1)
+    kept, add = pfc.finalize(mode, nmax, hits[::-1].copy(), threads=4, verify=True)
+    assert (termsum + add) % 2**64 == res.checksum
+    assert np.array_equal(o.sort_factors(kept), o.sort_factors(ofac))
+
+
+def test_finalize_rejects_false_hit(pfc):
+    bad = np.zeros(1, dtype=pfc.FACTOR_DTYPE)
+    bad[0] = (1000003, -1000, 0)   # 1000003 does not divide 1000!-1
+    with pytest.raises(pfc.PFCError) as e:
+        pfc.finalize(1, 2000, bad, verify=True)
+    assert e.value.code == -6

@@ -1,0 +1,183 @@
+"""Parity of the CUDA path (through the C ABI) with the oracle and with the
+reference's own golden vectors.  All tests need a GB300 (marker gpu).
+
+Bar: bit-exact.  Candidates are compared as sorted lists, residues candidate
+by candidate in the reference's representation (Montgomery, R = 2^64), hits
+as sorted (p, |n|, type, nc) lists, and whole searches by the reference's
+self-test triple (factorcount, primecount, checksum).
+"""
+import os
+
+import numpy as np
+import pytest
+
+from oracle import oracle as o
+from tests import goldens
+
+pfc = pytest.importorskip("pfcsieve_gb300")
+
+pytestmark = pytest.mark.gpu
+
+THREADS = os.cpu_count() or 1
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    c = pfc.Context(0)
+    yield c
+    c.close()
+
+
+def run_segment(ctx, mode, nmin, nmax, pmin, pmax, lo=None, hi=None):
+    lo = pmin if lo is None else lo
+    hi = pmax if hi is None else hi
+    with pfc.Job(ctx, mode, nmin, nmax, pmin, pmax) as job:
+        job.segment(lo, hi)
+        p, s0, s1 = job.segment_state()
+        hits = o.sort_factors(job.drain_hits())
+        termsum, count = job.totals()
+    order = np.argsort(p, kind="stable")
+    return p[order], s0[order], s1[order], hits, termsum, count
+
+
+def oracle_terms(mode, s4s6s7):
+    return goldens.terms_from_records(mode, s4s6s7)
+
+
+# ------------------------------------------------------------ candidates
+
+@pytest.mark.parametrize("lo,hi", [
+    (3, 200000), (101, 5000), (113, 130), (42000, 90000),
+    (10**9, 10**9 + 3 * 10**6), (2**32 - 200000, 2**32 + 200000),
+    (2**62, 2**62 + 300000), (2**64 - 300000, 2**64 - 1), (4294967290, 4294967300),
+])
+def test_candidates_match_oracle(ctx, lo, hi):
+    with pfc.Job(ctx, 1, 101, 102, lo, hi) as job:
+        job.gen(lo, hi)
+        job.setup()
+        job.iterate(101, 102)
+        job.check()
+        p, _, _ = job.segment_state()
+        _, count = job.totals()
+    assert count == len(p)
+    assert np.array_equal(np.sort(p), o.candidates(lo, hi))
+
+
+# --------------------------------------------- reference kernel fixtures
+
+def test_reference_fixture_segments(ctx):
+    segs, _, _ = goldens.ref_segments()
+    for s in segs:
+        p, s0, s1, hits, termsum, count = run_segment(ctx, s["mode"], s["nmin"], s["nmax"],
+                                                      s["pmin"], s["pmax"])
+        assert np.array_equal(p, s["cands"]), s["mode"]
+        ref = s["s4s6s7"]
+        assert np.array_equal(s0, ref[:, 1]), (s["mode"], s["pmin"])
+        if s["mode"] == 5:
+            assert np.array_equal(s1, ref[:, 0]), (s["mode"], s["pmin"])
+        assert np.array_equal(hits, s["hits"]), (s["mode"], s["pmin"])
+        with np.errstate(over="ignore"):
+            want = int(np.sum(oracle_terms(s["mode"], ref), dtype=np.uint64))
+        assert termsum == want
+        assert count == len(s["cands"])
+
+
+# ------------------------------------------- oracle at random small sizes
+
+@pytest.mark.parametrize("seed", range(6))
+def test_random_segments_vs_oracle(ctx, seed):
+    rng = np.random.default_rng(seed)
+    mode = [1, 2, 4, 5][seed % 4]
+    nmin = int(rng.integers(101, 30000))
+    nmax = nmin + int(rng.integers(1, 5000))
+    bits = int(rng.choice([20, 31, 33, 45, 63, 64]))
+    pmin = int(rng.integers(3, 2**bits - 100000)) if bits < 64 else 2**64 - 2000000
+    pmax = pmin + int(rng.integers(1000, 60000))
+    p, s0, s1, hits, termsum, _ = run_segment(ctx, mode, nmin, nmax, pmin, pmax)
+    cands = o.candidates(pmin, pmax)
+    assert np.array_equal(p, cands)
+    ohits, osum, terms = o.sieve(mode, nmin, nmax, cands, THREADS, want_terms=True)
+    assert np.array_equal(s0, terms[:, 0])
+    if mode == 5:
+        assert np.array_equal(s1, terms[:, 2])
+    assert np.array_equal(hits, ohits)
+    assert termsum == osum
+
+
+def test_wilson_and_small_p(ctx):
+    """p <= n: residues fall to 0 and (p-1)!+1 hits are real (self-test 3/6/10/14)."""
+    for mode in (1, 2, 4, 5):
+        p, s0, s1, hits, termsum, _ = run_segment(ctx, mode, 101, 6000, 3, 6000)
+        cands = o.candidates(3, 6000)
+        ohits, osum, terms = o.sieve(mode, 101, 6000, cands, THREADS, want_terms=True)
+        assert np.array_equal(s0, terms[:, 0]) and np.array_equal(hits, ohits) and termsum == osum
+
+
+# --------------------------------------------------- stage API, chunking
+
+@pytest.mark.parametrize("mode", [1, 2, 4, 5])
+def test_uneven_iterate_chunks(ctx, mode):
+    nmin, nmax, pmin, pmax = 150, 9001, 10**6, 10**6 + 40000
+    cands = o.candidates(pmin, pmax)
+    ohits, osum, terms = o.sieve(mode, nmin, nmax, cands, THREADS, want_terms=True)
+    with pfc.Job(ctx, mode, nmin, nmax, pmin, pmax) as job:
+        job.gen(pmin, pmax)
+        job.setup()
+        cuts = [nmin, nmin + 1, nmin + 8, nmin + 9, nmin + 40, 3001, 3017, 7000, nmax]
+        for a, b in zip(cuts[:-1], cuts[1:]):
+            job.iterate(a, b)
+        job.check()
+        p, s0, s1 = job.segment_state()
+        hits = o.sort_factors(job.drain_hits())
+        termsum, _ = job.totals()
+    order = np.argsort(p)
+    assert np.array_equal(s0[order], terms[:, 0])
+    assert np.array_equal(hits, ohits)
+    assert termsum == osum
+
+
+def test_out_of_order_iterate_rejected(ctx):
+    with pfc.Job(ctx, 1, 101, 1000, 10**6, 10**6 + 1000) as job:
+        job.gen(10**6, 10**6 + 1000)
+        with pytest.raises(pfc.PFCError):
+            job.iterate(101, 200)   # before setup
+        job.setup()
+        with pytest.raises(pfc.PFCError):
+            job.iterate(200, 300)   # skips [101, 200)
+        with pytest.raises(pfc.PFCError):
+            job.check()             # n range incomplete
+
+
+def test_segment_split_invariance(ctx):
+    """Totals over a p range equal the sum over any split of it."""
+    mode, nmin, nmax = 5, 101, 20000
+    lo, hi = 10**8, 10**8 + 400000
+    with pfc.Job(ctx, mode, nmin, nmax, lo, hi) as job:
+        job.segment(lo, hi)
+        whole = job.totals()
+        h1 = o.sort_factors(job.drain_hits())
+    with pfc.Job(ctx, mode, nmin, nmax, lo, hi) as job:
+        for a, b in [(lo, lo + 123457), (lo + 123457, lo + 300001), (lo + 300001, hi)]:
+            job.segment(a, b)
+        split = job.totals()
+        h2 = o.sort_factors(job.drain_hits())
+    assert whole == split
+    assert np.array_equal(h1, h2)
+
+
+# ------------------------------------------- the reference's self-test
+
+@pytest.mark.parametrize("cid", list(range(1, 17)))
+def test_selftest_triple(ctx, cid):
+    c = goldens.case(cid)
+    r = pfc.sieve(c["mode"], c["nmin"], c["nmax"], c["pmin"], c["pmax"], threads=THREADS, ctx=ctx)
+    assert (r.factorcount, r.primecount, r.checksum) == (c["factors"], c["primecount"], c["checksum_int"])
+
+
+@pytest.mark.parametrize("cid", [3, 9, 10, 14])
+def test_selftest_factor_lists(ctx, cid):
+    """Whole factor lists (not just the triple) equal the oracle's."""
+    c = goldens.case(cid)
+    r = pfc.sieve(c["mode"], c["nmin"], c["nmax"], c["pmin"], c["pmax"], threads=THREADS, ctx=ctx)
+    _, ofac = o.job(c["mode"], c["nmin"], c["nmax"], c["pmin"], c["pmax"], THREADS)
+    assert np.array_equal(o.sort_factors(r.factors), o.sort_factors(ofac))
