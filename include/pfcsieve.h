@@ -94,7 +94,7 @@ int pfc_ctx_device_info(pfc_ctx *ctx, char *name, size_t name_cap, int *sm_count
  * (setupSearch cl_sieve.cpp:596-665; setupPowerTable :842-984;
  * setupPrimeProducts :987-1148; setupCompositeProducts :1151-1326; prime list
  * :1494-1499), and upload them.  Range rules are the CLI's: 3 <= pmin < pmax,
- * 101 <= nmin < nmax < 2^31 (main.cpp:58-72). */
+ * 101 <= nmin <= nmax < 2^31 (main.cpp:58-72, cl_sieve.cpp:631-641). */
 int pfc_job_create(pfc_ctx *ctx, unsigned mode, uint32_t nmin, uint32_t nmax,
                    uint64_t pmin, uint64_t pmax, pfc_job **out);
 int pfc_job_destroy(pfc_job *job);

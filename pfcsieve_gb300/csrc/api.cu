@@ -286,7 +286,7 @@ extern "C" int pfc_job_create(pfc_ctx *c, unsigned mode, uint32_t nmin, uint32_t
                             mode == (PFC_FACTORIAL | PFC_COMPOSITORIAL);
     if (!valid_mode) return PFC_ERR_ARG;
     if (pmin < 3 || pmax <= pmin) return PFC_ERR_ARG;
-    if (nmin < 101 || nmax <= nmin || nmax > 0x7FFFFFFFu) return PFC_ERR_ARG;
+    if (nmin < 101 || nmax < nmin || nmax > 0x7FFFFFFFu) return PFC_ERR_ARG;
     CK(cudaSetDevice(c->device));
     pfc_job *j = new (std::nothrow) pfc_job();
     if (!j) return PFC_ERR_NOMEM;
