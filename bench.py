@@ -53,6 +53,9 @@ WORKLOADS = {
                       desc="-! n=[101,20000) p=[1e7,1.1e7)"),
     "primorial": dict(mode=2, nmin=101, nmax=10**6, pmin=2**62, pmax=2**62 + 5 * 10**7,
                       desc="-# n=[101,1e6) p=[2^62,2^62+5e7)"),
+    # reduced case of the combined search for ncu captures (same kernels)
+    "combined-small": dict(mode=5, nmin=101, nmax=20000, pmin=10**9, pmax=10**9 + 10**7,
+                           desc="-! -c n=[101,20000) p=[1e9,1.01e9)"),
 }
 
 
@@ -317,6 +320,8 @@ def run_ours(args, wl, world, rank, local, dist):
     alg_ops = cands_per_step * steps_per_cand * ops_per_mulmod
     it_s = float(np.mean(it_ms)) * 1e-3
     peak = pfc.int_peak(local, 0)
+    peaks_all = {k: pfc.int_peak(local, v) / 1e12 for k, v in
+                 (("imad", 0), ("mul_hi", 1), ("imad_wide", 2), ("iadd_xor", 3))}
     achieved = alg_ops / it_s
     traffic = None
     tfile = os.path.join(ROOT, "profiles", "iterate_traffic.json")
@@ -371,7 +376,8 @@ def run_ours(args, wl, world, rank, local, dist):
                          "unit": "Tops/s (32-bit integer multiply-add)", "frac": achieved / peak,
                          "traffic": traffic, "kernel": "iterate_kernel<%s,%d>" % ("Cls32" if cls32 else "Cls64", mode),
                          "kernel_ms_per_step": it_s * 1e3,
-                         "peak_source": "measured in this run (pfc_bench_int_peak, 32-bit IMAD chains)"},
+                         "peak_source": "measured in this run (pfc_bench_int_peak, 32-bit IMAD chains)",
+                         "int_peaks_tops": peaks_all},
             "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(launches), "clocks": clocks,
             "checksum_terms": "%016X" % termsum,
         }
