@@ -150,6 +150,7 @@ struct pfc_job {
     uint64_t setup_mulmods32 = 0, setup_mulmods64 = 0;
     DArr<uint32_t> primebits;
     DArr<uint32_t> qlist;
+    DArr<uint32_t> cmult;       // compositorial multipliers of the current chunk
     std::vector<uint32_t> h_qlist;
 
     DevClass<uint32_t> c32;
@@ -162,6 +163,7 @@ struct pfc_job {
     int stage = 0;              // 0 idle, 1 generated, 2 set up, 3 checked
     uint32_t next_it = 0;       // next n (or prime index) for pfc_iterate
     uint64_t seg_lo = 0, seg_hi = 0;
+    bool use32 = false, use64 = false;   // size classes the segment can hold
     uint64_t pairs = 0;
 };
 
@@ -185,6 +187,15 @@ static uint32_t iter_end(const pfc_job *j) {
     return j->mode == PFC_PRIMORIAL ? (uint32_t)j->h_qlist.size() : j->nmax;
 }
 static uint32_t iter_begin(const pfc_job *j) { return j->mode == PFC_PRIMORIAL ? 0u : j->nmin; }
+
+// steps every candidate walks over the whole search (all its chains)
+static uint32_t steps_needed(const pfc_job *j) {
+    const uint32_t len = iter_end(j) - iter_begin(j);
+    return j->mode == (PFC_FACTORIAL | PFC_COMPOSITORIAL) ? 2 * len : len;
+}
+
+// longest n chunk of one launch (bounds the compositorial multiplier table)
+constexpr uint32_t kMaxChunk = 1u << 22;
 
 // expected candidates in [lo, hi) (an over-estimate: density 1/ln x falls)
 static double est_cands(uint64_t lo, uint64_t hi) {
@@ -268,6 +279,7 @@ static int job_release(pfc_job *j) {
     j->b64.release(c);
     j->primebits.release(c);
     j->qlist.release(c);
+    j->cmult.release(c);
     j->c32.release(c);
     j->c64.release(c);
     j->hits.release(c);
@@ -371,13 +383,15 @@ extern "C" int pfc_job_segment_end(pfc_job *j, uint64_t p_lo, uint64_t *p_hi) {
 // ------------------------------------------------------------- stage calls
 
 static int ensure_class_caps(pfc_job *j, uint64_t lo, uint64_t hi) {
-    const uint64_t split = 1ull << 32;
+    const uint64_t split = kClassSplit;
     const double e32 = est_cands(lo, std::min(hi, split));
     const double e64 = est_cands(std::max(lo, split), hi);
     const double lim = 4.0e9;
     if (e32 > lim || e64 > lim) return PFC_ERR_NOMEM;
     CK(j->c32.ensure(j->ctx, lo < split ? (uint32_t)e32 : 0u));
     CK(j->c64.ensure(j->ctx, hi > split ? (uint32_t)e64 : 0u));
+    j->use32 = lo < split;
+    j->use64 = hi > split;
     return PFC_OK;
 }
 
@@ -391,8 +405,8 @@ static int enqueue_gen(pfc_job *j, uint64_t lo, uint64_t hi) {
     g.nodd = hi > base ? (hi - base + 1) / 2 : 0;
     g.p32 = j->c32.p.p;
     g.p64 = j->c64.p.p;
-    g.cap32 = j->c32.p.p ? j->c32.cap : 0;
-    g.cap64 = j->c64.p.p ? j->c64.cap : 0;
+    g.cap32 = j->use32 ? j->c32.cap : 0;
+    g.cap64 = j->use64 ? j->c64.cap : 0;
     g.count = counts_ptr(j);
     g.pat = c->d_pat;
     static const uint32_t sp[kSmallPrimes] = {3,  5,  7,  11, 13, 17, 19, 23, 29, 31, 37,  41,  43,  47,  53,
@@ -420,14 +434,14 @@ static int enqueue_setup(pfc_job *j) {
     s32.mode = j->mode;
     s32.a = j->a32.view;
     s32.b = j->b32.view;
-    s32.nnext0 = iter_begin(j);
+    s32.nnext0 = 0;
     SetupArgs<uint64_t> s64;
     s64.mode = j->mode;
     s64.a = j->a64.view;
     s64.b = j->b64.view;
-    s64.nnext0 = iter_begin(j);
-    if (j->c32.p.p) c->launches += launch_setup32(j->c32.view(counts_ptr(j)), s32, c->st);
-    if (j->c64.p.p) c->launches += launch_setup64(j->c64.view(counts_ptr(j) + 1), s64, c->st);
+    s64.nnext0 = 0;
+    if (j->use32) c->launches += launch_setup32(j->c32.view(counts_ptr(j)), s32, c->st);
+    if (j->use64) c->launches += launch_setup64(j->c64.view(counts_ptr(j) + 1), s64, c->st);
     CK(cudaGetLastError());
     j->stage = 2;
     j->next_it = iter_begin(j);
@@ -449,19 +463,49 @@ static HitBuf hitbuf(pfc_job *j) {
     return h;
 }
 
-// one iterate launch per class over [lo, hi) (n values or prime indices)
+// the walks of one chunk [lo, hi) (n values, or prime indices for n#):
+// factorial over n, compositorial over its multiplier table, primorial over
+// the prime list; each for both size classes
 static int enqueue_iter_range(pfc_job *j, uint32_t lo, uint32_t hi) {
     pfc_ctx *c = j->ctx;
-    IterArgs a;
-    a.mode = j->mode;
-    a.nmin = j->nmin;
-    a.lo = lo;
-    a.hi = hi;
-    a.primebits = j->primebits.p;
-    a.qlist = j->qlist.p;
     const HitBuf h = hitbuf(j);
-    if (j->c32.p.p) c->launches += launch_iterate32(j->c32.view(counts_ptr(j)), a, h, c->st);
-    if (j->c64.p.p) c->launches += launch_iterate64(j->c64.view(counts_ptr(j) + 1), a, h, c->st);
+    auto walk = [&](const WalkArgs &w) {
+        if (j->use32) c->launches += launch_walk32(j->c32.view(counts_ptr(j)), w, h, c->st);
+        if (j->use64) c->launches += launch_walk64(j->c64.view(counts_ptr(j) + 1), w, h, c->st);
+    };
+    WalkArgs w;
+    w.lo = lo;
+    w.hi = hi;
+    w.mult = nullptr;
+    w.mult2 = nullptr;
+    w.base = 0;
+    w.type = w.type2 = 0;
+    w.chain = 0;
+    if (j->mode == PFC_PRIMORIAL) {
+        w.mult = j->qlist.p;
+        w.type = PFC_TYPE_PRIMORIAL;
+        walk(w);
+        CK(cudaGetLastError());
+        return PFC_OK;
+    }
+    if (j->mode & PFC_COMPOSITORIAL) {
+        const size_t need = ((size_t)(hi - lo) + 15) & ~(size_t)15;
+        if (j->cmult.n < need) CK(j->cmult.alloc(c, std::max<size_t>(need, 4096)));
+        c->launches += launch_cmult(j->cmult.p, j->primebits.p, j->nmin, lo, hi, c->st);
+        w.base = lo;
+    }
+    if (j->mode == (PFC_FACTORIAL | PFC_COMPOSITORIAL)) {
+        // one launch walks both chains of each candidate
+        w.mult2 = j->cmult.p;
+        w.type = PFC_TYPE_FACTORIAL;
+        w.type2 = PFC_TYPE_COMPOSITORIAL;
+    } else if (j->mode == PFC_FACTORIAL) {
+        w.type = PFC_TYPE_FACTORIAL;
+    } else {
+        w.mult = j->cmult.p;
+        w.type = PFC_TYPE_COMPOSITORIAL;
+    }
+    walk(w);
     CK(cudaGetLastError());
     return PFC_OK;
 }
@@ -476,7 +520,7 @@ static uint32_t chunk_len(uint64_t count, double budget) {
 // [lo, hi) in launches of about 1.5e11 candidate-steps (class-64 steps
 // weigh 3), so no launch runs for more than a fraction of a second
 static int enqueue_iter_chunked(pfc_job *j, uint32_t lo, uint32_t hi, uint64_t n32, uint64_t n64) {
-    const uint32_t L = chunk_len(n32 + 3 * n64, 1.5e11);
+    const uint32_t L = std::min(chunk_len(n32 + 3 * n64, 1.5e11), kMaxChunk);
     while (lo < hi) {
         const uint32_t e = (uint32_t)std::min<uint64_t>((uint64_t)lo + L, hi);
         int rc = enqueue_iter_range(j, lo, e);
@@ -510,11 +554,11 @@ static int enqueue_check(pfc_job *j) {
     CheckArgs a;
     a.mode = j->mode;
     a.nlast = j->nmax - 1;
-    a.nend = iter_end(j);
+    a.nend = steps_needed(j);
     a.termsum = &j->stats.p->termsum;
     a.flags = &j->stats.p->flags;
-    if (j->c32.p.p) c->launches += launch_check32(j->c32.view(counts_ptr(j)), a, c->st);
-    if (j->c64.p.p) c->launches += launch_check64(j->c64.view(counts_ptr(j) + 1), a, c->st);
+    if (j->use32) c->launches += launch_check32(j->c32.view(counts_ptr(j)), a, c->st);
+    if (j->use64) c->launches += launch_check64(j->c64.view(counts_ptr(j) + 1), a, c->st);
     CK(cudaGetLastError());
     return PFC_OK;
 }
@@ -674,13 +718,12 @@ extern "C" int pfc_segment_state(pfc_job *j, uint64_t *p, uint64_t *s0, uint64_t
     if (!j || !n) return PFC_ERR_ARG;
     int rc = read_stats(j);
     if (rc) return rc;
-    const uint32_t n32 = std::min(j->h_stats->counts[0], j->c32.p.p ? j->c32.cap : 0u);
-    const uint32_t n64 = std::min(j->h_stats->counts[1], j->c64.p.p ? j->c64.cap : 0u);
+    const uint32_t n32 = std::min(j->h_stats->counts[0], j->use32 ? j->c32.cap : 0u);
+    const uint32_t n64 = std::min(j->h_stats->counts[1], j->use64 ? j->c64.cap : 0u);
     *n = (size_t)n32 + n64;
     if (*n > cap) return PFC_ERR_ARG;
     std::vector<uint32_t> a(n32), b(n32), d(n32);
     std::vector<uint64_t> e(n64), f(n64), g(n64);
-    pfc_ctx *c = j->ctx;
     if (n32) {
         CK(cudaMemcpy(a.data(), j->c32.p.p, n32 * 4, cudaMemcpyDeviceToHost));
         CK(cudaMemcpy(b.data(), j->c32.s0.p, n32 * 4, cudaMemcpyDeviceToHost));
@@ -691,10 +734,10 @@ extern "C" int pfc_segment_state(pfc_job *j, uint64_t *p, uint64_t *s0, uint64_t
         CK(cudaMemcpy(f.data(), j->c64.s0.p, n64 * 8, cudaMemcpyDeviceToHost));
         CK(cudaMemcpy(g.data(), j->c64.s1.p, n64 * 8, cudaMemcpyDeviceToHost));
     }
-    (void)c;
     typedef unsigned __int128 u128;
     for (uint32_t i = 0; i < n32; ++i) {
-        // class 32 holds x*2^32 mod p: the reference form is x*2^64 mod p
+        // class 32 holds x*2^32 mod p (walks leave it in [0, 2p)): the
+        // reference form is x*2^64 mod p
         p[i] = a[i];
         if (s0) s0[i] = (uint64_t)(((u128)b[i] << 32) % a[i]);
         if (s1) s1[i] = (uint64_t)(((u128)d[i] << 32) % a[i]);

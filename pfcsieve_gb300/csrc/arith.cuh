@@ -1,15 +1,17 @@
 // arith.cuh -- modular arithmetic for the sieve kernels (sm_103a).
 //
 // Two size classes of candidate prime p:
-//   class 32: p < 2^32, Montgomery with R = 2^32, one 32x32->64 product per
-//             multiplication (IMAD.WIDE) plus two IMADs for the reduction.
-//   class 64: p < 2^64, Montgomery with R = 2^64.
+//   class 32: p < 2^31, Montgomery with R = 2^32: one 32x32->64 multiply
+//             (IMAD.WIDE) plus an IMAD and an IMAD.HI per multiplication;
+//             walk residues are signed, in (-p, p) (redc31s).
+//   class 64: p >= 2^31, Montgomery with R = 2^64.
 //
 // The reference keeps every residue in Montgomery form with R = 2^64
-// (kernels/iterate.cl:44-50: m_mul(a,b) = a*b/2^64 mod p in [0,p)).  All
-// values here are canonical (in [0,p)), so any representation maps back to
-// the reference's by exact modular arithmetic; the checksum epilogue converts
-// class-32 residues to R = 2^64 before summing.
+// (kernels/iterate.cl:44-50: m_mul(a,b) = a*b/2^64 mod p in [0,p)).  Values
+// here are exact residues (canonical, or signed in (-p, p) inside class-32
+// walks), so any representation maps back to the reference's by exact
+// modular arithmetic; the checksum epilogue reduces and converts class-32
+// residues to R = 2^64 before summing.
 //
 // "redc(a*b)" below always means a*b*R^-1 mod p for a*b < p*R; it is used
 // with one operand in plain form (n, a prime q, a table word) so that the
@@ -40,6 +42,18 @@ __device__ __forceinline__ uint32_t redc32(uint32_t a, uint32_t b, uint32_t p, u
     uint32_t th = (uint32_t)(t >> 32);
     uint32_t r = th - u;
     return (th < u) ? r + p : r;
+}
+
+// Signed Montgomery step for p < 2^31: x in (-p, p), n < 2^31 (as int32).
+// m = lo(x*n) * p^-1 read as a signed 32-bit value, so |m*p| < 2^31 p and
+// (x*n - m*p) / 2^32 = hi(x*n) - hi(m*p) lies in (-p, p): no correction step.
+// Three multiplies (IMAD.WIDE, IMAD, IMAD.HI) and one subtract; result
+// = x*n*2^-32 (mod p).
+__device__ __forceinline__ int32_t redc31s(int32_t x, uint32_t n, int32_t p, uint32_t pinv) {
+    const int64_t t = (int64_t)x * (int32_t)n;
+    const int32_t m = (int32_t)((uint32_t)t * pinv);
+    const int32_t u = __mulhi(m, p);
+    return (int32_t)(t >> 32) - u;
 }
 
 struct Mont32 {

@@ -12,7 +12,7 @@
 // of 29 pattern lookups indexed by x0 mod s (32-bit arithmetic from a per-tile
 // base residue).  Survivors are popped bit by bit, tested with SPRP-2 in
 // 32-bit (x < 2^32) or 64-bit Montgomery arithmetic, and appended to the
-// class-32 or class-64 list with one atomic per warp (ballot + popc).
+// class-32 (x < 2^31) or class-64 list with one atomic per warp (ballot + popc).
 #include "arith.cuh"
 #include "kernels.cuh"
 
@@ -130,8 +130,8 @@ __global__ void __launch_bounds__(256) gen_kernel(GenArgs a) {
                 else if (x < (1ull << 32)) pass = sprp2_32((uint32_t)x);
                 else pass = sprp2_64(x);
             }
-            const bool c32 = pass && x < (1ull << 32);
-            const bool c64 = pass && x >= (1ull << 32);
+            const bool c32 = pass && x < kClassSplit;
+            const bool c64 = pass && x >= kClassSplit;
             warp_append<uint32_t>(c32, (uint32_t)x, a.p32, a.cap32, a.count + 0);
             warp_append<uint64_t>(c64, x, a.p64, a.cap64, a.count + 1);
         }

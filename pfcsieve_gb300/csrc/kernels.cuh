@@ -15,8 +15,8 @@ constexpr int kPatEntries = 1591;         // sum of the 29 primes: one 64-bit ma
 //   p      : candidate primes
 //   s0, s1 : residues (s0: factorial / primorial / compositorial-only;
 //            s1: compositorial of the combined search)
-//   nnext  : next n (or prime index) each candidate will process; the
-//            check kernel compares it with the end of the range
+//   nnext  : steps walked so far, summed over the candidate's chains; the
+//            check kernel compares it with the steps the search needs
 template <class W>
 struct ClassBuf {
     W *p;
@@ -54,18 +54,30 @@ struct SetupArgs {
     uint32_t nnext0; // nmin for n walks, 0 for the primorial prime index
 };
 
-struct IterArgs {
-    unsigned mode;
-    uint32_t nmin;              // bit k of compbits <-> n = nmin + k
-    uint32_t lo, hi;            // n range (or prime-index range for primorial)
-    const uint32_t *primebits;  // prime flags over [nmin, nmax) (+ 2 pad words)
-    const uint32_t *qlist;      // primorial: primes in [nmin, nmax)
+// One walk launch over step indices [lo, hi).  The multiplier of step k is k
+// itself (mult == nullptr: the factorial's n) or mult[k - base] (the
+// compositorial's table of n at composite n and 1 at prime n, or the
+// primorial's list of primes).  With mult2 set the launch also walks the
+// candidate's second residue over mult2 (the compositorial chain of the
+// combined search, fused with its factorial chain).  Hits record the
+// multiplier.
+struct WalkArgs {
+    uint32_t lo, hi;
+    const uint32_t *mult;
+    const uint32_t *mult2;
+    uint32_t base;      // index of mult[0] and mult2[0]
+    int32_t type;       // factor type of chain-0 hits (PFC_TYPE_*)
+    int32_t type2;      // factor type of the fused second chain
+    int chain;          // single-chain walks: 0 -> residue s0, 1 -> residue s1
 };
+
+// size classes: class 32 holds p < 2^31, class 64 the rest
+constexpr uint64_t kClassSplit = 1ull << 31;
 
 struct CheckArgs {
     unsigned mode;
     uint32_t nlast;             // nmax - 1
-    uint32_t nend;              // expected nnext: nmax, or the prime count
+    uint32_t nend;              // steps every candidate must have walked
     unsigned long long *termsum;
     uint32_t *flags;            // bit 0: n-counter validation failure
 };
@@ -85,8 +97,12 @@ struct GenArgs {
 int launch_gen(const GenArgs &a, int sms, cudaStream_t st);
 int launch_setup32(const ClassBuf<uint32_t> &c, const SetupArgs<uint32_t> &a, cudaStream_t st);
 int launch_setup64(const ClassBuf<uint64_t> &c, const SetupArgs<uint64_t> &a, cudaStream_t st);
-int launch_iterate32(const ClassBuf<uint32_t> &c, const IterArgs &a, const HitBuf &h, cudaStream_t st);
-int launch_iterate64(const ClassBuf<uint64_t> &c, const IterArgs &a, const HitBuf &h, cudaStream_t st);
+int launch_walk32(const ClassBuf<uint32_t> &c, const WalkArgs &a, const HitBuf &h, cudaStream_t st);
+int launch_walk64(const ClassBuf<uint64_t> &c, const WalkArgs &a, const HitBuf &h, cudaStream_t st);
+// compositorial multipliers of n in [lo, hi): n when composite, 1 when prime
+// (bit k of primebits <-> n = nmin + k); `out` is padded with 1 to a multiple of 16
+int launch_cmult(uint32_t *out, const uint32_t *primebits, uint32_t nmin, uint32_t lo, uint32_t hi,
+                 cudaStream_t st);
 int launch_check32(const ClassBuf<uint32_t> &c, const CheckArgs &a, cudaStream_t st);
 int launch_check64(const ClassBuf<uint64_t> &c, const CheckArgs &a, cudaStream_t st);
 

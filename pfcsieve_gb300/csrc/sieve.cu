@@ -17,9 +17,16 @@
 // ORs its comparisons into one predicate; if any lane of the warp saw a hit
 // the warp replays that block from its saved start with per-step recording.
 //
-// Compositorial steps at prime n multiply by 1 instead of n (the reference
-// skips them, iterate.cl:137-140): the drift stays one power of R per step and
-// the hit test at that step is masked off.
+// Each launch walks one residue chain.  The combined search (-! -c) walks the
+// factorial chain over n and then the compositorial chain over a multiplier
+// table holding n at composite n and 1 at prime n (the reference skips prime
+// n, iterate.cl:137-140, 181-184): multiplying by 1 keeps the drift at one
+// power of R per step, and the replay skips the test where the multiplier is
+// 1.  The fast path tests every step: at a prime n the compositorial value is
+// the previous step's, so an unmasked match there only repeats a hit already
+// seen and costs one replay, never a wrong record.  The per-step work is three
+// integer multiplies (IMAD.WIDE, IMAD, IMAD.HI), one compare and conditional
+// add for the reduction, and two compares for the hit test.
 #include "arith.cuh"
 #include "kernels.cuh"
 
@@ -30,7 +37,21 @@ constexpr unsigned kFull = 0xffffffffu;
 struct Cls32 {
     using W = uint32_t;
     using M = Mont32;
-    static constexpr int B = 16;
+    static constexpr int B = 8;           // block length with two candidates per thread
+    static constexpr int B_FUSED = 16;    // block length of the fused -! -c walk
+    static constexpr int NC = 2;          // candidates per thread in single-chain walks
+    static constexpr bool kSigned = true; // walk residues signed in (-p, p), p < 2^31
+    // fast walk step and its hit test: x = +-T (mod p) <=> |x| in {T, p - T}
+    __device__ static __forceinline__ W fstep(const M &m, W x, uint32_t n) {
+        return (W)redc31s((int32_t)x, n, (int32_t)m.p, m.pinv);
+    }
+    __device__ static __forceinline__ bool fhit(W x, W t, W nt) {
+        const uint32_t ax = (uint32_t)abs((int32_t)x);
+        return (ax == t) | (ax == nt);
+    }
+    __device__ static __forceinline__ W canon(const M &m, W x) { return (int32_t)x < 0 ? x + m.p : x; }
+    // x*K*R^-1 for the block restore (K < p < 2^31)
+    __device__ static __forceinline__ W restore(const M &m, W x, W K) { return fstep(m, x, K); }
     __device__ static __forceinline__ W step(const M &m, W s, uint32_t n) { return redc32(s, n, m.p, m.pinv); }
     __device__ static __forceinline__ W word(const M &m, W s, W w) { return redc32(s, w, m.p, m.pinv); }
     // checksum form: residue * 2^64 mod p from its class-32 Montgomery form
@@ -42,6 +63,13 @@ struct Cls64 {
     using W = uint64_t;
     using M = Mont64;
     static constexpr int B = 8;
+    static constexpr int B_FUSED = 8;
+    static constexpr int NC = 1;
+    static constexpr bool kSigned = false;
+    __device__ static __forceinline__ W fstep(const M &m, W x, uint32_t n) { return redc64_u32(x, n, m.p, m.pinv); }
+    __device__ static __forceinline__ bool fhit(W x, W t, W nt) { return (x == t) | (x == nt); }
+    __device__ static __forceinline__ W canon(const M &, W x) { return x; }
+    __device__ static __forceinline__ W restore(const M &m, W x, W K) { return m.mul(x, K); }
     __device__ static __forceinline__ W step(const M &m, W s, uint32_t n) { return redc64_u32(s, n, m.p, m.pinv); }
     __device__ static __forceinline__ W word(const M &m, W s, W w) { return redc64(s, w, m.p, m.pinv); }
     __device__ static __forceinline__ uint64_t term(const M &, W s) { return s; }
@@ -116,149 +144,222 @@ __device__ __forceinline__ void append_hit(bool hit, uint64_t p, int32_t nc, int
     }
 }
 
-// composite flags for n .. n+B-1 (bit j set <=> n+j composite); uniform loads
+// Multipliers of steps k .. k+B-1 (uniform across the warp): k itself when
+// `mult` is null, else mult[k - base ...] (vector loads when aligned).
 template <int B>
-__device__ __forceinline__ uint32_t comp_bits(const IterArgs &a, uint32_t n) {
-    const uint32_t off = n - a.nmin;
-    const uint32_t k = off >> 5, sh = off & 31;
-    const uint64_t v = ((uint64_t)__ldg(a.primebits + k + 1) << 32) | __ldg(a.primebits + k);
-    return ~(uint32_t)(v >> sh) & (uint32_t)((1ull << B) - 1);
+__device__ __forceinline__ void load_mult(const uint32_t *mult, uint32_t base, uint32_t k, bool vec, uint32_t (&mv)[B]) {
+    if (!mult) {
+#pragma unroll
+        for (int j = 0; j < B; ++j) mv[j] = k + j;
+    } else if (vec) {
+        const uint4 *src = reinterpret_cast<const uint4 *>(mult + (k - base));
+#pragma unroll
+        for (int j = 0; j < B / 4; ++j) {
+            const uint4 v = __ldg(src + j);
+            mv[4 * j] = v.x;
+            mv[4 * j + 1] = v.y;
+            mv[4 * j + 2] = v.z;
+            mv[4 * j + 3] = v.w;
+        }
+    } else {
+#pragma unroll
+        for (int j = 0; j < B; ++j) mv[j] = __ldg(mult + (k - base) + j);
+    }
 }
 
-// Replay `len` steps from the block start with explicit per-step recording.
-// X: factorial (or primorial / compositorial-only) residue, Y: compositorial
-// residue of the combined search.
-template <class T, unsigned MODE>
-__device__ __noinline__ void replay_block(const typename T::M &m, typename T::W x, typename T::W y,
-                                          uint32_t n, int len, uint32_t cbits, const uint32_t *q,
-                                          bool active, const HitBuf &h) {
+// Replay `len` steps of one chain from the block start x with the exact
+// per-step test and record the hits.  A multiplier of 1 marks a prime n of
+// the compositorial walk: nothing was multiplied there, so nothing is tested.
+template <class T>
+__device__ __noinline__ void replay_chain(const typename T::M m, typename T::W x, const uint32_t *mult,
+                                          uint32_t base, uint32_t k, int len, int32_t type, bool active,
+                                          const HitBuf h) {
     using W = typename T::W;
+    x = T::canon(m, x);
     W t = 1;
     for (int j = 0; j < len; ++j) {
         if (j) t = m.mul(t, 1);
-        const W nt = m.p - t;
-        if (MODE == PFC_PRIMORIAL) {
-            const uint32_t qq = __ldg(q + j);
-            x = T::step(m, x, qq);
-            const bool hit = active && (x == t || x == nt);
-            append_hit(hit, m.p, x == t ? -(int32_t)qq : (int32_t)qq, PFC_TYPE_PRIMORIAL, h);
-        } else {
-            const uint32_t nn = n + j;
-            if (MODE & PFC_FACTORIAL) {
-                x = T::step(m, x, nn);
-                const bool hit = active && (x == t || x == nt);
-                append_hit(hit, m.p, x == t ? -(int32_t)nn : (int32_t)nn, PFC_TYPE_FACTORIAL, h);
-            }
-            if (MODE & PFC_COMPOSITORIAL) {
-                const bool comp = (cbits >> j) & 1;
-                W &z = (MODE & PFC_FACTORIAL) ? y : x;
-                z = T::step(m, z, comp ? nn : 1u);
-                const bool hit = active && comp && (z == t || z == nt);
-                append_hit(hit, m.p, z == t ? -(int32_t)nn : (int32_t)nn, PFC_TYPE_COMPOSITORIAL, h);
-            }
-        }
+        const uint32_t mul = mult ? __ldg(mult + (k - base) + j) : k + j;
+        x = T::step(m, x, mul);
+        const bool hit = active && mul != 1u && (x == t || x == m.p - t);
+        append_hit(hit, m.p, x == t ? -(int32_t)mul : (int32_t)mul, type, h);
     }
 }
 
-template <class T, unsigned MODE>
-__global__ void __launch_bounds__(256) iterate_kernel(ClassBuf<typename T::W> c, IterArgs a, HitBuf h) {
+// One walk launch.  Each thread runs two independent streams of steps so
+// that the scheduler always has a second dependent chain to interleave:
+//   FUSED (-! -c): the factorial chain (multiplier n) and the compositorial
+//     chain (multiplier table) of one candidate, sharing its targets;
+//   otherwise NC candidates (1 or 2) on the same multiplier sequence.
+// Inactive streams hold 0, which never matches a target (targets are in
+// [1, p-1]), so they never trigger a replay.
+template <class T, int NC, bool FUSED>
+__global__ void __launch_bounds__(256) walk_kernel(ClassBuf<typename T::W> c, WalkArgs a, HitBuf h) {
     using W = typename T::W;
-    constexpr int B = T::B;
-    constexpr bool kF = (MODE & PFC_FACTORIAL) != 0;
-    constexpr bool kC = (MODE & PFC_COMPOSITORIAL) != 0;
-    constexpr bool kP = MODE == PFC_PRIMORIAL;
-    constexpr bool kFC = kF && kC;
-
+    constexpr int B = FUSED ? T::B_FUSED : T::B;
+    constexpr int NS = FUSED ? 2 : NC;   // streams per thread
     const uint32_t cnt = min(*c.count, c.cap);
-    if (blockIdx.x * blockDim.x >= cnt) return;  // whole block idle
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    const bool active = i < cnt;
+    const uint32_t blk0 = blockIdx.x * blockDim.x * NC;
+    if (blk0 >= cnt) return;  // whole block idle
 
-    typename T::M m;
-    m.init(active ? c.p[i] : (W)3);
-    W x = active ? c.s0[i] : 0;
-    W y = (kFC && active) ? c.s1[i] : 0;
-
-    W tg[B], ntg[B];
-    tg[0] = 1;
+    uint32_t idx[NC];
+    bool act[NC];
+    typename T::M m[NC];
+    W x[NS];
 #pragma unroll
-    for (int j = 1; j < B; ++j) tg[j] = m.mul(tg[j - 1], 1);
+    for (int s = 0; s < NC; ++s) {
+        idx[s] = blk0 + s * blockDim.x + threadIdx.x;
+        act[s] = idx[s] < cnt;
+        m[s].init(act[s] ? c.p[idx[s]] : (W)3);
+    }
+    if (FUSED) {
+        x[0] = act[0] ? c.s0[idx[0]] : 0;
+        x[NS - 1] = act[0] ? c.s1[idx[0]] : 0;
+    } else {
+        W *st = a.chain ? c.s1 : c.s0;
 #pragma unroll
-    for (int j = 0; j < B; ++j) ntg[j] = m.p - tg[j];
-    const W K = m.mont_R_pow(B);
+        for (int s = 0; s < NC; ++s) x[s] = act[s] ? st[idx[s]] : 0;
+    }
 
-    uint32_t n = a.lo;
+    W tg[NC][B], ntg[NC][B], K[NC];
+#pragma unroll
+    for (int s = 0; s < NC; ++s) {
+        tg[s][0] = 1;
+#pragma unroll
+        for (int j = 1; j < B; ++j) tg[s][j] = m[s].mul(tg[s][j - 1], 1);
+#pragma unroll
+        for (int j = 0; j < B; ++j) ntg[s][j] = m[s].p - tg[s][j];
+        K[s] = m[s].mont_R_pow(B);
+    }
+
+    const uint32_t *mult0 = FUSED ? nullptr : a.mult;
+    const uint32_t *mult1 = a.mult2;
+    const bool vec = ((a.lo - a.base) & 3u) == 0;
+    uint32_t k = a.lo;
     const uint32_t nblk = (a.hi - a.lo) / B;
-    for (uint32_t b = 0; b < nblk; ++b, n += B) {
-        const W x0 = x, y0 = y;
-        const uint32_t cb = kC ? comp_bits<B>(a, n) : 0u;
+    for (uint32_t b = 0; b < nblk; ++b, k += B) {
+        uint32_t mv[B], cv[B];
+        load_mult<B>(mult0, a.base, k, vec, mv);
+        if (FUSED) load_mult<B>(mult1, a.base, k, vec, cv);
+        W xs[NS];
+#pragma unroll
+        for (int s = 0; s < NS; ++s) xs[s] = x[s];
         bool any = false;
-        if (kP) {
-            const uint32_t *q = a.qlist + n;
 #pragma unroll
-            for (int j = 0; j < B; ++j) {
-                x = T::step(m, x, __ldg(q + j));
-                any |= (x == tg[j]) | (x == ntg[j]);
-            }
-        } else {
+        for (int j = 0; j < B; ++j) {
+            if (FUSED) {
+                x[0] = T::fstep(m[0], x[0], mv[j]);
+                x[NS - 1] = T::fstep(m[0], x[NS - 1], cv[j]);
+                any |= T::fhit(x[0], tg[0][j], ntg[0][j]) | T::fhit(x[NS - 1], tg[0][j], ntg[0][j]);
+            } else {
 #pragma unroll
-            for (int j = 0; j < B; ++j) {
-                if (kF) {
-                    x = T::step(m, x, n + j);
-                    any |= (x == tg[j]) | (x == ntg[j]);
-                }
-                if (kC) {
-                    const bool comp = (cb >> j) & 1;
-                    W &z = kFC ? y : x;
-                    z = T::step(m, z, comp ? n + j : 1u);
-                    any |= comp & ((z == tg[j]) | (z == ntg[j]));
+                for (int s = 0; s < NC; ++s) {
+                    x[s] = T::fstep(m[s], x[s], mv[j]);
+                    any |= T::fhit(x[s], tg[s][j], ntg[s][j]);
                 }
             }
         }
-        if (__any_sync(kFull, any && active))
-            replay_block<T, MODE>(m, x0, y0, n, B, cb, kP ? a.qlist + n : nullptr, active, h);
-        x = m.mul(x, K);
-        if (kFC) y = m.mul(y, K);
+        if (__any_sync(kFull, any)) {
+            if (FUSED) {
+                replay_chain<T>(m[0], xs[0], nullptr, a.base, k, B, a.type, act[0], h);
+                replay_chain<T>(m[0], xs[NS - 1], mult1, a.base, k, B, a.type2, act[0], h);
+            } else {
+#pragma unroll
+                for (int s = 0; s < NC; ++s) replay_chain<T>(m[s], xs[s], mult0, a.base, k, B, a.type, act[s], h);
+            }
+        }
+        // back to Montgomery form (class 32: |x*K| < p^2 < p*2^31)
+        if (FUSED) {
+            x[0] = T::restore(m[0], x[0], K[0]);
+            x[NS - 1] = T::restore(m[0], x[NS - 1], K[0]);
+        } else {
+#pragma unroll
+            for (int s = 0; s < NC; ++s) x[s] = T::restore(m[s], x[s], K[s]);
+        }
     }
 
-    // tail of fewer than B steps
-    const int r = (int)(a.hi - n);
-    if (r > 0) {
-        const W x0 = x, y0 = y;
-        const uint32_t cb = kC ? comp_bits<B>(a, n) : 0u;
+    // canonical form for the tail, the state store and the check kernel
+    if (FUSED) {
+        x[0] = T::canon(m[0], x[0]);
+        x[NS - 1] = T::canon(m[0], x[NS - 1]);
+    } else {
+#pragma unroll
+        for (int s = 0; s < NC; ++s) x[s] = T::canon(m[s], x[s]);
+    }
+    const int r = (int)(a.hi - k);
+    if (r > 0) {  // tail of fewer than B steps
+        W xs[NS];
+#pragma unroll
+        for (int s = 0; s < NS; ++s) xs[s] = x[s];
         bool any = false;
 #pragma unroll
         for (int j = 0; j < B; ++j) {
             if (j < r) {
-                if (kP) {
-                    x = T::step(m, x, __ldg(a.qlist + n + j));
-                    any |= (x == tg[j]) | (x == ntg[j]);
+                const uint32_t mul0 = mult0 ? __ldg(mult0 + (k - a.base) + j) : k + j;
+                if (FUSED) {
+                    const uint32_t mul1 = __ldg(mult1 + (k - a.base) + j);
+                    x[0] = T::step(m[0], x[0], mul0);
+                    x[NS - 1] = T::step(m[0], x[NS - 1], mul1);
+                    any |= (x[0] == tg[0][j]) | (x[0] == ntg[0][j]) | (x[NS - 1] == tg[0][j]) |
+                           (x[NS - 1] == ntg[0][j]);
                 } else {
-                    if (kF) {
-                        x = T::step(m, x, n + j);
-                        any |= (x == tg[j]) | (x == ntg[j]);
-                    }
-                    if (kC) {
-                        const bool comp = (cb >> j) & 1;
-                        W &z = kFC ? y : x;
-                        z = T::step(m, z, comp ? n + j : 1u);
-                        any |= comp & ((z == tg[j]) | (z == ntg[j]));
+#pragma unroll
+                    for (int s = 0; s < NC; ++s) {
+                        x[s] = T::step(m[s], x[s], mul0);
+                        any |= (x[s] == tg[s][j]) | (x[s] == ntg[s][j]);
                     }
                 }
             }
         }
-        if (__any_sync(kFull, any && active))
-            replay_block<T, MODE>(m, x0, y0, n, r, cb, kP ? a.qlist + n : nullptr, active, h);
-        const W Kr = m.mont_R_pow((uint64_t)r);
-        x = m.mul(x, Kr);
-        if (kFC) y = m.mul(y, Kr);
+        if (__any_sync(kFull, any)) {
+            if (FUSED) {
+                replay_chain<T>(m[0], xs[0], nullptr, a.base, k, r, a.type, act[0], h);
+                replay_chain<T>(m[0], xs[NS - 1], mult1, a.base, k, r, a.type2, act[0], h);
+            } else {
+#pragma unroll
+                for (int s = 0; s < NC; ++s) replay_chain<T>(m[s], xs[s], mult0, a.base, k, r, a.type, act[s], h);
+            }
+        }
+#pragma unroll
+        for (int s = 0; s < NC; ++s) {
+            const W Kr = m[s].mont_R_pow((uint64_t)r);
+            if (FUSED) {
+                x[0] = m[0].mul(x[0], Kr);
+                x[NS - 1] = m[0].mul(x[NS - 1], Kr);
+            } else {
+                x[s] = m[s].mul(x[s], Kr);
+            }
+        }
     }
 
-    if (active) {
-        c.s0[i] = x;
-        if (kFC) c.s1[i] = y;
-        if (c.nnext[i] == a.lo) c.nnext[i] = a.hi;
-        else c.nnext[i] = 0xffffffffu;   // out-of-order chunk: fails the check
+    const uint32_t walked = (a.hi - a.lo) * (FUSED ? 2u : 1u);
+    if (FUSED) {
+        if (act[0]) {
+            c.s0[idx[0]] = x[0];
+            c.s1[idx[0]] = x[NS - 1];
+            c.nnext[idx[0]] += walked;
+        }
+    } else {
+        W *st = a.chain ? c.s1 : c.s0;
+#pragma unroll
+        for (int s = 0; s < NC; ++s)
+            if (act[s]) {
+                st[idx[s]] = x[s];
+                c.nnext[idx[s]] += walked;
+            }
+    }
+}
+
+__global__ void cmult_kernel(uint32_t *out, const uint32_t *primebits, uint32_t nmin, uint32_t lo, uint32_t len,
+                             uint32_t padded) {
+    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < padded; k += gridDim.x * blockDim.x) {
+        uint32_t v = 1u;
+        if (k < len) {
+            const uint32_t n = lo + k, off = n - nmin;
+            const bool prime = (__ldg(primebits + (off >> 5)) >> (off & 31)) & 1u;
+            v = prime ? 1u : n;
+        }
+        out[k] = v;
     }
 }
 
@@ -275,9 +376,12 @@ __global__ void __launch_bounds__(256) check_kernel(ClassBuf<typename T::W> c, C
     if (active) {
         typename T::M m;
         m.init(c.p[i]);
-        term = T::term(m, c.s0[i]);                         // check.cl:59,115,161
+        typename T::W s0 = c.s0[i], s1 = c.s1[i];
+        if (s0 >= m.p) s0 -= m.p;                           // walks leave [0, 2p)
+        if (s1 >= m.p) s1 -= m.p;
+        term = T::term(m, s0);                              // check.cl:59,115,161
         if (a.mode != PFC_PRIMORIAL) term += T::mont64_of(m, a.nlast);
-        if (a.mode == (PFC_FACTORIAL | PFC_COMPOSITORIAL)) term += T::term(m, c.s1[i]);
+        if (a.mode == (PFC_FACTORIAL | PFC_COMPOSITORIAL)) term += T::term(m, s1);
         bad = c.nnext[i] != a.nend;                         // check.cl:61-73
     }
 #pragma unroll
@@ -302,25 +406,31 @@ int launch_setup64(const ClassBuf<uint64_t> &c, const SetupArgs<uint64_t> &a, cu
 }
 
 template <class T>
-static int launch_iter(const ClassBuf<typename T::W> &c, const IterArgs &a, const HitBuf &h, cudaStream_t st) {
+static int launch_walk(const ClassBuf<typename T::W> &c, const WalkArgs &a, const HitBuf &h, cudaStream_t st) {
     if (!c.cap || a.hi <= a.lo) return 0;
-    const unsigned g = grid_for(c.cap);
-    switch (a.mode) {
-        case PFC_FACTORIAL: iterate_kernel<T, PFC_FACTORIAL><<<g, 256, 0, st>>>(c, a, h); break;
-        case PFC_PRIMORIAL: iterate_kernel<T, PFC_PRIMORIAL><<<g, 256, 0, st>>>(c, a, h); break;
-        case PFC_COMPOSITORIAL: iterate_kernel<T, PFC_COMPOSITORIAL><<<g, 256, 0, st>>>(c, a, h); break;
-        case PFC_FACTORIAL | PFC_COMPOSITORIAL:
-            iterate_kernel<T, PFC_FACTORIAL | PFC_COMPOSITORIAL><<<g, 256, 0, st>>>(c, a, h);
-            break;
-        default: return 0;
+    if (a.mult2) {
+        walk_kernel<T, 1, true><<<grid_for(c.cap), 256, 0, st>>>(c, a, h);
+    } else {
+        const uint32_t per_block = 256u * T::NC;
+        walk_kernel<T, T::NC, false><<<(c.cap + per_block - 1) / per_block, 256, 0, st>>>(c, a, h);
     }
     return 1;
 }
-int launch_iterate32(const ClassBuf<uint32_t> &c, const IterArgs &a, const HitBuf &h, cudaStream_t st) {
-    return launch_iter<Cls32>(c, a, h, st);
+int launch_walk32(const ClassBuf<uint32_t> &c, const WalkArgs &a, const HitBuf &h, cudaStream_t st) {
+    return launch_walk<Cls32>(c, a, h, st);
 }
-int launch_iterate64(const ClassBuf<uint64_t> &c, const IterArgs &a, const HitBuf &h, cudaStream_t st) {
-    return launch_iter<Cls64>(c, a, h, st);
+int launch_walk64(const ClassBuf<uint64_t> &c, const WalkArgs &a, const HitBuf &h, cudaStream_t st) {
+    return launch_walk<Cls64>(c, a, h, st);
+}
+
+int launch_cmult(uint32_t *out, const uint32_t *primebits, uint32_t nmin, uint32_t lo, uint32_t hi,
+                 cudaStream_t st) {
+    const uint32_t len = hi - lo, padded = (len + 15u) & ~15u;
+    unsigned blocks = (padded + 255) / 256;
+    if (blocks > 4096) blocks = 4096;
+    if (!padded) return 0;
+    cmult_kernel<<<blocks, 256, 0, st>>>(out, primebits, nmin, lo, len, padded);
+    return 1;
 }
 
 int launch_check32(const ClassBuf<uint32_t> &c, const CheckArgs &a, cudaStream_t st) {
