@@ -315,7 +315,7 @@ def run_ours(args, wl, world, rank, local, dist):
         steps_per_cand = ncomp
     else:
         steps_per_cand = wl["nmax"] - wl["nmin"]
-    cls32 = hi <= 2**32
+    cls32 = hi <= 2**31
     ops_per_mulmod = 4 if cls32 else 16
     alg_ops = cands_per_step * steps_per_cand * ops_per_mulmod
     it_s = float(np.mean(it_ms)) * 1e-3
@@ -323,8 +323,10 @@ def run_ours(args, wl, world, rank, local, dist):
     peaks_all = {k: pfc.int_peak(local, v) / 1e12 for k, v in
                  (("imad", 0), ("mul_hi", 1), ("imad_wide", 2), ("iadd_xor", 3))}
     achieved = alg_ops / it_s
+    # DRAM bytes of the walk launches of one step, from the committed ncu
+    # capture of this workload (profiles/walk_kernel_traffic.json)
     traffic = None
-    tfile = os.path.join(ROOT, "profiles", "iterate_traffic.json")
+    tfile = os.path.join(ROOT, "profiles", "walk_kernel_traffic.json")
     if os.path.exists(tfile):
         try:
             t = json.load(open(tfile))
@@ -374,7 +376,10 @@ def run_ours(args, wl, world, rank, local, dist):
                        "device": name, "sms": sms},
             "roofline": {"bound": "int (IMAD pipe)", "achieved": achieved / 1e12, "peak": peak / 1e12,
                          "unit": "Tops/s (32-bit integer multiply-add)", "frac": achieved / peak,
-                         "traffic": traffic, "kernel": "iterate_kernel<%s,%d>" % ("Cls32" if cls32 else "Cls64", mode),
+                         "traffic": traffic,
+                         "kernel": "walk_kernel<%s>" % ("Cls32" if cls32 else "Cls64"),
+                         "alg_ops_per_step": alg_ops,
+                         "ops_per_mulmod": ops_per_mulmod,
                          "kernel_ms_per_step": it_s * 1e3,
                          "peak_source": "measured in this run (pfc_bench_int_peak, 32-bit IMAD chains)",
                          "int_peaks_tops": peaks_all},
