@@ -183,6 +183,41 @@ int pfc_is_prime(uint64_t p);
  * returns the length written (without NUL), or a negative code. */
 int pfc_format_factor(const pfc_factor *f, char *buf, size_t cap);
 
+/* --------------------------------------------------- allocation-free segment */
+
+/* Size of the device array that pfc_segment_noalloc works in: 16 MiB, held by
+ * every GPU that loads this library from its first use until the process
+ * exits. */
+#define PFC_NOALLOC_SCRATCH_BYTES (16u << 20)
+
+/* One p-segment [p_lo, p_hi) of a search (the work of pfc_segment) without
+ * allocating any device memory: for callers that cannot call cudaMalloc or
+ * cudaFree while they run this path, such as a server that has reserved the
+ * whole device under its own budget and admits work against it, or a host
+ * that must not issue those calls while its other streams are busy (cudaFree
+ * synchronises the device).  No counterpart in the reference.
+ *
+ * The caller passes device buffers: d_hits (capacity hit_cap records; hits
+ * beyond it are counted, not written) and d_totals (4 x uint64): the wrapping
+ * sum of the checksum terms, the candidate count, the hit count, and flags
+ * (bit 0 candidate overflow, bit 1 n-counter validation failure).  Everything
+ * else lives in one file-scope device array of PFC_NOALLOC_SCRATCH_BYTES.
+ * Work is enqueued on `stream` (a cudaStream_t, 0 for the default stream) on
+ * the current device, and the call returns after that stream has finished it.
+ *
+ * Limits (PFC_ERR_ARG beyond them): at most 2^18 expected candidates per size
+ * class (p < 2^31 and p >= 2^31; roughly (p_hi - p_lo) / ln p_lo <= 2^18 / 1.25),
+ * nmax - nmin <= 2^22, at most 2^18 primes in [nmin, nmax) for n#, and setup
+ * tables of at most 2^17 32-bit and 2^16 64-bit words (nmin up to a few 10^5).
+ *
+ * The first call on each device resolves the device address of the array and
+ * stores the sieve patterns in it; make that first call before any stream
+ * capture.  All calls on a device share the array and it keeps the last call's
+ * contents (the call clears what must start at zero): calls that overlap on
+ * the GPU race, so issue them one at a time per device. */
+int pfc_segment_noalloc(unsigned mode, uint32_t nmin, uint32_t nmax, uint64_t p_lo, uint64_t p_hi,
+                        pfc_factor *d_hits, uint64_t hit_cap, uint64_t *d_totals, void *stream);
+
 /* ------------------------------------------------------------ measurement */
 
 /* Throughput of the integer pipes on `device`, in operations per second:

@@ -81,6 +81,7 @@ def lib():
             "pfc_format_factor": (ctypes.c_int, [vp, ctypes.c_char_p, sz]),
             "pfc_status_string": (ctypes.c_char_p, [ctypes.c_int]),
             "pfc_bench_int_peak": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, P(ctypes.c_double)]),
+            "pfc_segment_noalloc": (ctypes.c_int, [ctypes.c_uint, u32, u32, u64, u64, vp, u64, vp, vp]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(L, name)
