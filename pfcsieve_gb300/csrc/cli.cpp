@@ -452,6 +452,17 @@ static bool prepare_search(workStatus &st, Search &sd) {
     return true;
 }
 
+// Environment knobs: PFCSIEVE_CHECKPOINT_SECONDS (default 60, the reference's
+// cadence, cl_sieve.cpp:1581), PFCSIEVE_SEGMENT_SPAN (p-range per segment;
+// default: sized by the library to the device memory) and
+// PFCSIEVE_EXIT_AFTER_CHECKPOINT=k, a host-side crash for resume tests: the
+// process exits with status 3 right after writing its k-th checkpoint, when no
+// kernel is in flight (the checkpoint follows a synchronising drain).
+static double env_double(const char *name, double dflt) {
+    const char *v = getenv(name);
+    return (v && *v) ? strtod(v, nullptr) : dflt;
+}
+
 // the reference's cl_sieve() loop (cl_sieve.cpp:1328-1761), after
 // prepare_search()
 static void run_search(pfc_ctx *ctx, workStatus &st, Search &sd) {
@@ -463,12 +474,17 @@ static void run_search(pfc_ctx *ctx, workStatus &st, Search &sd) {
     fprintf(stderr, "Starting Sieve...\n");
     printf("Starting Sieve...\n");
     uint64_t term_prev = 0, count_prev = 0;
+    const double ckpt_secs = env_double("PFCSIEVE_CHECKPOINT_SECONDS", 60.0);
+    const double span = env_double("PFCSIEVE_SEGMENT_SPAN", 0.0);
+    const int exit_after = (int)env_double("PFCSIEVE_EXIT_AFTER_CHECKPOINT", 0.0);
+    int ckpts = 0;
     auto last_progress = std::chrono::steady_clock::now(), last_ckpt = last_progress;
     const double irsize = 1.0 / (double)(st.pmax - st.pmin ? st.pmax - st.pmin : 1);
     while (job && st.p < st.pmax) {
         uint64_t hi = 0;
         rc = pfc_job_segment_end(job, st.p, &hi);
         if (rc) die_status("pfc_job_segment_end", rc);
+        if (span >= 1.0 && (double)(hi - st.p) > span) hi = st.p + (uint64_t)span;
         rc = pfc_segment(job, st.p, hi);
         if (rc) die_status("pfc_segment", rc);
         st.p = hi;
@@ -477,11 +493,15 @@ static void run_search(pfc_ctx *ctx, workStatus &st, Search &sd) {
             printf("Sieve Progress: %.1f%%\n", (double)(st.p - st.pmin) * irsize * 100.0);
             last_progress = now;
         }
-        if (std::chrono::duration<double>(now - last_ckpt).count() > 60.0 && st.p < st.pmax) {
+        if (std::chrono::duration<double>(now - last_ckpt).count() >= ckpt_secs && st.p < st.pmax) {
             rc = get_results(job, st, sd, term_prev, count_prev);
             if (rc) die_status("results", rc);
             if (!sd.test) checkpoint(st, sd);
             last_ckpt = now;
+            if (exit_after > 0 && ++ckpts == exit_after) {
+                fflush(stdout);
+                exit(3);
+            }
         }
     }
     st.p = st.pmax;
