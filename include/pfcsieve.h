@@ -218,6 +218,65 @@ int pfc_format_factor(const pfc_factor *f, char *buf, size_t cap);
 int pfc_segment_noalloc(unsigned mode, uint32_t nmin, uint32_t nmax, uint64_t p_lo, uint64_t p_hi,
                         pfc_factor *d_hits, uint64_t hit_cap, uint64_t *d_totals, void *stream);
 
+/* ------------------------------------------------------------------ batches */
+
+/* Many searches on one device at once, with continuous batching.  The
+ * reference runs one search per process (main.cpp:219-323); a queue of small
+ * searches there leaves a large GPU mostly idle.  A batch takes searches as
+ * they arrive; every pfc_batch_step admits queued searches while the memory
+ * budget and the slots (4096) allow, runs one iteration in which each admitted
+ * search advances a bounded stretch of its setup and walk, and retires the
+ * searches that finished.  Results equal pfc_job_run's for the same search
+ * (hits, checksum terms, candidate count).  No counterpart in the reference. */
+typedef struct pfc_batch pfc_batch;
+
+typedef struct {
+    unsigned mode;          /* PFC_* mode bits, as for pfc_job_create */
+    uint32_t nmin, nmax;    /* n range [nmin, nmax), nmin >= 101, nmax - nmin <= 2^26 */
+    uint64_t pmin, pmax;    /* p range [pmin, pmax), pmin >= 3 */
+} pfc_job_desc;
+
+typedef struct {
+    int done;               /* 1 once the search has finished */
+    int status;             /* PFC_OK or the error that ended it */
+    uint64_t term_checksum; /* wrapping sum of the checksum terms (as pfc_job_totals) */
+    uint64_t primecount;    /* candidates sieved */
+    uint64_t pairs;         /* candidates x (nmax - nmin) */
+    uint64_t hits;          /* raw hits, before pfc_finalize_factors */
+} pfc_batch_status;
+
+int pfc_batch_create(pfc_ctx *ctx, pfc_batch **out);
+int pfc_batch_destroy(pfc_batch *b);
+/* Queue one search; *id names it in later calls. */
+int pfc_batch_submit(pfc_batch *b, const pfc_job_desc *desc, uint64_t *id);
+/* One iteration (admit, advance, retire); returns after the GPU finished it.
+ * *active / *queued (either may be NULL) receive the searches still running
+ * and still waiting. */
+int pfc_batch_step(pfc_batch *b, uint32_t *active, uint32_t *queued);
+int pfc_batch_result(pfc_batch *b, uint64_t id, pfc_batch_status *r);
+/* Raw hits of a finished search (PFC_ERR_HIT_OVERFLOW with *n = the count
+ * when cap is short). */
+int pfc_batch_take_hits(pfc_batch *b, uint64_t id, pfc_factor *buf, size_t cap, size_t *n);
+/* Forget a finished search. */
+int pfc_batch_release(pfc_batch *b, uint64_t id);
+/* Iterations run so far. */
+uint64_t pfc_batch_iterations(pfc_batch *b);
+/* Work of one iteration in candidate-steps (default 4e11; a class-64
+ * candidate step counts 3): smaller values give new searches and finished
+ * results a shorter wait, larger ones less host overhead per step. */
+int pfc_batch_set_iteration_work(pfc_batch *b, double candidate_steps);
+
+/* Where a batch's time went, summed over its steps. */
+typedef struct {
+    double step_s;          /* wall time inside pfc_batch_step */
+    double gpu_s;           /* iteration kernels: span from launch to the last class finishing */
+    double gpu32_s, gpu64_s;/* per size class (the two class kernels overlap) */
+    double prep_s;          /* host tables of new searches (overlaps the kernels) */
+    double admit_s;         /* uploads and candidate generation of new searches */
+    uint64_t iterations, tasks;
+} pfc_batch_times;
+int pfc_batch_timing(pfc_batch *b, pfc_batch_times *t);
+
 /* ------------------------------------------------------------ measurement */
 
 /* Throughput of the integer pipes on `device`, in operations per second:

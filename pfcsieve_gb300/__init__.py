@@ -33,6 +33,25 @@ PFC_ERR_NO_DEVICE = -9
 LIB_PATH = _build.LIB
 
 
+class JobDesc(ctypes.Structure):
+    """pfc_job_desc: one search submitted to a batch."""
+    _fields_ = [("mode", ctypes.c_uint), ("nmin", ctypes.c_uint32), ("nmax", ctypes.c_uint32),
+                ("pmin", ctypes.c_uint64), ("pmax", ctypes.c_uint64)]
+
+
+class BatchStatus(ctypes.Structure):
+    """pfc_batch_status: state and totals of one search in a batch."""
+    _fields_ = [("done", ctypes.c_int), ("status", ctypes.c_int), ("term_checksum", ctypes.c_uint64),
+                ("primecount", ctypes.c_uint64), ("pairs", ctypes.c_uint64), ("hits", ctypes.c_uint64)]
+
+
+class BatchTimes(ctypes.Structure):
+    """pfc_batch_times: where a batch's time went."""
+    _fields_ = [("step_s", ctypes.c_double), ("gpu_s", ctypes.c_double), ("gpu32_s", ctypes.c_double),
+                ("gpu64_s", ctypes.c_double), ("prep_s", ctypes.c_double), ("admit_s", ctypes.c_double),
+                ("iterations", ctypes.c_uint64), ("tasks", ctypes.c_uint64)]
+
+
 class PFCError(RuntimeError):
     def __init__(self, code, where=""):
         self.code = code
@@ -82,6 +101,16 @@ def lib():
             "pfc_status_string": (ctypes.c_char_p, [ctypes.c_int]),
             "pfc_bench_int_peak": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, P(ctypes.c_double)]),
             "pfc_segment_noalloc": (ctypes.c_int, [ctypes.c_uint, u32, u32, u64, u64, vp, u64, vp, vp]),
+            "pfc_batch_create": (ctypes.c_int, [vp, P(vp)]),
+            "pfc_batch_destroy": (ctypes.c_int, [vp]),
+            "pfc_batch_submit": (ctypes.c_int, [vp, P(JobDesc), P(u64)]),
+            "pfc_batch_step": (ctypes.c_int, [vp, P(u32), P(u32)]),
+            "pfc_batch_result": (ctypes.c_int, [vp, u64, P(BatchStatus)]),
+            "pfc_batch_take_hits": (ctypes.c_int, [vp, u64, vp, sz, P(sz)]),
+            "pfc_batch_release": (ctypes.c_int, [vp, u64]),
+            "pfc_batch_iterations": (u64, [vp]),
+            "pfc_batch_set_iteration_work": (ctypes.c_int, [vp, ctypes.c_double]),
+            "pfc_batch_timing": (ctypes.c_int, [vp, P(BatchTimes)]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(L, name)
@@ -246,6 +275,86 @@ class Job:
 
     def setup_mulmods(self, cls64):
         return lib().pfc_job_setup_mulmods(self.h, int(cls64))
+
+
+class Batch:
+    """Many searches on one device with continuous batching (pfc_batch_*).
+
+    submit() queues a search and returns its id; step() runs one iteration
+    (admit queued searches, advance every admitted one, retire finished ones);
+    result(id) gives the raw totals and hits of a finished search."""
+
+    def __init__(self, ctx, iteration_work=None):
+        self.ctx = ctx
+        h = ctypes.c_void_p()
+        _ck(lib().pfc_batch_create(ctx.h, ctypes.byref(h)), "pfc_batch_create")
+        self.h = h
+        if iteration_work is not None:
+            _ck(lib().pfc_batch_set_iteration_work(self.h, float(iteration_work)),
+                "pfc_batch_set_iteration_work")
+
+    def close(self):
+        if self.h:
+            lib().pfc_batch_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def submit(self, mode, nmin, nmax, pmin, pmax):
+        d = JobDesc(mode, nmin, nmax, pmin, pmax)
+        i = ctypes.c_uint64(0)
+        _ck(lib().pfc_batch_submit(self.h, ctypes.byref(d), ctypes.byref(i)), "pfc_batch_submit")
+        return i.value
+
+    def step(self):
+        """One iteration; returns (searches running, searches waiting)."""
+        a, q = ctypes.c_uint32(0), ctypes.c_uint32(0)
+        _ck(lib().pfc_batch_step(self.h, ctypes.byref(a), ctypes.byref(q)), "pfc_batch_step")
+        return a.value, q.value
+
+    def status(self, job_id):
+        r = BatchStatus()
+        _ck(lib().pfc_batch_result(self.h, job_id, ctypes.byref(r)), "pfc_batch_result")
+        return r
+
+    def hits(self, job_id):
+        n = ctypes.c_size_t(0)
+        rc = lib().pfc_batch_take_hits(self.h, job_id, None, 0, ctypes.byref(n))
+        if rc not in (PFC_OK, PFC_ERR_HIT_OVERFLOW):
+            _ck(rc, "pfc_batch_take_hits")
+        buf = np.zeros(max(n.value, 1), dtype=FACTOR_DTYPE)
+        _ck(lib().pfc_batch_take_hits(self.h, job_id, buf.ctypes.data, n.value, ctypes.byref(n)),
+            "pfc_batch_take_hits")
+        return buf[: n.value]
+
+    def release(self, job_id):
+        _ck(lib().pfc_batch_release(self.h, job_id), "pfc_batch_release")
+
+    @property
+    def iterations(self):
+        return lib().pfc_batch_iterations(self.h)
+
+    def timing(self):
+        t = BatchTimes()
+        _ck(lib().pfc_batch_timing(self.h, ctypes.byref(t)), "pfc_batch_timing")
+        return {k: getattr(t, k) for k, _ in BatchTimes._fields_}
+
+    def run(self):
+        """Step until every submitted search has finished."""
+        while True:
+            a, q = self.step()
+            if a == 0 and q == 0:
+                return
 
 
 def finalize(mode, nmax, hits, threads=2, verify=True):

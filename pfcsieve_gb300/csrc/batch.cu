@@ -1,0 +1,921 @@
+// batch.cu -- many sieve jobs on the GPU at once: the batched persistent
+// kernel and the iteration-level scheduler behind pfc_batch_* (continuous
+// batching).
+//
+// The reference runs one search per process and one kernel per stage
+// (cl_sieve.cpp:1563-1726); a small search there leaves most of a large GPU
+// idle.  Here every admitted job contributes blocks of candidates (256, or 512
+// for two-candidate class-32 walks).  Each block has a timeline: its setup
+// program as an op stream ([0, S): 0 = square, 1 = fork of the combined search,
+// any other value = a table word to multiply in), then its walk ([S, S+N): n
+// steps, or prime steps for n#).  One iteration gives every unfinished block a
+// task, a window of at most L positions of its timeline; a persistent kernel
+// per size class takes tasks from a device counter until the list is empty, so
+// jobs of every size and mode share the SMs.  Between iterations the host
+// admits new jobs as memory and slots allow, drains the hits (tagged with the
+// job slot) and retires finished jobs: requests that arrive while others run
+// join at the next iteration.
+//
+// Results equal the per-job path bit for bit: the same kernels (walk.cuh), the
+// same setup values (a job's op stream evaluates the same programs) and the
+// same check terms.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <deque>
+#include <map>
+#include <memory>
+#include <vector>
+
+#include "devmem.hpp"
+#include "walk.cuh"
+
+namespace pfc {
+
+// ------------------------------------------------------------- device side
+
+template <class W>
+struct JobDev {
+    unsigned mode;
+    uint32_t nmin, nlast;     // first n; nmax - 1
+    uint32_t nsetup, nwalk;   // timeline: [0, nsetup) setup ops, then nwalk walk steps
+    const W *ops;             // setup op stream
+    uint64_t corr_a, corr_b;  // drift corrections (first program; second of the combined search)
+    const uint32_t *cmult;    // compositorial multipliers of [nmin, nmax)
+    const uint32_t *qlist;    // primorial: primes in [nmin, nmax)
+    ClassBuf<W> c;
+    unsigned long long *termsum;
+    uint32_t *flags;
+};
+
+struct BatchStats {  // one per job slot
+    uint32_t counts[2];
+    uint32_t flags;
+    uint32_t pad;
+    unsigned long long termsum;
+};
+
+struct Task {
+    uint32_t slot, first, count, lo, hi;
+};
+
+template <class T, int NC, bool FUSED>
+__device__ void run_task(const JobDev<typename T::W> &J, const Task &t, const HitBuf &h) {
+    using W = typename T::W;
+    constexpr int NS = FUSED ? 2 : NC;
+    uint32_t idx[NC];
+    bool act[NC];
+    typename T::M m[NC];
+    const uint32_t end = t.first + t.count;
+#pragma unroll
+    for (int s = 0; s < NC; ++s) {
+        idx[s] = t.first + s * blockDim.x + threadIdx.x;
+        act[s] = idx[s] < end;
+        m[s].init(act[s] ? J.c.p[idx[s]] : (W)3);
+    }
+    const uint32_t S = J.nsetup, N = J.nwalk;
+    W x[NS];
+    uint32_t walked = 0;
+    if (t.lo < S) {
+        // setup part: evaluate ops [lo, min(hi, S)) of the job's program
+        W acc[NC], fork[NC];
+#pragma unroll
+        for (int s = 0; s < NC; ++s) {
+            acc[s] = t.lo == 0 ? m[s].one : (act[s] ? J.c.s0[idx[s]] : (W)0);
+            fork[s] = (FUSED && t.lo > 0 && act[s]) ? J.c.s1[idx[s]] : (W)0;
+        }
+        const uint32_t e = min(t.hi, S);
+        for (uint32_t i = t.lo; i < e; ++i) {
+            const W w = __ldg(J.ops + i);
+            if (w == 0) {
+#pragma unroll
+                for (int s = 0; s < NC; ++s) acc[s] = m[s].mul(acc[s], acc[s]);
+            } else if (w == 1) {
+#pragma unroll
+                for (int s = 0; s < NC; ++s) {
+                    acc[s] = m[s].mul(acc[s], m[s].mont_R_pow(J.corr_a));
+                    fork[s] = acc[s];
+                }
+            } else {
+#pragma unroll
+                for (int s = 0; s < NC; ++s) acc[s] = T::word(m[s], acc[s], w);
+            }
+        }
+        if (e == S) {
+#pragma unroll
+            for (int s = 0; s < NC; ++s) acc[s] = m[s].mul(acc[s], m[s].mont_R_pow(FUSED ? J.corr_b : J.corr_a));
+        }
+        if (e < S || (t.hi == S && N > 0)) {  // setup not finished, or the walk starts in a later task
+#pragma unroll
+            for (int s = 0; s < NC; ++s)
+                if (act[s]) {
+                    J.c.s0[idx[s]] = acc[s];
+                    if (FUSED) J.c.s1[idx[s]] = fork[s];
+                    J.c.nnext[idx[s]] = 0;
+                }
+            return;
+        }
+        if (FUSED) {
+            x[0] = acc[0];
+            x[NS - 1] = fork[0];
+        } else {
+#pragma unroll
+            for (int s = 0; s < NC; ++s) x[s] = acc[s];
+        }
+    } else {
+        if (FUSED) {
+            x[0] = act[0] ? J.c.s0[idx[0]] : 0;
+            x[NS - 1] = act[0] ? J.c.s1[idx[0]] : 0;
+        } else {
+#pragma unroll
+            for (int s = 0; s < NC; ++s) x[s] = act[s] ? J.c.s0[idx[s]] : 0;
+        }
+        walked = act[0] ? J.c.nnext[idx[0]] : 0;
+    }
+
+    // walk part: steps [max(lo, S) - S, hi - S) of the job's walk
+    const uint32_t wlo = max(t.lo, S) - S, whi = t.hi - S;
+    if (whi > wlo) {
+        WalkArgs a;
+        const bool prim = J.mode == PFC_PRIMORIAL;
+        const uint32_t base = prim ? 0u : J.nmin;
+        a.lo = base + wlo;
+        a.hi = base + whi;
+        a.base = base;
+        a.mult = nullptr;
+        a.mult2 = nullptr;
+        a.chain = 0;
+        a.type = a.type2 = 0;
+        if (FUSED) {
+            a.mult2 = J.cmult;
+            a.type = PFC_TYPE_FACTORIAL;
+            a.type2 = PFC_TYPE_COMPOSITORIAL;
+        } else if (prim) {
+            a.mult = J.qlist;
+            a.type = PFC_TYPE_PRIMORIAL;
+        } else if (J.mode == PFC_COMPOSITORIAL) {
+            a.mult = J.cmult;
+            a.type = PFC_TYPE_COMPOSITORIAL;
+        } else {
+            a.type = PFC_TYPE_FACTORIAL;
+        }
+        walk_streams<T, NC, FUSED>(m, x, act, a, h);
+        if (!FUSED && NC > 1) {
+            // walked counts are equal for the candidates of one thread
+        }
+        walked += (whi - wlo) * (FUSED ? 2u : 1u);
+    }
+
+    if (t.hi < S + N) {
+#pragma unroll
+        for (int s = 0; s < NC; ++s)
+            if (act[s]) {
+                J.c.s0[idx[s]] = FUSED ? x[0] : x[s];
+                if (FUSED) J.c.s1[idx[s]] = x[NS - 1];
+                J.c.nnext[idx[s]] = walked;
+            }
+        return;
+    }
+
+    // last task of the block: checksum terms (check.cl:59,115,161) and the
+    // step-count check of every candidate
+    unsigned long long term = 0;
+    bool bad = false;
+#pragma unroll
+    for (int s = 0; s < NC; ++s) {
+        if (!act[s]) continue;
+        const W x0 = FUSED ? x[0] : x[s];
+        term += T::term(m[s], x0);
+        if (J.mode != PFC_PRIMORIAL) term += T::mont64_of(m[s], J.nlast);
+        if (FUSED) term += T::term(m[s], x[NS - 1]);
+        bad |= walked != N * (FUSED ? 2u : 1u);
+    }
+#pragma unroll
+    for (int o = 16; o; o >>= 1) term += __shfl_down_sync(kFull, term, o);
+    if ((threadIdx.x & 31) == 0 && term) atomicAdd(J.termsum, term);
+    if (__any_sync(kFull, bad) && (threadIdx.x & 31) == 0) atomicOr(J.flags, 1u);
+}
+
+template <class T>
+__global__ void __launch_bounds__(256, 3) batch_kernel(const Task *tasks, const uint32_t *ntasks, unsigned *head,
+                                                    const JobDev<typename T::W> *jobs, HitBuf h) {
+    __shared__ Task st;
+    for (;;) {
+        if (threadIdx.x == 0) {
+            const unsigned i = atomicAdd(head, 1u);
+            if (i < *ntasks) st = tasks[i];
+            else st.slot = 0xffffffffu;
+        }
+        __syncthreads();
+        const Task t = st;
+        __syncthreads();
+        if (t.slot == 0xffffffffu) break;
+        const JobDev<typename T::W> J = jobs[t.slot];
+        HitBuf hh = h;
+        hh.tagval = t.slot;
+        if (J.mode == (PFC_FACTORIAL | PFC_COMPOSITORIAL)) run_task<T, 1, true>(J, t, hh);
+        else run_task<T, T::NC, false>(J, t, hh);
+    }
+}
+
+// ------------------------------------------------------------------ host side
+
+struct Block {
+    uint32_t first, count, pos;
+};
+
+// queued -> prepared (host tables built) -> ready (on the device, candidates
+// generated) -> running (blocks in the task list) -> done
+enum JobState { kQueued = 0, kPrepared, kReady, kRunning, kDone };
+
+struct BatchJob {
+    uint64_t id = 0;
+    unsigned mode = 0;
+    uint32_t nmin = 0, nmax = 0;
+    uint64_t pmin = 0, pmax = 0;
+    int state = kQueued;
+    uint32_t slot = 0;
+    // host tables, built by prepare_job
+    int prep_rc = PFC_OK;
+    std::vector<uint32_t> ops32, cmult, qlist;
+    std::vector<uint64_t> ops64;
+    uint64_t c32a = 0, c32b = 0, c64a = 0, c64b = 0;
+    uint32_t nwalk = 0;
+    bool use32 = false, use64 = false;
+    uint32_t cap32 = 0, cap64 = 0;
+    // device
+    DArr<uint32_t> d_ops32, d_cmult, d_qlist;
+    DArr<uint64_t> d_ops64;
+    DevClass<uint32_t> c32;
+    DevClass<uint64_t> c64;
+    std::vector<Block> b32, b64;
+    uint32_t tot32 = 0, tot64 = 0;  // timeline lengths (setup ops + walk steps)
+    // results
+    uint64_t termsum = 0, primecount = 0;
+    uint32_t flags = 0;
+    bool rerun = false;
+    int status = PFC_OK;
+    std::vector<pfc_factor> hits;
+};
+
+static double est_cands(uint64_t lo, uint64_t hi) {
+    if (hi <= lo) return 0;
+    const double a = (double)std::max<uint64_t>(lo, 114);
+    return (double)(hi - lo) / std::log(a) * 1.25 + 30.0;
+}
+
+// a setup program as one op stream: 0 = square, else a word to multiply in
+template <class W>
+static void append_ops(const HostProg<W> &h, std::vector<W> &ops) {
+    for (size_t g = 0; g + 2 < h.groups.size(); g += 3) {
+        ops.insert(ops.end(), h.groups[g + 2], (W)0);
+        ops.insert(ops.end(), h.words.begin() + h.groups[g], h.words.begin() + h.groups[g + 1]);
+    }
+    ops.insert(ops.end(), h.final_sq, (W)0);
+}
+
+static uint32_t prime_limit(const BatchJob *j) {
+    const uint32_t startN = j->nmin - 1;
+    return (j->mode & PFC_COMPOSITORIAL) ? j->nmax : std::max(startN, j->nmax - 1);
+}
+
+// Host tables of one search: the same programs, prime lists and multiplier
+// table pfc_job_create builds (from the batch's shared prime list).
+static void prepare_job(BatchJob *j, const std::vector<uint32_t> &cache) {
+    const uint32_t startN = j->nmin - 1;
+    const std::vector<uint32_t> primes(cache.begin(), std::upper_bound(cache.begin(), cache.end(), prime_limit(j)));
+    const std::vector<uint32_t> below(primes.begin(), std::upper_bound(primes.begin(), primes.end(), startN));
+    HostProg<uint32_t> a32, b32;
+    HostProg<uint64_t> a64, b64;
+    bool ok;
+    const unsigned mode = j->mode;
+    if (mode == PFC_FACTORIAL) ok = build_power_prog(startN, 0, primes, a32) && build_power_prog(startN, 0, primes, a64);
+    else if (mode == PFC_COMPOSITORIAL) ok = build_power_prog(startN, 1, primes, a32) && build_power_prog(startN, 1, primes, a64);
+    else if (mode == PFC_PRIMORIAL) ok = build_product_prog(below, a32) && build_product_prog(below, a64);
+    else
+        ok = build_power_prog(startN, 1, primes, a32) && build_power_prog(startN, 1, primes, a64) &&
+             build_product_prog(below, b32) && build_product_prog(below, b64);
+    if (!ok) {
+        j->prep_rc = PFC_ERR_ARG;
+        return;
+    }
+    append_ops(a32, j->ops32);
+    append_ops(a64, j->ops64);
+    j->c32a = a32.corr;
+    j->c64a = a64.corr;
+    if (mode == (PFC_FACTORIAL | PFC_COMPOSITORIAL)) {
+        j->ops32.push_back(1u);  // fork: the compositorial residue is complete here
+        j->ops64.push_back(1u);
+        append_ops(b32, j->ops32);
+        append_ops(b64, j->ops64);
+        j->c32b = b32.corr;
+        j->c64b = b64.corr;
+    }
+    if (mode & PFC_COMPOSITORIAL) {
+        // n at composite n, 1 at prime n (iterate.cl:137-140, 181-184), padded for vector loads
+        const std::vector<uint32_t> pb = prime_bitmap(j->nmin, j->nmax, primes);
+        j->cmult.assign((size_t)(j->nmax - j->nmin) + 16, 1u);
+        for (uint32_t k = 0; k < j->nmax - j->nmin; ++k)
+            if (!((pb[k >> 5] >> (k & 31)) & 1u)) j->cmult[k] = j->nmin + k;
+        j->nwalk = j->nmax - j->nmin;
+    } else if (mode == PFC_PRIMORIAL) {
+        j->qlist.assign(std::lower_bound(primes.begin(), primes.end(), j->nmin),
+                        std::lower_bound(primes.begin(), primes.end(), j->nmax));
+        j->nwalk = (uint32_t)j->qlist.size();
+        j->qlist.resize(j->qlist.size() + 32, 1u);
+    } else {
+        j->nwalk = j->nmax - j->nmin;
+    }
+    j->use32 = j->pmin < kClassSplit;
+    j->use64 = j->pmax > kClassSplit;
+    const double e32 = est_cands(j->pmin, std::min<uint64_t>(j->pmax, kClassSplit));
+    const double e64 = est_cands(std::max<uint64_t>(j->pmin, kClassSplit), j->pmax);
+    j->cap32 = j->use32 ? (uint32_t)std::min(e32, 4.0e9) : 0;
+    j->cap64 = j->use64 ? (uint32_t)std::min(e64, 4.0e9) : 0;
+    j->tot32 = (uint32_t)j->ops32.size() + j->nwalk;
+    j->tot64 = (uint32_t)j->ops64.size() + j->nwalk;
+    j->prep_rc = PFC_OK;
+}
+
+template <class W>
+static void free_vec(std::vector<W> &v) {
+    std::vector<W>().swap(v);
+}
+
+}  // namespace pfc
+
+using namespace pfc;
+
+struct pfc_batch {
+    pfc_ctx *ctx = nullptr;
+    static constexpr uint32_t kSlots = 4096;
+    cudaStream_t st32 = nullptr, st64 = nullptr;
+    cudaEvent_t ev = nullptr;
+    DArr<BatchStats> stats;
+    DArr<JobDev<uint32_t>> jobs32;
+    DArr<JobDev<uint64_t>> jobs64;
+    DArr<Task> tasks32, tasks64;
+    DArr<uint32_t> ctrl;  // [0] ntasks32, [1] ntasks64, [2] head32, [3] head64
+    DArr<pfc_factor> hits;
+    DArr<uint32_t> tags;
+    DArr<unsigned long long> hitcount;
+    BatchStats *h_stats = nullptr;       // pinned mirror of `stats`
+    unsigned long long *h_hitcount = nullptr;
+    std::map<uint64_t, std::unique_ptr<BatchJob>> all;
+    std::deque<BatchJob *> queued;       // kQueued and kPrepared, in arrival order
+    std::vector<BatchJob *> ready;       // kReady: join the next iteration
+    std::vector<BatchJob *> running;     // kRunning
+    std::vector<uint32_t> free_slots;
+    std::vector<uint32_t> prime_cache;   // primes up to cache_lim
+    uint32_t cache_lim = 0;
+    std::vector<Task> t32, t64;
+    uint64_t next_id = 1;
+    int grid32 = 0, grid64 = 0;
+    double work_per_iter = 4e11;         // candidate-steps per iteration (class 64 weighs 3)
+    uint64_t iterations = 0;
+    // timing: kernel spans (CUDA events) and host phases (wall clock)
+    cudaEvent_t ev_start = nullptr, ev_end32 = nullptr, ev_end64 = nullptr;
+    double gpu_s = 0, gpu32_s = 0, gpu64_s = 0, prep_s = 0, admit_s = 0, step_s = 0;
+    uint64_t tasks = 0;
+    size_t t32_n = 0, t64_n = 0;   // task counts of the iteration in flight
+};
+
+static double now_s() {
+    return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
+namespace {
+
+// Build the host tables of the queued searches that have none yet (at most
+// as many as there are free slots), in parallel across searches.
+void prepare_queued(pfc_batch *b) {
+    std::vector<BatchJob *> todo;
+    size_t room = b->free_slots.size();
+    for (BatchJob *j : b->queued) {
+        if (todo.size() >= room) break;
+        if (j->state == kQueued) todo.push_back(j);
+    }
+    if (todo.empty()) return;
+    uint32_t lim = 0;
+    for (BatchJob *j : todo) lim = std::max(lim, prime_limit(j));
+    if (lim > b->cache_lim) {
+        const uint32_t want = (uint32_t)std::min<uint64_t>(std::max<uint64_t>(lim, 2ull * b->cache_lim), 0x7FFFFFFFu);
+        b->prime_cache = primes_between(2, want);
+        b->cache_lim = want;
+    }
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int64_t k = 0; k < (int64_t)todo.size(); ++k) prepare_job(todo[k], b->prime_cache);
+    for (BatchJob *j : todo) j->state = kPrepared;
+}
+
+void release_device(pfc_batch *b, BatchJob *j) {
+    pfc_ctx *c = b->ctx;
+    j->d_ops32.release(c);
+    j->d_ops64.release(c);
+    j->d_cmult.release(c);
+    j->d_qlist.release(c);
+    j->c32.release(c);
+    j->c64.release(c);
+}
+
+int launch_job_gen(pfc_batch *b, BatchJob *j) {
+    pfc_ctx *c = b->ctx;
+    BatchStats *st = b->stats.p + j->slot;
+    CK(cudaMemsetAsync(st, 0, sizeof(BatchStats), c->st));
+    GenArgs g;
+    memset(&g, 0, sizeof(g));
+    const uint64_t base = j->pmin | 1;
+    g.base = base;
+    g.nodd = j->pmax > base ? (j->pmax - base + 1) / 2 : 0;
+    g.p32 = j->c32.p.p;
+    g.p64 = j->c64.p.p;
+    g.cap32 = j->use32 ? j->c32.cap : 0;
+    g.cap64 = j->use64 ? j->c64.cap : 0;
+    g.count = st->counts;
+    g.pat = c->d_pat;
+    static const uint32_t sp[kSmallPrimes] = {3,  5,  7,  11, 13, 17, 19, 23, 29, 31, 37,  41,  43,  47,  53,
+                                              59, 61, 67, 71, 73, 79, 83, 89, 97, 101, 103, 107, 109, 113};
+    for (int k = 0; k < kSmallPrimes; ++k) g.bmod[k] = (uint32_t)(base % sp[k]);
+    c->launches += launch_gen(g, c->sms, c->st);
+    CK(cudaGetLastError());
+    return PFC_OK;
+}
+
+// Device buffers, tables and candidate generation of one prepared search.
+// PFC_ERR_NOMEM leaves nothing allocated.
+int upload_job(pfc_batch *b, BatchJob *j) {
+    pfc_ctx *c = b->ctx;
+    cudaError_t e = j->d_ops32.upload(c, j->ops32);
+    if (e == cudaSuccess) e = j->d_ops64.upload(c, j->ops64);
+    if (e == cudaSuccess) e = j->d_cmult.upload(c, j->cmult);
+    if (e == cudaSuccess) e = j->d_qlist.upload(c, j->qlist);
+    if (e == cudaSuccess) e = j->c32.ensure(c, j->cap32);
+    if (e == cudaSuccess) e = j->c64.ensure(c, j->cap64);
+    if (e != cudaSuccess) {
+        release_device(b, j);
+        return cuda_fail(e);
+    }
+    return launch_job_gen(b, j);
+}
+
+template <class W>
+JobDev<W> job_view(pfc_batch *b, BatchJob *j, const DevClass<W> &cls, int which, const DArr<W> &ops, uint64_t ca,
+                   uint64_t cb, uint32_t nsetup) {
+    JobDev<W> d;
+    memset(&d, 0, sizeof(d));
+    d.mode = j->mode;
+    d.nmin = j->nmin;
+    d.nlast = j->nmax - 1;
+    d.nsetup = nsetup;
+    d.nwalk = j->nwalk;
+    d.ops = ops.p;
+    d.corr_a = ca;
+    d.corr_b = cb;
+    d.cmult = j->d_cmult.p;
+    d.qlist = j->d_qlist.p;
+    d.c = cls.view(b->stats.p[j->slot].counts + which);
+    d.termsum = &b->stats.p[j->slot].termsum;
+    d.flags = &b->stats.p[j->slot].flags;
+    return d;
+}
+
+// Move prepared searches onto the device while slots and the memory budget
+// allow; on return their candidates exist and their blocks are laid out.
+int admit_prepared(pfc_batch *b) {
+    pfc_ctx *c = b->ctx;
+    std::vector<BatchJob *> fresh;
+    while (!b->queued.empty() && b->queued.front()->state == kPrepared && !b->free_slots.empty()) {
+        BatchJob *j = b->queued.front();
+        if (j->prep_rc != PFC_OK) {
+            b->queued.pop_front();
+            j->state = kDone;
+            j->status = j->prep_rc;
+            continue;
+        }
+        j->slot = b->free_slots.back();
+        const int rc = upload_job(b, j);
+        if (rc == PFC_ERR_NOMEM && !(b->running.empty() && b->ready.empty() && fresh.empty()))
+            break;  // waits for running searches to free memory
+        b->queued.pop_front();
+        if (rc != PFC_OK) {
+            release_device(b, j);
+            j->state = kDone;
+            j->status = rc;
+            if (rc != PFC_ERR_NOMEM) return rc;
+            continue;
+        }
+        b->free_slots.pop_back();
+        fresh.push_back(j);
+    }
+    if (fresh.empty()) return PFC_OK;
+    // candidate counts; regenerate with exact capacities where an estimate was short
+    CK(cudaMemcpyAsync(b->h_stats, b->stats.p, sizeof(BatchStats) * pfc_batch::kSlots, cudaMemcpyDeviceToHost, c->st));
+    CK(cudaStreamSynchronize(c->st));
+    bool regen = false;
+    for (BatchJob *j : fresh) {
+        const BatchStats &s = b->h_stats[j->slot];
+        if ((j->use32 && s.counts[0] > j->c32.cap) || (j->use64 && s.counts[1] > j->c64.cap)) {
+            CK(j->c32.ensure(c, j->use32 ? s.counts[0] + 1024 : 0));
+            CK(j->c64.ensure(c, j->use64 ? s.counts[1] + 1024 : 0));
+            const int g = launch_job_gen(b, j);
+            if (g) return g;
+            regen = true;
+        }
+    }
+    if (regen) {
+        CK(cudaMemcpyAsync(b->h_stats, b->stats.p, sizeof(BatchStats) * pfc_batch::kSlots, cudaMemcpyDeviceToHost,
+                           c->st));
+        CK(cudaStreamSynchronize(c->st));
+    }
+    std::vector<JobDev<uint32_t>> v32(fresh.size());
+    std::vector<JobDev<uint64_t>> v64(fresh.size());
+    for (size_t f = 0; f < fresh.size(); ++f) {
+        BatchJob *j = fresh[f];
+        const BatchStats &s = b->h_stats[j->slot];
+        const uint32_t n32 = j->use32 ? s.counts[0] : 0;
+        const uint32_t n64 = j->use64 ? s.counts[1] : 0;
+        j->primecount = (uint64_t)n32 + n64;
+        const uint32_t per32 = (j->mode == (PFC_FACTORIAL | PFC_COMPOSITORIAL)) ? 256u : 256u * Cls32::NC;
+        const uint32_t per64 = 256u * Cls64::NC;
+        for (uint32_t k = 0; k < n32; k += per32) j->b32.push_back({k, std::min(per32, n32 - k), 0});
+        for (uint32_t k = 0; k < n64; k += per64) j->b64.push_back({k, std::min(per64, n64 - k), 0});
+        v32[f] = job_view<uint32_t>(b, j, j->c32, 0, j->d_ops32, j->c32a, j->c32b, (uint32_t)j->ops32.size());
+        v64[f] = job_view<uint64_t>(b, j, j->c64, 1, j->d_ops64, j->c64a, j->c64b, (uint32_t)j->ops64.size());
+        CK(cudaMemcpyAsync(b->jobs32.p + j->slot, &v32[f], sizeof(v32[f]), cudaMemcpyHostToDevice, c->st));
+        CK(cudaMemcpyAsync(b->jobs64.p + j->slot, &v64[f], sizeof(v64[f]), cudaMemcpyHostToDevice, c->st));
+        c->h2d += sizeof(v32[f]) + sizeof(v64[f]);
+    }
+    CK(cudaStreamSynchronize(c->st));
+    for (BatchJob *j : fresh) {
+        free_vec(j->ops32);  // on the device now; only the lengths are kept
+        free_vec(j->ops64);
+        free_vec(j->cmult);
+        free_vec(j->qlist);
+        j->state = kReady;
+        b->ready.push_back(j);
+    }
+    return PFC_OK;
+}
+
+// One task per unfinished block: a window of at most L timeline positions.
+// Returns the window length used.
+uint32_t build_tasks(pfc_batch *b) {
+    for (BatchJob *j : b->ready) {
+        j->state = kRunning;
+        b->running.push_back(j);
+    }
+    b->ready.clear();
+    double cands = 0;
+    for (BatchJob *j : b->running) {
+        for (const Block &k : j->b32) cands += k.pos < j->tot32 ? k.count : 0;
+        for (const Block &k : j->b64) cands += k.pos < j->tot64 ? 3.0 * k.count : 0;
+    }
+    const double Ld = std::max(64.0, std::min(b->work_per_iter / std::max(cands, 1.0), 4194304.0));
+    const uint32_t L = ((uint32_t)Ld + 15u) & ~15u;
+    b->t32.clear();
+    b->t64.clear();
+    for (BatchJob *j : b->running) {
+        for (const Block &k : j->b32)
+            if (k.pos < j->tot32)
+                b->t32.push_back({j->slot, k.first, k.count, k.pos, (uint32_t)std::min<uint64_t>((uint64_t)k.pos + L, j->tot32)});
+        for (const Block &k : j->b64)
+            if (k.pos < j->tot64)
+                b->t64.push_back({j->slot, k.first, k.count, k.pos, (uint32_t)std::min<uint64_t>((uint64_t)k.pos + L, j->tot64)});
+    }
+    return L;
+}
+
+int launch_iteration(pfc_batch *b) {
+    pfc_ctx *c = b->ctx;
+    const size_t n32 = b->t32.size(), n64 = b->t64.size();
+    if (b->tasks32.n < n32) CK(b->tasks32.alloc(c, n32 + n32 / 2 + 64));
+    if (b->tasks64.n < n64) CK(b->tasks64.alloc(c, n64 + n64 / 2 + 64));
+    const uint32_t ctrl[4] = {(uint32_t)n32, (uint32_t)n64, 0u, 0u};
+    if (n32) CK(cudaMemcpyAsync(b->tasks32.p, b->t32.data(), n32 * sizeof(Task), cudaMemcpyHostToDevice, c->st));
+    if (n64) CK(cudaMemcpyAsync(b->tasks64.p, b->t64.data(), n64 * sizeof(Task), cudaMemcpyHostToDevice, c->st));
+    CK(cudaMemcpyAsync(b->ctrl.p, ctrl, sizeof(ctrl), cudaMemcpyHostToDevice, c->st));
+    c->h2d += (n32 + n64) * sizeof(Task) + sizeof(ctrl);
+    CK(cudaEventRecord(b->ev_start, c->st));
+    CK(cudaStreamWaitEvent(b->st32, b->ev_start, 0));
+    CK(cudaStreamWaitEvent(b->st64, b->ev_start, 0));
+    HitBuf h{};
+    h.buf = b->hits.p;
+    h.count = b->hitcount.p;
+    h.cap = b->hits.n;
+    h.tag = b->tags.p;
+    if (n32) {
+        const int grid = (int)std::min<size_t>(b->grid32, n32);
+        batch_kernel<Cls32><<<grid, 256, 0, b->st32>>>(b->tasks32.p, b->ctrl.p + 0, b->ctrl.p + 2, b->jobs32.p, h);
+        c->launches++;
+    }
+    if (n64) {
+        const int grid = (int)std::min<size_t>(b->grid64, n64);
+        batch_kernel<Cls64><<<grid, 256, 0, b->st64>>>(b->tasks64.p, b->ctrl.p + 1, b->ctrl.p + 3, b->jobs64.p, h);
+        c->launches++;
+    }
+    CK(cudaGetLastError());
+    // the main stream waits for both classes before the hit read-back
+    CK(cudaEventRecord(b->ev_end32, b->st32));
+    CK(cudaStreamWaitEvent(c->st, b->ev_end32, 0));
+    CK(cudaEventRecord(b->ev_end64, b->st64));
+    CK(cudaStreamWaitEvent(c->st, b->ev_end64, 0));
+    b->tasks += n32 + n64;
+    b->t32_n = n32;
+    b->t64_n = n64;
+    CK(cudaMemcpyAsync(b->h_hitcount, b->hitcount.p, sizeof(unsigned long long), cudaMemcpyDeviceToHost, c->st));
+    return PFC_OK;
+}
+
+// After the iteration: route the hits by slot (on overflow, every search of
+// the iteration is redone alone at the end) and advance the blocks.
+int finish_iteration(pfc_batch *b, uint32_t L) {
+    pfc_ctx *c = b->ctx;
+    CK(cudaStreamSynchronize(c->st));
+    ++b->iterations;
+    float ms32 = 0, ms64 = 0;
+    CK(cudaEventElapsedTime(&ms32, b->ev_start, b->ev_end32));
+    CK(cudaEventElapsedTime(&ms64, b->ev_start, b->ev_end64));
+    b->gpu32_s += (b->t32_n ? ms32 : 0) * 1e-3;
+    b->gpu64_s += (b->t64_n ? ms64 : 0) * 1e-3;
+    b->gpu_s += std::max(b->t32_n ? ms32 : 0.f, b->t64_n ? ms64 : 0.f) * 1e-3;
+    const unsigned long long nh = *b->h_hitcount;
+    if (nh > b->hits.n) {
+        for (BatchJob *j : b->running) j->rerun = true;
+    } else if (nh) {
+        std::vector<pfc_factor> hv(nh);
+        std::vector<uint32_t> tv(nh);
+        CK(cudaMemcpyAsync(hv.data(), b->hits.p, nh * sizeof(pfc_factor), cudaMemcpyDeviceToHost, c->st));
+        CK(cudaMemcpyAsync(tv.data(), b->tags.p, nh * sizeof(uint32_t), cudaMemcpyDeviceToHost, c->st));
+        CK(cudaStreamSynchronize(c->st));
+        c->d2h += nh * (sizeof(pfc_factor) + sizeof(uint32_t));
+        std::vector<BatchJob *> by_slot(pfc_batch::kSlots, nullptr);
+        for (BatchJob *j : b->running) by_slot[j->slot] = j;
+        for (unsigned long long i = 0; i < nh; ++i)
+            if (tv[i] < pfc_batch::kSlots && by_slot[tv[i]]) by_slot[tv[i]]->hits.push_back(hv[i]);
+    }
+    if (nh) CK(cudaMemsetAsync(b->hitcount.p, 0, sizeof(unsigned long long), c->st));
+    for (BatchJob *j : b->running) {
+        for (Block &k : j->b32) k.pos = (uint32_t)std::min<uint64_t>((uint64_t)k.pos + L, j->tot32);
+        for (Block &k : j->b64) k.pos = (uint32_t)std::min<uint64_t>((uint64_t)k.pos + L, j->tot64);
+    }
+    return PFC_OK;
+}
+
+// a search whose hits overflowed the batch's hit buffer is redone on the
+// per-job path
+int rerun_alone(pfc_batch *b, BatchJob *j) {
+    pfc_job *pj = nullptr;
+    int rc = pfc_job_create(b->ctx, j->mode, j->nmin, j->nmax, j->pmin, j->pmax, &pj);
+    if (rc) return rc;
+    std::vector<pfc_factor> buf(1 << 16);
+    size_t n = 0;
+    for (;;) {
+        rc = pfc_job_run(pj, buf.data(), buf.size(), &n);
+        if (rc != PFC_ERR_HIT_OVERFLOW) break;
+        pfc_job_destroy(pj);
+        buf.resize(n + 1024);
+        rc = pfc_job_create(b->ctx, j->mode, j->nmin, j->nmax, j->pmin, j->pmax, &pj);
+        if (rc) return rc;
+    }
+    if (rc == PFC_OK) {
+        buf.resize(n);
+        j->hits = buf;
+        uint64_t term = 0, count = 0;
+        pfc_job_totals(pj, &term, &count);
+        j->termsum = term;
+        j->primecount = count;
+        j->flags = 0;
+    }
+    pfc_job_destroy(pj);
+    return rc;
+}
+
+int retire_finished(pfc_batch *b) {
+    pfc_ctx *c = b->ctx;
+    std::vector<BatchJob *> done, still;
+    for (BatchJob *j : b->running) {
+        bool fin = true;
+        for (const Block &k : j->b32) fin &= k.pos >= j->tot32;
+        for (const Block &k : j->b64) fin &= k.pos >= j->tot64;
+        (fin ? done : still).push_back(j);
+    }
+    if (done.empty()) return PFC_OK;
+    CK(cudaMemcpyAsync(b->h_stats, b->stats.p, sizeof(BatchStats) * pfc_batch::kSlots, cudaMemcpyDeviceToHost, c->st));
+    CK(cudaStreamSynchronize(c->st));
+    for (BatchJob *j : done) {
+        const BatchStats &s = b->h_stats[j->slot];
+        j->termsum = s.termsum;
+        j->flags = s.flags;
+        release_device(b, j);
+        b->free_slots.push_back(j->slot);
+        j->b32.clear();
+        j->b64.clear();
+        j->state = kDone;
+        if (j->rerun) {
+            j->hits.clear();
+            j->status = rerun_alone(b, j);
+        } else if (j->flags & 1u) {
+            j->status = PFC_ERR_VALIDATION;
+        }
+    }
+    b->running.swap(still);
+    return PFC_OK;
+}
+
+}  // namespace
+
+// ====================================================================== C ABI
+
+extern "C" int pfc_batch_destroy(pfc_batch *b);
+
+extern "C" int pfc_batch_create(pfc_ctx *c, pfc_batch **out) {
+    if (!c || !out) return PFC_ERR_ARG;
+    *out = nullptr;
+    CK(cudaSetDevice(c->device));
+    pfc_batch *b = new (std::nothrow) pfc_batch();
+    if (!b) return PFC_ERR_NOMEM;
+    b->ctx = c;
+    cudaError_t e = cudaStreamCreateWithFlags(&b->st32, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b->st64, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->ev, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreate(&b->ev_start);
+    if (e == cudaSuccess) e = cudaEventCreate(&b->ev_end32);
+    if (e == cudaSuccess) e = cudaEventCreate(&b->ev_end64);
+    if (e == cudaSuccess) e = b->stats.alloc(c, pfc_batch::kSlots);
+    if (e == cudaSuccess) e = b->jobs32.alloc(c, pfc_batch::kSlots);
+    if (e == cudaSuccess) e = b->jobs64.alloc(c, pfc_batch::kSlots);
+    if (e == cudaSuccess) e = b->ctrl.alloc(c, 4);
+    if (e == cudaSuccess) e = b->hits.alloc(c, 1u << 20);
+    if (e == cudaSuccess) e = b->tags.alloc(c, 1u << 20);
+    if (e == cudaSuccess) e = b->hitcount.alloc(c, 1);
+    if (e == cudaSuccess) e = cudaMallocHost((void **)&b->h_stats, sizeof(BatchStats) * pfc_batch::kSlots);
+    if (e == cudaSuccess) e = cudaMallocHost((void **)&b->h_hitcount, sizeof(unsigned long long));
+    if (e == cudaSuccess) e = cudaMemsetAsync(b->hitcount.p, 0, sizeof(unsigned long long), c->st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(b->stats.p, 0, sizeof(BatchStats) * pfc_batch::kSlots, c->st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->st);
+    int n32 = 0, n64 = 0;
+    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n32, batch_kernel<Cls32>, 256, 0);
+    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n64, batch_kernel<Cls64>, 256, 0);
+    if (e != cudaSuccess) {
+        pfc_batch_destroy(b);
+        return cuda_fail(e);
+    }
+    b->grid32 = std::max(1, n32) * c->sms;
+    b->grid64 = std::max(1, n64) * c->sms;
+    for (uint32_t s = pfc_batch::kSlots; s-- > 0;) b->free_slots.push_back(s);
+    *out = b;
+    return PFC_OK;
+}
+
+extern "C" int pfc_batch_destroy(pfc_batch *b) {
+    if (!b) return PFC_ERR_ARG;
+    pfc_ctx *c = b->ctx;
+    cudaSetDevice(c->device);
+    if (b->st32) cudaStreamSynchronize(b->st32);
+    if (b->st64) cudaStreamSynchronize(b->st64);
+    cudaStreamSynchronize(c->st);
+    for (auto &kv : b->all) release_device(b, kv.second.get());
+    b->stats.release(c);
+    b->jobs32.release(c);
+    b->jobs64.release(c);
+    b->tasks32.release(c);
+    b->tasks64.release(c);
+    b->ctrl.release(c);
+    b->hits.release(c);
+    b->tags.release(c);
+    b->hitcount.release(c);
+    if (b->h_stats) cudaFreeHost(b->h_stats);
+    if (b->h_hitcount) cudaFreeHost(b->h_hitcount);
+    if (b->ev) cudaEventDestroy(b->ev);
+    if (b->ev_start) cudaEventDestroy(b->ev_start);
+    if (b->ev_end32) cudaEventDestroy(b->ev_end32);
+    if (b->ev_end64) cudaEventDestroy(b->ev_end64);
+    if (b->st32) cudaStreamDestroy(b->st32);
+    if (b->st64) cudaStreamDestroy(b->st64);
+    delete b;
+    return PFC_OK;
+}
+
+extern "C" int pfc_batch_submit(pfc_batch *b, const pfc_job_desc *d, uint64_t *id) {
+    if (!b || !d || !id) return PFC_ERR_ARG;
+    const unsigned mode = d->mode;
+    const bool valid_mode = mode == PFC_FACTORIAL || mode == PFC_PRIMORIAL || mode == PFC_COMPOSITORIAL ||
+                            mode == (PFC_FACTORIAL | PFC_COMPOSITORIAL);
+    // the ranges of pfc_job_create, and at most 2^26 n per search (the
+    // per-search multiplier table lives on the device for the whole search)
+    if (!valid_mode || d->pmin < 3 || d->pmax <= d->pmin || d->nmin < 101 || d->nmax < d->nmin ||
+        d->nmax > 0x7FFFFFFFu || d->nmax - d->nmin > (1u << 26))
+        return PFC_ERR_ARG;
+    auto j = std::make_unique<BatchJob>();
+    j->id = b->next_id++;
+    j->mode = mode;
+    j->nmin = d->nmin;
+    j->nmax = d->nmax;
+    j->pmin = d->pmin;
+    j->pmax = d->pmax;
+    b->queued.push_back(j.get());
+    *id = j->id;
+    b->all[j->id] = std::move(j);
+    return PFC_OK;
+}
+
+// One iteration, pipelined with the host work of admission:
+//   1. searches made ready by the previous call join; every running block
+//      gets a task; both class kernels are launched (asynchronously);
+//   2. while they run, the host tables of queued searches are built;
+//   3. the iteration is finished (hits routed, blocks advanced) and finished
+//      searches are retired, freeing slots and memory;
+//   4. prepared searches are uploaded and their candidates generated while
+//      the budget allows; they join at the next call.
+// When nothing was running, the call admits and then runs at once.
+extern "C" int pfc_batch_step(pfc_batch *b, uint32_t *active, uint32_t *queued) {
+    if (!b) return PFC_ERR_ARG;
+    CK(cudaSetDevice(b->ctx->device));
+    const double ts = now_s();
+    for (int pass = 0; pass < 2; ++pass) {
+        const uint32_t L = build_tasks(b);
+        const bool work = !b->t32.empty() || !b->t64.empty();
+        if (work) {
+            const int rc = launch_iteration(b);
+            if (rc) return rc;
+        }
+        const double tp = now_s();
+        prepare_queued(b);
+        b->prep_s += now_s() - tp;
+        if (work) {
+            int rc = finish_iteration(b, L);
+            if (rc) return rc;
+            rc = retire_finished(b);
+            if (rc) return rc;
+        }
+        const double ta = now_s();
+        const int rc = admit_prepared(b);
+        b->admit_s += now_s() - ta;
+        if (rc) return rc;
+        if (work || b->ready.empty()) break;
+    }
+    b->step_s += now_s() - ts;
+    if (active) *active = (uint32_t)(b->running.size() + b->ready.size());
+    if (queued) *queued = (uint32_t)b->queued.size();
+    return PFC_OK;
+}
+
+extern "C" int pfc_batch_result(pfc_batch *b, uint64_t id, pfc_batch_status *r) {
+    if (!b || !r) return PFC_ERR_ARG;
+    auto it = b->all.find(id);
+    if (it == b->all.end()) return PFC_ERR_ARG;
+    const BatchJob &j = *it->second;
+    memset(r, 0, sizeof(*r));
+    r->done = j.state == kDone;
+    r->status = j.status;
+    if (r->done) {
+        r->term_checksum = j.termsum;
+        r->primecount = j.primecount;
+        r->pairs = j.primecount * (uint64_t)(j.nmax - j.nmin);
+        r->hits = j.hits.size();
+    }
+    return PFC_OK;
+}
+
+extern "C" int pfc_batch_take_hits(pfc_batch *b, uint64_t id, pfc_factor *buf, size_t cap, size_t *n) {
+    if (!b || !n || (!buf && cap)) return PFC_ERR_ARG;
+    auto it = b->all.find(id);
+    if (it == b->all.end() || it->second->state != kDone) return PFC_ERR_STATE;
+    const std::vector<pfc_factor> &h = it->second->hits;
+    *n = h.size();
+    if (h.size() > cap) return PFC_ERR_HIT_OVERFLOW;
+    if (!h.empty()) memcpy(buf, h.data(), h.size() * sizeof(pfc_factor));
+    return PFC_OK;
+}
+
+extern "C" int pfc_batch_release(pfc_batch *b, uint64_t id) {
+    if (!b) return PFC_ERR_ARG;
+    auto it = b->all.find(id);
+    if (it == b->all.end() || it->second->state != kDone) return PFC_ERR_STATE;
+    b->all.erase(it);
+    return PFC_OK;
+}
+
+extern "C" uint64_t pfc_batch_iterations(pfc_batch *b) { return b ? b->iterations : 0; }
+
+extern "C" int pfc_batch_timing(pfc_batch *b, pfc_batch_times *t) {
+    if (!b || !t) return PFC_ERR_ARG;
+    t->step_s = b->step_s;
+    t->gpu_s = b->gpu_s;
+    t->gpu32_s = b->gpu32_s;
+    t->gpu64_s = b->gpu64_s;
+    t->prep_s = b->prep_s;
+    t->admit_s = b->admit_s;
+    t->iterations = b->iterations;
+    t->tasks = b->tasks;
+    return PFC_OK;
+}
+
+extern "C" int pfc_batch_set_iteration_work(pfc_batch *b, double candidate_steps) {
+    if (!b || !(candidate_steps >= 1.0)) return PFC_ERR_ARG;
+    b->work_per_iter = candidate_steps;
+    return PFC_OK;
+}

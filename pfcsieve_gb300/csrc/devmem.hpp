@@ -1,0 +1,144 @@
+// devmem.hpp -- the context record and budgeted device buffers shared by
+// the C ABI implementations (api.cu, batch.cu).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdint>
+#include <vector>
+
+#include "host.hpp"
+#include "kernels.cuh"
+#include "pfcsieve.h"
+
+struct pfc_ctx {
+    int device = 0;
+    cudaStream_t st = nullptr;
+    int sms = 0;
+    char name[256] = {0};
+    uint64_t budget = 0, used = 0;
+    uint64_t launches = 0;
+    uint64_t h2d = 0, d2h = 0;   // bytes copied by this context
+    uint64_t *d_pat = nullptr;
+};
+
+namespace pfc {
+
+inline cudaError_t dalloc_bytes(pfc_ctx *c, void **p, size_t bytes) {
+    *p = nullptr;
+    if (bytes == 0) return cudaSuccess;
+    if (c->used + bytes > c->budget) return cudaErrorMemoryAllocation;
+    cudaError_t e = cudaMalloc(p, bytes);
+    if (e == cudaSuccess) c->used += bytes;
+    return e;
+}
+
+template <class T>
+struct DArr {
+    T *p = nullptr;
+    size_t n = 0;
+    cudaError_t alloc(pfc_ctx *c, size_t count) {
+        release(c);
+        cudaError_t e = dalloc_bytes(c, (void **)&p, count * sizeof(T));
+        if (e == cudaSuccess) n = count;
+        return e;
+    }
+    cudaError_t upload(pfc_ctx *c, const std::vector<T> &v) {
+        cudaError_t e = alloc(c, std::max<size_t>(v.size(), 1));
+        if (e != cudaSuccess) return e;
+        if (v.empty()) return cudaMemsetAsync(p, 0, sizeof(T), c->st);
+        c->h2d += v.size() * sizeof(T);
+        return cudaMemcpyAsync(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, c->st);
+    }
+    void release(pfc_ctx *c) {
+        if (p) {
+            cudaFree(p);
+            c->used -= n * sizeof(T);
+        }
+        p = nullptr;
+        n = 0;
+    }
+};
+
+template <class W>
+struct DevProg {
+    DArr<W> words;
+    DArr<uint32_t> groups;
+    Prog<W> view{};
+    cudaError_t upload(pfc_ctx *c, const HostProg<W> &h) {
+        cudaError_t e = words.upload(c, h.words);
+        if (e == cudaSuccess) e = groups.upload(c, h.groups);
+        view.words = words.p;
+        view.groups = groups.p;
+        view.ngroups = (uint32_t)(h.groups.size() / 3);
+        view.final_sq = h.final_sq;
+        view.corr = h.corr;
+        return e;
+    }
+    void release(pfc_ctx *c) {
+        words.release(c);
+        groups.release(c);
+    }
+};
+
+template <class W>
+struct DevClass {
+    DArr<W> p, s0, s1;
+    DArr<uint32_t> nnext;
+    uint32_t cap = 0;
+    cudaError_t ensure(pfc_ctx *c, uint32_t want) {
+        if (want <= cap && p.p) return cudaSuccess;
+        release(c);
+        const size_t n = std::max<uint32_t>(want, 256);
+        cudaError_t e = p.alloc(c, n);
+        if (e == cudaSuccess) e = s0.alloc(c, n);
+        if (e == cudaSuccess) e = s1.alloc(c, n);
+        if (e == cudaSuccess) e = nnext.alloc(c, n);
+        if (e == cudaSuccess) cap = (uint32_t)n;
+        return e;
+    }
+    void release(pfc_ctx *c) {
+        p.release(c);
+        s0.release(c);
+        s1.release(c);
+        nnext.release(c);
+        cap = 0;
+    }
+    ClassBuf<W> view(const uint32_t *count) const {
+        ClassBuf<W> b;
+        b.p = p.p;
+        b.s0 = s0.p;
+        b.s1 = s1.p;
+        b.nnext = nnext.p;
+        b.cap = cap;
+        b.count = count;
+        return b;
+    }
+};
+
+// small per-segment read-back block (pinned host mirror)
+struct SegStats {
+    uint32_t counts[2];
+    uint32_t flags;
+    uint32_t pad;
+    unsigned long long termsum;
+    unsigned long long hits;
+};
+
+}  // namespace pfc
+
+
+namespace pfc {
+
+inline int cuda_fail(cudaError_t e) {
+    if (e == cudaErrorMemoryAllocation) return PFC_ERR_NOMEM;
+    return e == cudaSuccess ? PFC_OK : PFC_ERR_CUDA;
+}
+#define CK(x)                                    \
+    do {                                         \
+        cudaError_t e_ = (x);                    \
+        if (e_ != cudaSuccess) return cuda_fail(e_); \
+    } while (0)
+
+
+}  // namespace pfc

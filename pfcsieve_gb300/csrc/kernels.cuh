@@ -31,6 +31,8 @@ struct HitBuf {
     pfc_factor *buf;
     unsigned long long *count;   // total hits (may exceed cap)
     uint64_t cap;
+    uint32_t *tag;               // batches: job slot of each hit (else null)
+    uint32_t tagval;
 };
 
 // Setup program for one quantity: a product of table words with squarings in

@@ -251,7 +251,7 @@ extern "C" int pfc_segment_noalloc(unsigned mode, uint32_t nmin, uint32_t nmax, 
     if (use64) launch_setup64(c64, s64, st);
 
     // walks over [nmin, nmax) (prime indices for n#), in chunks of kChunk
-    HitBuf h;
+    HitBuf h{};
     h.buf = d_hits;
     h.count = &stats->hits;
     h.cap = hit_cap;

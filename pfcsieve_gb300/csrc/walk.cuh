@@ -1,0 +1,292 @@
+// walk.cuh -- the walk machinery shared by the per-job kernels (sieve.cu)
+// and the batch kernel (batch.cu): size-class traits, hit appends,
+// multiplier loads, the per-block walk and its replay.
+//
+// Drift walk.  The reference keeps r and n both in Montgomery form and spends
+// an add-mod per n to advance Mont(n) (iterate.cl:73-74).  Here the
+// multiplier is the plain integer n (or the prime q for n#), and each step is
+// one reduction s <- s*n*R^-1.  Starting a block of B steps from s = r*R, after
+// j+1 steps s = r_{j+1} * R^-j, so r_{j+1} = +-1 exactly when s equals
+// T[j] = R^-j mod p or p - T[j].  The B targets are per-thread registers
+// computed once per launch; one multiplication by K = R^(B+1) returns s to
+// Montgomery form at the end of the block.  Hits are rare, so a block only
+// ORs its comparisons into one predicate; if any lane of the warp saw a hit
+// the warp replays that block from its saved start with per-step recording.
+//
+// Each launch walks one residue chain.  The combined search (-! -c) walks the
+// factorial chain over n and then the compositorial chain over a multiplier
+// table holding n at composite n and 1 at prime n (the reference skips prime
+// n, iterate.cl:137-140, 181-184): multiplying by 1 keeps the drift at one
+// power of R per step, and the replay skips the test where the multiplier is
+// 1.  The fast path tests every step: at a prime n the compositorial value is
+// the previous step's, so an unmasked match there only repeats a hit already
+// seen and costs one replay, never a wrong record.  The per-step work is three
+// integer multiplies (IMAD.WIDE, IMAD, IMAD.HI), one compare and conditional
+// add for the reduction, and two compares for the hit test.
+#pragma once
+#include "arith.cuh"
+#include "kernels.cuh"
+
+namespace pfc {
+
+constexpr unsigned kFull = 0xffffffffu;
+
+struct Cls32 {
+    using W = uint32_t;
+    using M = Mont32;
+    static constexpr int B = 8;           // block length with two candidates per thread
+    static constexpr int B_FUSED = 16;    // block length of the fused -! -c walk
+    static constexpr int NC = 2;          // candidates per thread in single-chain walks
+    static constexpr bool kSigned = true; // walk residues signed in (-p, p), p < 2^31
+    // fast walk step and its hit test: x = +-T (mod p) <=> |x| in {T, p - T}
+    __device__ static __forceinline__ W fstep(const M &m, W x, uint32_t n) {
+        return (W)redc31s((int32_t)x, n, (int32_t)m.p, m.pinv);
+    }
+    __device__ static __forceinline__ bool fhit(W x, W t, W nt) {
+        const uint32_t ax = (uint32_t)abs((int32_t)x);
+        return (ax == t) | (ax == nt);
+    }
+    __device__ static __forceinline__ W canon(const M &m, W x) { return (int32_t)x < 0 ? x + m.p : x; }
+    // x*K*R^-1 for the block restore (K < p < 2^31)
+    __device__ static __forceinline__ W restore(const M &m, W x, W K) { return fstep(m, x, K); }
+    __device__ static __forceinline__ W step(const M &m, W s, uint32_t n) { return redc32(s, n, m.p, m.pinv); }
+    __device__ static __forceinline__ W word(const M &m, W s, W w) { return redc32(s, w, m.p, m.pinv); }
+    // checksum form: residue * 2^64 mod p from its class-32 Montgomery form
+    __device__ static __forceinline__ uint64_t term(const M &m, W s) { return m.mul(s, m.r2); }
+    __device__ static __forceinline__ uint64_t mont64_of(const M &m, uint32_t v) { return m.mul(m.mul(v, m.r2), m.r2); }
+};
+
+struct Cls64 {
+    using W = uint64_t;
+    using M = Mont64;
+    static constexpr int B = 8;
+    static constexpr int B_FUSED = 8;
+    static constexpr int NC = 1;
+    static constexpr bool kSigned = false;
+    __device__ static __forceinline__ W fstep(const M &m, W x, uint32_t n) { return redc64_u32(x, n, m.p, m.pinv); }
+    __device__ static __forceinline__ bool fhit(W x, W t, W nt) { return (x == t) | (x == nt); }
+    __device__ static __forceinline__ W canon(const M &, W x) { return x; }
+    __device__ static __forceinline__ W restore(const M &m, W x, W K) { return m.mul(x, K); }
+    __device__ static __forceinline__ W step(const M &m, W s, uint32_t n) { return redc64_u32(s, n, m.p, m.pinv); }
+    __device__ static __forceinline__ W word(const M &m, W s, W w) { return redc64(s, w, m.p, m.pinv); }
+    __device__ static __forceinline__ uint64_t term(const M &, W s) { return s; }
+    __device__ static __forceinline__ uint64_t mont64_of(const M &m, uint32_t v) { return m.to_mont(v); }
+};
+
+template <class W>
+__device__ __forceinline__ W ldg(const W *p) { return __ldg(p); }
+
+// Evaluate a setup program from Montgomery-form `acc` (see kernels.cuh Prog).
+template <class T>
+__device__ typename T::W run_prog(const typename T::M &m, const Prog<typename T::W> &pg, typename T::W acc) {
+    for (uint32_t g = 0; g < pg.ngroups; ++g) {
+        const uint32_t b = __ldg(pg.groups + 3 * g), e = __ldg(pg.groups + 3 * g + 1);
+        const uint32_t sq = __ldg(pg.groups + 3 * g + 2);
+        for (uint32_t k = 0; k < sq; ++k) acc = m.mul(acc, acc);
+        uint32_t i = b;
+        for (; i + 4 <= e; i += 4) {
+            acc = T::word(m, acc, ldg(pg.words + i));
+            acc = T::word(m, acc, ldg(pg.words + i + 1));
+            acc = T::word(m, acc, ldg(pg.words + i + 2));
+            acc = T::word(m, acc, ldg(pg.words + i + 3));
+        }
+        for (; i < e; ++i) acc = T::word(m, acc, ldg(pg.words + i));
+    }
+    for (uint32_t k = 0; k < pg.final_sq; ++k) acc = m.mul(acc, acc);
+    return m.mul(acc, m.mont_R_pow(pg.corr));
+}
+
+// warp-aggregated bounded append of one hit per lane (all 32 lanes call it);
+// batches also record the job of each hit in h.tag
+__device__ __forceinline__ void append_hit(bool hit, uint64_t p, int32_t nc, int32_t type, const HitBuf &h) {
+    const unsigned msk = __ballot_sync(kFull, hit);
+    if (!msk) return;
+    const unsigned lane = threadIdx.x & 31;
+    const int leader = __ffs(msk) - 1;
+    unsigned long long base = 0;
+    if ((int)lane == leader) base = atomicAdd(h.count, (unsigned long long)__popc(msk));
+    base = __shfl_sync(kFull, base, leader);
+    if (hit) {
+        const unsigned long long idx = base + __popc(msk & ((1u << lane) - 1u));
+        if (idx < h.cap) {
+            pfc_factor f;
+            f.p = p;
+            f.nc = nc;
+            f.type = type;
+            h.buf[idx] = f;
+            if (h.tag) h.tag[idx] = h.tagval;
+        }
+    }
+}
+
+// Multipliers of steps k .. k+B-1 (uniform across the warp): k itself when
+// `mult` is null, else mult[k - base ...] (vector loads when aligned).
+template <int B>
+__device__ __forceinline__ void load_mult(const uint32_t *mult, uint32_t base, uint32_t k, bool vec, uint32_t (&mv)[B]) {
+    if (!mult) {
+#pragma unroll
+        for (int j = 0; j < B; ++j) mv[j] = k + j;
+    } else if (vec) {
+        const uint4 *src = reinterpret_cast<const uint4 *>(mult + (k - base));
+#pragma unroll
+        for (int j = 0; j < B / 4; ++j) {
+            const uint4 v = __ldg(src + j);
+            mv[4 * j] = v.x;
+            mv[4 * j + 1] = v.y;
+            mv[4 * j + 2] = v.z;
+            mv[4 * j + 3] = v.w;
+        }
+    } else {
+#pragma unroll
+        for (int j = 0; j < B; ++j) mv[j] = __ldg(mult + (k - base) + j);
+    }
+}
+
+// Replay `len` steps of one chain from the block start x with the exact
+// per-step test and record the hits.  A multiplier of 1 marks a prime n of
+// the compositorial walk: nothing was multiplied there, so nothing is tested.
+template <class T>
+__device__ __noinline__ void replay_chain(const typename T::M m, typename T::W x, const uint32_t *mult,
+                                          uint32_t base, uint32_t k, int len, int32_t type, bool active,
+                                          const HitBuf h) {
+    using W = typename T::W;
+    x = T::canon(m, x);
+    W t = 1;
+    for (int j = 0; j < len; ++j) {
+        if (j) t = m.mul(t, 1);
+        const uint32_t mul = mult ? __ldg(mult + (k - base) + j) : k + j;
+        x = T::step(m, x, mul);
+        const bool hit = active && mul != 1u && (x == t || x == m.p - t);
+        append_hit(hit, m.p, x == t ? -(int32_t)mul : (int32_t)mul, type, h);
+    }
+}
+
+// Walk steps [a.lo, a.hi) of the streams of one thread.  Each thread runs
+// two independent streams of steps so that the scheduler always has a second
+// dependent chain to interleave:
+//   FUSED (-! -c): the factorial chain (multiplier n) and the compositorial
+//     chain (multiplier table a.mult2) of one candidate, sharing its targets;
+//   otherwise NC candidates (1 or 2) on the same multiplier sequence.
+// x holds canonical Montgomery-form residues on entry and on exit.  Inactive
+// streams hold 0, which never matches a target (targets are in [1, p-1]), so
+// they never trigger a replay.
+template <class T, int NC, bool FUSED>
+__device__ __forceinline__ void walk_streams(const typename T::M (&m)[NC], typename T::W (&x)[FUSED ? 2 : NC],
+                                             const bool (&act)[NC], const WalkArgs &a, const HitBuf &h) {
+    using W = typename T::W;
+    constexpr int B = FUSED ? T::B_FUSED : T::B;
+    constexpr int NS = FUSED ? 2 : NC;
+    W tg[NC][B], ntg[NC][B], K[NC];
+#pragma unroll
+    for (int s = 0; s < NC; ++s) {
+        tg[s][0] = 1;
+#pragma unroll
+        for (int j = 1; j < B; ++j) tg[s][j] = m[s].mul(tg[s][j - 1], 1);
+#pragma unroll
+        for (int j = 0; j < B; ++j) ntg[s][j] = m[s].p - tg[s][j];
+        K[s] = m[s].mont_R_pow(B);
+    }
+
+    const uint32_t *mult0 = FUSED ? nullptr : a.mult;
+    const uint32_t *mult1 = a.mult2;
+    const bool vec = ((a.lo - a.base) & 3u) == 0;
+    uint32_t k = a.lo;
+    const uint32_t nblk = (a.hi - a.lo) / B;
+    for (uint32_t b = 0; b < nblk; ++b, k += B) {
+        uint32_t mv[B], cv[B];
+        load_mult<B>(mult0, a.base, k, vec, mv);
+        if (FUSED) load_mult<B>(mult1, a.base, k, vec, cv);
+        W xs[NS];
+#pragma unroll
+        for (int s = 0; s < NS; ++s) xs[s] = x[s];
+        bool any = false;
+#pragma unroll
+        for (int j = 0; j < B; ++j) {
+            if (FUSED) {
+                x[0] = T::fstep(m[0], x[0], mv[j]);
+                x[NS - 1] = T::fstep(m[0], x[NS - 1], cv[j]);
+                any |= T::fhit(x[0], tg[0][j], ntg[0][j]) | T::fhit(x[NS - 1], tg[0][j], ntg[0][j]);
+            } else {
+#pragma unroll
+                for (int s = 0; s < NC; ++s) {
+                    x[s] = T::fstep(m[s], x[s], mv[j]);
+                    any |= T::fhit(x[s], tg[s][j], ntg[s][j]);
+                }
+            }
+        }
+        if (__any_sync(kFull, any)) {
+            if (FUSED) {
+                replay_chain<T>(m[0], xs[0], nullptr, a.base, k, B, a.type, act[0], h);
+                replay_chain<T>(m[0], xs[NS - 1], mult1, a.base, k, B, a.type2, act[0], h);
+            } else {
+#pragma unroll
+                for (int s = 0; s < NC; ++s) replay_chain<T>(m[s], xs[s], mult0, a.base, k, B, a.type, act[s], h);
+            }
+        }
+        // back to Montgomery form (class 32: |x*K| < p^2 < p*2^31)
+        if (FUSED) {
+            x[0] = T::restore(m[0], x[0], K[0]);
+            x[NS - 1] = T::restore(m[0], x[NS - 1], K[0]);
+        } else {
+#pragma unroll
+            for (int s = 0; s < NC; ++s) x[s] = T::restore(m[s], x[s], K[s]);
+        }
+    }
+
+    // canonical form for the tail, the state store and the check kernel
+    if (FUSED) {
+        x[0] = T::canon(m[0], x[0]);
+        x[NS - 1] = T::canon(m[0], x[NS - 1]);
+    } else {
+#pragma unroll
+        for (int s = 0; s < NC; ++s) x[s] = T::canon(m[s], x[s]);
+    }
+    const int r = (int)(a.hi - k);
+    if (r > 0) {  // tail of fewer than B steps
+        W xs[NS];
+#pragma unroll
+        for (int s = 0; s < NS; ++s) xs[s] = x[s];
+        bool any = false;
+#pragma unroll
+        for (int j = 0; j < B; ++j) {
+            if (j < r) {
+                const uint32_t mul0 = mult0 ? __ldg(mult0 + (k - a.base) + j) : k + j;
+                if (FUSED) {
+                    const uint32_t mul1 = __ldg(mult1 + (k - a.base) + j);
+                    x[0] = T::step(m[0], x[0], mul0);
+                    x[NS - 1] = T::step(m[0], x[NS - 1], mul1);
+                    any |= (x[0] == tg[0][j]) | (x[0] == ntg[0][j]) | (x[NS - 1] == tg[0][j]) |
+                           (x[NS - 1] == ntg[0][j]);
+                } else {
+#pragma unroll
+                    for (int s = 0; s < NC; ++s) {
+                        x[s] = T::step(m[s], x[s], mul0);
+                        any |= (x[s] == tg[s][j]) | (x[s] == ntg[s][j]);
+                    }
+                }
+            }
+        }
+        if (__any_sync(kFull, any)) {
+            if (FUSED) {
+                replay_chain<T>(m[0], xs[0], nullptr, a.base, k, r, a.type, act[0], h);
+                replay_chain<T>(m[0], xs[NS - 1], mult1, a.base, k, r, a.type2, act[0], h);
+            } else {
+#pragma unroll
+                for (int s = 0; s < NC; ++s) replay_chain<T>(m[s], xs[s], mult0, a.base, k, r, a.type, act[s], h);
+            }
+        }
+#pragma unroll
+        for (int s = 0; s < NC; ++s) {
+            const W Kr = m[s].mont_R_pow((uint64_t)r);
+            if (FUSED) {
+                x[0] = m[0].mul(x[0], Kr);
+                x[NS - 1] = m[0].mul(x[NS - 1], Kr);
+            } else {
+                x[s] = m[s].mul(x[s], Kr);
+            }
+        }
+    }
+
+}
+
+}  // namespace pfc

@@ -1,0 +1,118 @@
+"""The batch engine (pfc_batch_*) against the per-job path and the oracle.
+
+Every search run inside a batch must give exactly what it gives alone
+(pfc_job_run): the same wrapping checksum-term sum, candidate count and raw hit
+multiset, whatever else shares the GPU with it and whenever it joined.  Small
+cases are also checked against the oracle directly.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from oracle import oracle as o
+
+pfc = pytest.importorskip("pfcsieve_gb300")
+
+pytestmark = pytest.mark.gpu
+
+THREADS = min(os.cpu_count() or 1, 64)
+
+# every mode, both size classes, p <= n (Wilson hits), tiny n ranges, a primorial
+# range with no prime n, and nmin == nmax
+MIX = [
+    (5, 101, 20000, 10**9, 10**9 + 2 * 10**6),
+    (1, 101, 5000, 3, 50000),
+    (2, 2000, 60000, 2**40, 2**40 + 3 * 10**6),
+    (4, 150, 30000, 2**31 - 10**6, 2**31 + 10**6),
+    (2, 101, 40000, 1000, 3 * 10**6),
+    (1, 30000, 31000, 2**33, 2**33 + 5 * 10**6),
+    (5, 5000, 9000, 10**5, 4 * 10**6),
+    (4, 101, 102, 10**6, 2 * 10**6),
+    (2, 114, 126, 10**7, 10**7 + 10**6),
+    (1, 500, 500, 10**6, 10**6 + 10**5),
+]
+
+
+def alone(ctx, case):
+    with pfc.Job(ctx, *case) as job:
+        hits = job.run()
+        termsum, count = job.totals()
+    return termsum, count, o.sort_factors(hits)
+
+
+def batched(b, jid):
+    st = b.status(jid)
+    assert st.done == 1 and st.status == 0, (jid, st.status)
+    return st.term_checksum, st.primecount, o.sort_factors(b.hits(jid))
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    with pfc.Context(0) as c:
+        yield c
+
+
+def test_batch_equals_jobs_alone(ctx):
+    with pfc.Batch(ctx) as b:
+        ids = [b.submit(*c) for c in MIX]
+        b.run()
+        for case, jid in zip(MIX, ids):
+            got = batched(b, jid)
+            want = alone(ctx, case)
+            assert got[:2] == want[:2], case
+            assert np.array_equal(got[2], want[2]), case
+
+
+def test_batch_matches_oracle_on_small_cases(ctx):
+    cases = [MIX[1], MIX[4], MIX[6]]
+    with pfc.Batch(ctx) as b:
+        ids = [b.submit(*c) for c in cases]
+        b.run()
+        for case, jid in zip(cases, ids):
+            termsum, count, hits = batched(b, jid)
+            mode, nmin, nmax, pmin, pmax = case
+            cands = o.candidates(pmin, pmax)
+            ohits, oterm, _ = o.sieve(mode, nmin, nmax, cands, threads=THREADS)
+            assert count == len(cands), case
+            assert termsum == oterm, case
+            assert np.array_equal(hits, ohits), case
+
+
+def test_jobs_joining_a_running_batch(ctx):
+    """Continuous batching: searches submitted between iterations start at
+    the next one and still give their stand-alone results."""
+    first, later = MIX[:4], MIX[4:]
+    with pfc.Batch(ctx, iteration_work=2e8) as b:
+        ids = [b.submit(*c) for c in first]
+        b.step()
+        active, queued = b.step()
+        assert active == len(first) and queued == 0   # still running when the others arrive
+        ids += [b.submit(*c) for c in later]
+        active, queued = b.step()
+        assert queued == 0 and active >= 1
+        assert not b.status(ids[0]).done                # overlapped with the newcomers
+        b.run()
+        assert b.iterations >= 4
+        for case, jid in zip(first + later, ids):
+            got = batched(b, jid)
+            want = alone(ctx, case)
+            assert got[:2] == want[:2], case
+            assert np.array_equal(got[2], want[2]), case
+
+
+def test_finished_search_is_released(ctx):
+    with pfc.Batch(ctx) as b:
+        jid = b.submit(*MIX[1])
+        b.run()
+        b.release(jid)
+        with pytest.raises(pfc.PFCError):
+            b.status(jid)
+
+
+def test_invalid_searches_are_rejected(ctx):
+    with pfc.Batch(ctx) as b:
+        for bad in [(3, 101, 200, 10**6, 2 * 10**6), (1, 100, 200, 10**6, 2 * 10**6),
+                    (1, 101, 200, 2, 10**6), (1, 101, 200, 10**6, 10**6)]:
+            with pytest.raises(pfc.PFCError):
+                b.submit(*bad)
