@@ -346,7 +346,7 @@ static int enqueue_iter_range(pfc_job *j, uint32_t lo, uint32_t hi) {
     const HitBuf h = hitbuf(j);
     auto walk = [&](const WalkArgs &w) {
         if (j->use32) c->launches += launch_walk32(j->c32.view(counts_ptr(j)), w, h, c->st);
-        if (j->use64) c->launches += launch_walk64(j->c64.view(counts_ptr(j) + 1), w, h, c->st);
+        if (j->use64) c->launches += launch_walk64(j->c64.view(counts_ptr(j) + 1), w, h, c->st, j->seg_hi <= (1ull << 63));
     };
     WalkArgs w;
     w.lo = lo;

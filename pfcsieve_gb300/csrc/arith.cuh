@@ -4,7 +4,9 @@
 //   class 32: p < 2^31, Montgomery with R = 2^32: one 32x32->64 multiply
 //             (IMAD.WIDE) plus an IMAD and an IMAD.HI per multiplication;
 //             walk residues are signed, in (-p, p) (redc31s).
-//   class 64: p >= 2^31, Montgomery with R = 2^64.
+//   class 64: p >= 2^31, Montgomery with R = 2^64; walks with p < 2^63 use
+//             lazy one-word steps with R = 2^32 and residues in [0, 2p)
+//             (redc64l).
 //
 // The reference keeps every residue in Montgomery form with R = 2^64
 // (kernels/iterate.cl:44-50: m_mul(a,b) = a*b/2^64 mod p in [0,p)).  Values
@@ -121,11 +123,47 @@ __device__ __forceinline__ uint64_t addmod64(uint64_t a, uint64_t b, uint64_t p)
     return a + b - c;
 }
 
+// Lazy walk step for 2^31 < p < 2^63: x*n*2^-32 (mod p) for x in [0, 2p) and
+// n < 2^31, result again in [0, 2p), no conditional correction.  Montgomery
+// reduction by one 32-bit word with m = lo(x*n) * (-p^-1) mod 2^32:
+//   t = x*n = a0 + 2^32 B,  B = x1*n + hi(x0*n)
+//   m*p = c0 + 2^32 D,      D = m*p1 + hi(m*p0), and a0 + c0 = 2^32 [a0 != 0]
+//   (t + m*p) / 2^32 = B + D + [a0 != 0] < (2p*2^31 + 2^32 p) / 2^32 = 2p.
+// Three 32x32->64 multiply-adds, one multiply-low, one multiply-high.
+__device__ __forceinline__ uint64_t redc64l(uint64_t x, uint32_t n, uint64_t p, uint32_t q) {
+    uint64_t r;
+    asm("{\n\t"
+        ".reg .u32 x0, x1, a0, a1, b0, b1, m, c1, d0, d1, p0, p1, z;\n\t"
+        ".reg .u64 A, Bv, D;\n\t"
+        "mov.b64 {x0, x1}, %1;\n\t"
+        "mov.b64 {p0, p1}, %3;\n\t"
+        "mul.wide.u32 A, x0, %2;\n\t"
+        "mov.b64 {a0, a1}, A;\n\t"
+        "cvt.u64.u32 Bv, a1;\n\t"
+        "mad.wide.u32 Bv, x1, %2, Bv;\n\t"
+        "mul.lo.u32 m, a0, %4;\n\t"
+        "mul.hi.u32 c1, m, p0;\n\t"
+        "cvt.u64.u32 D, c1;\n\t"
+        "mad.wide.u32 D, m, p1, D;\n\t"
+        "mov.b64 {b0, b1}, Bv;\n\t"
+        "mov.b64 {d0, d1}, D;\n\t"
+        "add.cc.u32 z, a0, 0xffffffff;\n\t"
+        "addc.cc.u32 b0, b0, d0;\n\t"
+        "addc.u32 b1, b1, d1;\n\t"
+        "mov.b64 %0, {b0, b1};\n\t"
+        "}"
+        : "=l"(r)
+        : "l"(x), "r"(n), "l"(p), "r"(q));
+    return r;
+}
+
 struct Mont64 {
     uint64_t p, pinv, one /* 2^64 mod p */, r2 /* 2^128 mod p */;
+    uint32_t q32;  // -p^-1 mod 2^32 (lazy walk steps)
     __device__ __forceinline__ void init(uint64_t p_) {
         p = p_;
         pinv = inv64(p);
+        q32 = 0u - (uint32_t)pinv;
         one = (0ull - p) % p;
         uint64_t two = addmod64(one, one, p);
         uint64_t x = addmod64(two, two, p);         // 4*2^64

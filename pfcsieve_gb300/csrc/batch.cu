@@ -37,12 +37,22 @@ namespace pfc {
 
 // ------------------------------------------------------------- device side
 
+// One run of a setup program's timeline: `n` squarings (kind 0), `n` table
+// words from words[a] (kind 1), or the fork of the combined search (kind 2:
+// the compositorial residue is complete).  The runs of a search tile its
+// setup positions [0, nsetup) in order; `start` is the first position.
+struct SetupSeg {
+    uint32_t start, kind, a, n;
+};
+
 template <class W>
 struct JobDev {
     unsigned mode;
     uint32_t nmin, nlast;     // first n; nmax - 1
-    uint32_t nsetup, nwalk;   // timeline: [0, nsetup) setup ops, then nwalk walk steps
-    const W *ops;             // setup op stream
+    uint32_t nsetup, nwalk;   // timeline: [0, nsetup) setup positions, then nwalk walk steps
+    const SetupSeg *segs;     // runs of the setup timeline
+    uint32_t nsegs;
+    const W *words;           // table words of the setup programs
     uint64_t corr_a, corr_b;  // drift corrections (first program; second of the combined search)
     const uint32_t *cmult;    // compositorial multipliers of [nmin, nmax)
     const uint32_t *qlist;    // primorial: primes in [nmin, nmax)
@@ -62,6 +72,60 @@ struct Task {
     uint32_t slot, first, count, lo, hi;
 };
 
+// Setup positions [lo, hi) of NC candidates: acc advances through the
+// program, fork receives the compositorial residue at the fork.  Same
+// operations as run_prog in the same order, resumable at any position.
+template <class T, int NC, bool FUSED>
+__device__ __forceinline__ void run_setup(const typename T::M (&m)[NC], typename T::W (&acc)[NC],
+                                          typename T::W (&fork)[NC], const JobDev<typename T::W> &J, uint32_t lo,
+                                          uint32_t hi) {
+    using W = typename T::W;
+    uint32_t a = 0, b = J.nsegs;  // segs[a].start <= lo
+    while (b - a > 1) {
+        const uint32_t mid = (a + b) >> 1;
+        if (__ldg(&J.segs[mid].start) <= lo) a = mid;
+        else b = mid;
+    }
+    uint32_t pos = lo;
+    for (uint32_t s = a; pos < hi && s < J.nsegs; ++s) {
+        const uint4 g = __ldg(reinterpret_cast<const uint4 *>(J.segs + s));  // start, kind, a, n
+        const uint32_t off = pos - g.x;
+        const uint32_t len = g.y == 2 ? 1u : g.w;
+        const uint32_t cnt = min(len - off, hi - pos);
+        if (g.y == 0) {
+            for (uint32_t k = 0; k < cnt; ++k) {
+#pragma unroll
+                for (int c = 0; c < NC; ++c) acc[c] = m[c].mul(acc[c], acc[c]);
+            }
+        } else if (g.y == 1) {
+            const W *wp = J.words + g.z + off;
+            uint32_t k = 0;
+            for (; k + 4 <= cnt; k += 4) {
+                const W w0 = __ldg(wp + k), w1 = __ldg(wp + k + 1), w2 = __ldg(wp + k + 2), w3 = __ldg(wp + k + 3);
+#pragma unroll
+                for (int c = 0; c < NC; ++c) {
+                    acc[c] = T::word(m[c], acc[c], w0);
+                    acc[c] = T::word(m[c], acc[c], w1);
+                    acc[c] = T::word(m[c], acc[c], w2);
+                    acc[c] = T::word(m[c], acc[c], w3);
+                }
+            }
+            for (; k < cnt; ++k) {
+                const W w = __ldg(wp + k);
+#pragma unroll
+                for (int c = 0; c < NC; ++c) acc[c] = T::word(m[c], acc[c], w);
+            }
+        } else {
+#pragma unroll
+            for (int c = 0; c < NC; ++c) {
+                acc[c] = m[c].mul(acc[c], m[c].mont_R_pow(J.corr_a));
+                fork[c] = acc[c];
+            }
+        }
+        pos += cnt;
+    }
+}
+
 template <class T, int NC, bool FUSED>
 __device__ void run_task(const JobDev<typename T::W> &J, const Task &t, const HitBuf &h) {
     using W = typename T::W;
@@ -80,7 +144,7 @@ __device__ void run_task(const JobDev<typename T::W> &J, const Task &t, const Hi
     W x[NS];
     uint32_t walked = 0;
     if (t.lo < S) {
-        // setup part: evaluate ops [lo, min(hi, S)) of the job's program
+        // setup part: positions [lo, min(hi, S)) of the job's programs
         W acc[NC], fork[NC];
 #pragma unroll
         for (int s = 0; s < NC; ++s) {
@@ -88,22 +152,7 @@ __device__ void run_task(const JobDev<typename T::W> &J, const Task &t, const Hi
             fork[s] = (FUSED && t.lo > 0 && act[s]) ? J.c.s1[idx[s]] : (W)0;
         }
         const uint32_t e = min(t.hi, S);
-        for (uint32_t i = t.lo; i < e; ++i) {
-            const W w = __ldg(J.ops + i);
-            if (w == 0) {
-#pragma unroll
-                for (int s = 0; s < NC; ++s) acc[s] = m[s].mul(acc[s], acc[s]);
-            } else if (w == 1) {
-#pragma unroll
-                for (int s = 0; s < NC; ++s) {
-                    acc[s] = m[s].mul(acc[s], m[s].mont_R_pow(J.corr_a));
-                    fork[s] = acc[s];
-                }
-            } else {
-#pragma unroll
-                for (int s = 0; s < NC; ++s) acc[s] = T::word(m[s], acc[s], w);
-            }
-        }
+        run_setup<T, NC, FUSED>(m, acc, fork, J, t.lo, e);
         if (e == S) {
 #pragma unroll
             for (int s = 0; s < NC; ++s) acc[s] = m[s].mul(acc[s], m[s].mont_R_pow(FUSED ? J.corr_b : J.corr_a));
@@ -199,26 +248,29 @@ __device__ void run_task(const JobDev<typename T::W> &J, const Task &t, const Hi
     if (__any_sync(kFull, bad) && (threadIdx.x & 31) == 0) atomicOr(J.flags, 1u);
 }
 
+// One CTA per task.  The task list of an iteration is ordered longest first
+// (windows with setup work, then full walk windows, then the short ends of
+// blocks), and the hardware block scheduler hands tasks to SMs as CTA slots
+// free up: a device-side work queue whose tail is spread over all SMs.  (A
+// persistent grid taking tasks from an atomic counter let the last tasks of
+// an iteration crowd onto a few SMs: 78% of the per-job path's throughput on
+// a single large search, against 100% with hardware dispatch.)
 template <class T>
-__global__ void __launch_bounds__(256, 3) batch_kernel(const Task *tasks, const uint32_t *ntasks, unsigned *head,
-                                                    const JobDev<typename T::W> *jobs, HitBuf h) {
+__global__ void __launch_bounds__(256, sizeof(typename T::W) == 4 ? 4 : 2)
+    batch_kernel(const Task *tasks, const JobDev<typename T::W> *jobs, HitBuf h) {
+    // the task and its search record live in shared memory: every thread
+    // reads the same fields, and registers stay free for the residues
     __shared__ Task st;
-    for (;;) {
-        if (threadIdx.x == 0) {
-            const unsigned i = atomicAdd(head, 1u);
-            if (i < *ntasks) st = tasks[i];
-            else st.slot = 0xffffffffu;
-        }
-        __syncthreads();
-        const Task t = st;
-        __syncthreads();
-        if (t.slot == 0xffffffffu) break;
-        const JobDev<typename T::W> J = jobs[t.slot];
-        HitBuf hh = h;
-        hh.tagval = t.slot;
-        if (J.mode == (PFC_FACTORIAL | PFC_COMPOSITORIAL)) run_task<T, 1, true>(J, t, hh);
-        else run_task<T, T::NC, false>(J, t, hh);
+    __shared__ JobDev<typename T::W> sj;
+    if (threadIdx.x == 0) {
+        st = tasks[blockIdx.x];
+        sj = jobs[st.slot];
     }
+    __syncthreads();
+    HitBuf hh = h;
+    hh.tagval = st.slot;
+    if (sj.mode == (PFC_FACTORIAL | PFC_COMPOSITORIAL)) run_task<T, 1, true>(sj, st, hh);
+    else run_task<T, T::NC, false>(sj, st, hh);
 }
 
 // ------------------------------------------------------------------ host side
@@ -240,15 +292,18 @@ struct BatchJob {
     uint32_t slot = 0;
     // host tables, built by prepare_job
     int prep_rc = PFC_OK;
-    std::vector<uint32_t> ops32, cmult, qlist;
-    std::vector<uint64_t> ops64;
+    std::vector<uint32_t> words32, cmult, qlist;
+    std::vector<uint64_t> words64;
+    std::vector<SetupSeg> segs32, segs64;
+    uint32_t nsetup32 = 0, nsetup64 = 0;
     uint64_t c32a = 0, c32b = 0, c64a = 0, c64b = 0;
     uint32_t nwalk = 0;
     bool use32 = false, use64 = false;
     uint32_t cap32 = 0, cap64 = 0;
     // device
-    DArr<uint32_t> d_ops32, d_cmult, d_qlist;
-    DArr<uint64_t> d_ops64;
+    DArr<uint32_t> d_words32, d_cmult, d_qlist;
+    DArr<uint64_t> d_words64;
+    DArr<SetupSeg> d_segs32, d_segs64;
     DevClass<uint32_t> c32;
     DevClass<uint64_t> c64;
     std::vector<Block> b32, b64;
@@ -267,14 +322,28 @@ static double est_cands(uint64_t lo, uint64_t hi) {
     return (double)(hi - lo) / std::log(a) * 1.25 + 30.0;
 }
 
-// a setup program as one op stream: 0 = square, else a word to multiply in
+// append a setup program's runs (and words) to a search's timeline; returns
+// the next position
 template <class W>
-static void append_ops(const HostProg<W> &h, std::vector<W> &ops) {
+static uint32_t append_prog(const HostProg<W> &h, uint32_t pos, std::vector<SetupSeg> &segs, std::vector<W> &words) {
+    const uint32_t wbase = (uint32_t)words.size();
+    words.insert(words.end(), h.words.begin(), h.words.end());
     for (size_t g = 0; g + 2 < h.groups.size(); g += 3) {
-        ops.insert(ops.end(), h.groups[g + 2], (W)0);
-        ops.insert(ops.end(), h.words.begin() + h.groups[g], h.words.begin() + h.groups[g + 1]);
+        const uint32_t b = h.groups[g], e = h.groups[g + 1], sq = h.groups[g + 2];
+        if (sq) {
+            segs.push_back({pos, 0u, 0u, sq});
+            pos += sq;
+        }
+        if (e > b) {
+            segs.push_back({pos, 1u, wbase + b, e - b});
+            pos += e - b;
+        }
     }
-    ops.insert(ops.end(), h.final_sq, (W)0);
+    if (h.final_sq) {
+        segs.push_back({pos, 0u, 0u, h.final_sq});
+        pos += h.final_sq;
+    }
+    return pos;
 }
 
 static uint32_t prime_limit(const BatchJob *j) {
@@ -302,15 +371,16 @@ static void prepare_job(BatchJob *j, const std::vector<uint32_t> &cache) {
         j->prep_rc = PFC_ERR_ARG;
         return;
     }
-    append_ops(a32, j->ops32);
-    append_ops(a64, j->ops64);
+    j->nsetup32 = append_prog(a32, 0, j->segs32, j->words32);
+    j->nsetup64 = append_prog(a64, 0, j->segs64, j->words64);
     j->c32a = a32.corr;
     j->c64a = a64.corr;
     if (mode == (PFC_FACTORIAL | PFC_COMPOSITORIAL)) {
-        j->ops32.push_back(1u);  // fork: the compositorial residue is complete here
-        j->ops64.push_back(1u);
-        append_ops(b32, j->ops32);
-        append_ops(b64, j->ops64);
+        // fork: the compositorial residue is complete here
+        j->segs32.push_back({j->nsetup32++, 2u, 0u, 1u});
+        j->segs64.push_back({j->nsetup64++, 2u, 0u, 1u});
+        j->nsetup32 = append_prog(b32, j->nsetup32, j->segs32, j->words32);
+        j->nsetup64 = append_prog(b64, j->nsetup64, j->segs64, j->words64);
         j->c32b = b32.corr;
         j->c64b = b64.corr;
     }
@@ -335,8 +405,8 @@ static void prepare_job(BatchJob *j, const std::vector<uint32_t> &cache) {
     const double e64 = est_cands(std::max<uint64_t>(j->pmin, kClassSplit), j->pmax);
     j->cap32 = j->use32 ? (uint32_t)std::min(e32, 4.0e9) : 0;
     j->cap64 = j->use64 ? (uint32_t)std::min(e64, 4.0e9) : 0;
-    j->tot32 = (uint32_t)j->ops32.size() + j->nwalk;
-    j->tot64 = (uint32_t)j->ops64.size() + j->nwalk;
+    j->tot32 = j->nsetup32 + j->nwalk;
+    j->tot64 = j->nsetup64 + j->nwalk;
     j->prep_rc = PFC_OK;
 }
 
@@ -357,8 +427,8 @@ struct pfc_batch {
     DArr<BatchStats> stats;
     DArr<JobDev<uint32_t>> jobs32;
     DArr<JobDev<uint64_t>> jobs64;
-    DArr<Task> tasks32, tasks64;
-    DArr<uint32_t> ctrl;  // [0] ntasks32, [1] ntasks64, [2] head32, [3] head64
+    // task lists: class 32, class 64 below 2^63 (lazy walk), other class 64
+    DArr<Task> tasks32, tasks64, tasks64c;
     DArr<pfc_factor> hits;
     DArr<uint32_t> tags;
     DArr<unsigned long long> hitcount;
@@ -371,9 +441,8 @@ struct pfc_batch {
     std::vector<uint32_t> free_slots;
     std::vector<uint32_t> prime_cache;   // primes up to cache_lim
     uint32_t cache_lim = 0;
-    std::vector<Task> t32, t64;
+    std::vector<Task> t32, t64, t64c;
     uint64_t next_id = 1;
-    int grid32 = 0, grid64 = 0;
     double work_per_iter = 4e11;         // candidate-steps per iteration (class 64 weighs 3)
     uint64_t iterations = 0;
     // timing: kernel spans (CUDA events) and host phases (wall clock)
@@ -413,8 +482,10 @@ void prepare_queued(pfc_batch *b) {
 
 void release_device(pfc_batch *b, BatchJob *j) {
     pfc_ctx *c = b->ctx;
-    j->d_ops32.release(c);
-    j->d_ops64.release(c);
+    j->d_words32.release(c);
+    j->d_words64.release(c);
+    j->d_segs32.release(c);
+    j->d_segs64.release(c);
     j->d_cmult.release(c);
     j->d_qlist.release(c);
     j->c32.release(c);
@@ -448,8 +519,10 @@ int launch_job_gen(pfc_batch *b, BatchJob *j) {
 // PFC_ERR_NOMEM leaves nothing allocated.
 int upload_job(pfc_batch *b, BatchJob *j) {
     pfc_ctx *c = b->ctx;
-    cudaError_t e = j->d_ops32.upload(c, j->ops32);
-    if (e == cudaSuccess) e = j->d_ops64.upload(c, j->ops64);
+    cudaError_t e = j->d_words32.upload(c, j->words32);
+    if (e == cudaSuccess) e = j->d_words64.upload(c, j->words64);
+    if (e == cudaSuccess) e = j->d_segs32.upload(c, j->segs32);
+    if (e == cudaSuccess) e = j->d_segs64.upload(c, j->segs64);
     if (e == cudaSuccess) e = j->d_cmult.upload(c, j->cmult);
     if (e == cudaSuccess) e = j->d_qlist.upload(c, j->qlist);
     if (e == cudaSuccess) e = j->c32.ensure(c, j->cap32);
@@ -462,8 +535,8 @@ int upload_job(pfc_batch *b, BatchJob *j) {
 }
 
 template <class W>
-JobDev<W> job_view(pfc_batch *b, BatchJob *j, const DevClass<W> &cls, int which, const DArr<W> &ops, uint64_t ca,
-                   uint64_t cb, uint32_t nsetup) {
+JobDev<W> job_view(pfc_batch *b, BatchJob *j, const DevClass<W> &cls, int which, const DArr<W> &words,
+                   const DArr<SetupSeg> &segs, size_t nsegs, uint64_t ca, uint64_t cb, uint32_t nsetup) {
     JobDev<W> d;
     memset(&d, 0, sizeof(d));
     d.mode = j->mode;
@@ -471,7 +544,9 @@ JobDev<W> job_view(pfc_batch *b, BatchJob *j, const DevClass<W> &cls, int which,
     d.nlast = j->nmax - 1;
     d.nsetup = nsetup;
     d.nwalk = j->nwalk;
-    d.ops = ops.p;
+    d.segs = segs.p;
+    d.nsegs = (uint32_t)nsegs;
+    d.words = words.p;
     d.corr_a = ca;
     d.corr_b = cb;
     d.cmult = j->d_cmult.p;
@@ -542,16 +617,20 @@ int admit_prepared(pfc_batch *b) {
         const uint32_t per64 = 256u * Cls64::NC;
         for (uint32_t k = 0; k < n32; k += per32) j->b32.push_back({k, std::min(per32, n32 - k), 0});
         for (uint32_t k = 0; k < n64; k += per64) j->b64.push_back({k, std::min(per64, n64 - k), 0});
-        v32[f] = job_view<uint32_t>(b, j, j->c32, 0, j->d_ops32, j->c32a, j->c32b, (uint32_t)j->ops32.size());
-        v64[f] = job_view<uint64_t>(b, j, j->c64, 1, j->d_ops64, j->c64a, j->c64b, (uint32_t)j->ops64.size());
+        v32[f] = job_view<uint32_t>(b, j, j->c32, 0, j->d_words32, j->d_segs32, j->segs32.size(), j->c32a, j->c32b,
+                                    j->nsetup32);
+        v64[f] = job_view<uint64_t>(b, j, j->c64, 1, j->d_words64, j->d_segs64, j->segs64.size(), j->c64a, j->c64b,
+                                    j->nsetup64);
         CK(cudaMemcpyAsync(b->jobs32.p + j->slot, &v32[f], sizeof(v32[f]), cudaMemcpyHostToDevice, c->st));
         CK(cudaMemcpyAsync(b->jobs64.p + j->slot, &v64[f], sizeof(v64[f]), cudaMemcpyHostToDevice, c->st));
         c->h2d += sizeof(v32[f]) + sizeof(v64[f]);
     }
     CK(cudaStreamSynchronize(c->st));
     for (BatchJob *j : fresh) {
-        free_vec(j->ops32);  // on the device now; only the lengths are kept
-        free_vec(j->ops64);
+        free_vec(j->words32);  // on the device now
+        free_vec(j->words64);
+        free_vec(j->segs32);
+        free_vec(j->segs64);
         free_vec(j->cmult);
         free_vec(j->qlist);
         j->state = kReady;
@@ -575,29 +654,40 @@ uint32_t build_tasks(pfc_batch *b) {
     }
     const double Ld = std::max(64.0, std::min(b->work_per_iter / std::max(cands, 1.0), 4194304.0));
     const uint32_t L = ((uint32_t)Ld + 15u) & ~15u;
-    b->t32.clear();
-    b->t64.clear();
+    // longest first: windows with setup work, full walk windows, short ends
+    std::vector<Task> part[3][3];  // [list][kind]
     for (BatchJob *j : b->running) {
-        for (const Block &k : j->b32)
-            if (k.pos < j->tot32)
-                b->t32.push_back({j->slot, k.first, k.count, k.pos, (uint32_t)std::min<uint64_t>((uint64_t)k.pos + L, j->tot32)});
-        for (const Block &k : j->b64)
-            if (k.pos < j->tot64)
-                b->t64.push_back({j->slot, k.first, k.count, k.pos, (uint32_t)std::min<uint64_t>((uint64_t)k.pos + L, j->tot64)});
+        const int l64 = j->pmax <= kLazyLimit ? 1 : 2;
+        for (int cls = 0; cls < 2; ++cls) {
+            const std::vector<Block> &blocks = cls ? j->b64 : j->b32;
+            const uint32_t tot = cls ? j->tot64 : j->tot32, ns = cls ? j->nsetup64 : j->nsetup32;
+            std::vector<Task> *dst = part[cls ? l64 : 0];
+            for (const Block &k : blocks) {
+                if (k.pos >= tot) continue;
+                const uint32_t hi = (uint32_t)std::min<uint64_t>((uint64_t)k.pos + L, tot);
+                const int kind = k.pos < ns ? 0 : (hi - k.pos == L ? 1 : 2);
+                dst[kind].push_back({j->slot, k.first, k.count, k.pos, hi});
+            }
+        }
+    }
+    std::vector<Task> *out[3] = {&b->t32, &b->t64, &b->t64c};
+    for (int l = 0; l < 3; ++l) {
+        out[l]->clear();
+        for (int kind = 0; kind < 3; ++kind) out[l]->insert(out[l]->end(), part[l][kind].begin(), part[l][kind].end());
     }
     return L;
 }
 
 int launch_iteration(pfc_batch *b) {
     pfc_ctx *c = b->ctx;
-    const size_t n32 = b->t32.size(), n64 = b->t64.size();
+    const size_t n32 = b->t32.size(), n64 = b->t64.size(), n64c = b->t64c.size();
     if (b->tasks32.n < n32) CK(b->tasks32.alloc(c, n32 + n32 / 2 + 64));
     if (b->tasks64.n < n64) CK(b->tasks64.alloc(c, n64 + n64 / 2 + 64));
-    const uint32_t ctrl[4] = {(uint32_t)n32, (uint32_t)n64, 0u, 0u};
+    if (b->tasks64c.n < n64c) CK(b->tasks64c.alloc(c, n64c + n64c / 2 + 64));
     if (n32) CK(cudaMemcpyAsync(b->tasks32.p, b->t32.data(), n32 * sizeof(Task), cudaMemcpyHostToDevice, c->st));
     if (n64) CK(cudaMemcpyAsync(b->tasks64.p, b->t64.data(), n64 * sizeof(Task), cudaMemcpyHostToDevice, c->st));
-    CK(cudaMemcpyAsync(b->ctrl.p, ctrl, sizeof(ctrl), cudaMemcpyHostToDevice, c->st));
-    c->h2d += (n32 + n64) * sizeof(Task) + sizeof(ctrl);
+    if (n64c) CK(cudaMemcpyAsync(b->tasks64c.p, b->t64c.data(), n64c * sizeof(Task), cudaMemcpyHostToDevice, c->st));
+    c->h2d += (n32 + n64 + n64c) * sizeof(Task);
     CK(cudaEventRecord(b->ev_start, c->st));
     CK(cudaStreamWaitEvent(b->st32, b->ev_start, 0));
     CK(cudaStreamWaitEvent(b->st64, b->ev_start, 0));
@@ -607,13 +697,15 @@ int launch_iteration(pfc_batch *b) {
     h.cap = b->hits.n;
     h.tag = b->tags.p;
     if (n32) {
-        const int grid = (int)std::min<size_t>(b->grid32, n32);
-        batch_kernel<Cls32><<<grid, 256, 0, b->st32>>>(b->tasks32.p, b->ctrl.p + 0, b->ctrl.p + 2, b->jobs32.p, h);
+        batch_kernel<Cls32><<<(unsigned)n32, 256, 0, b->st32>>>(b->tasks32.p, b->jobs32.p, h);
         c->launches++;
     }
     if (n64) {
-        const int grid = (int)std::min<size_t>(b->grid64, n64);
-        batch_kernel<Cls64><<<grid, 256, 0, b->st64>>>(b->tasks64.p, b->ctrl.p + 1, b->ctrl.p + 3, b->jobs64.p, h);
+        batch_kernel<Cls64L><<<(unsigned)n64, 256, 0, b->st64>>>(b->tasks64.p, b->jobs64.p, h);
+        c->launches++;
+    }
+    if (n64c) {
+        batch_kernel<Cls64><<<(unsigned)n64c, 256, 0, b->st64>>>(b->tasks64c.p, b->jobs64.p, h);
         c->launches++;
     }
     CK(cudaGetLastError());
@@ -622,9 +714,9 @@ int launch_iteration(pfc_batch *b) {
     CK(cudaStreamWaitEvent(c->st, b->ev_end32, 0));
     CK(cudaEventRecord(b->ev_end64, b->st64));
     CK(cudaStreamWaitEvent(c->st, b->ev_end64, 0));
-    b->tasks += n32 + n64;
+    b->tasks += n32 + n64 + n64c;
     b->t32_n = n32;
-    b->t64_n = n64;
+    b->t64_n = n64 + n64c;
     CK(cudaMemcpyAsync(b->h_hitcount, b->hitcount.p, sizeof(unsigned long long), cudaMemcpyDeviceToHost, c->st));
     return PFC_OK;
 }
@@ -747,7 +839,6 @@ extern "C" int pfc_batch_create(pfc_ctx *c, pfc_batch **out) {
     if (e == cudaSuccess) e = b->stats.alloc(c, pfc_batch::kSlots);
     if (e == cudaSuccess) e = b->jobs32.alloc(c, pfc_batch::kSlots);
     if (e == cudaSuccess) e = b->jobs64.alloc(c, pfc_batch::kSlots);
-    if (e == cudaSuccess) e = b->ctrl.alloc(c, 4);
     if (e == cudaSuccess) e = b->hits.alloc(c, 1u << 20);
     if (e == cudaSuccess) e = b->tags.alloc(c, 1u << 20);
     if (e == cudaSuccess) e = b->hitcount.alloc(c, 1);
@@ -756,15 +847,10 @@ extern "C" int pfc_batch_create(pfc_ctx *c, pfc_batch **out) {
     if (e == cudaSuccess) e = cudaMemsetAsync(b->hitcount.p, 0, sizeof(unsigned long long), c->st);
     if (e == cudaSuccess) e = cudaMemsetAsync(b->stats.p, 0, sizeof(BatchStats) * pfc_batch::kSlots, c->st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(c->st);
-    int n32 = 0, n64 = 0;
-    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n32, batch_kernel<Cls32>, 256, 0);
-    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n64, batch_kernel<Cls64>, 256, 0);
     if (e != cudaSuccess) {
         pfc_batch_destroy(b);
         return cuda_fail(e);
     }
-    b->grid32 = std::max(1, n32) * c->sms;
-    b->grid64 = std::max(1, n64) * c->sms;
     for (uint32_t s = pfc_batch::kSlots; s-- > 0;) b->free_slots.push_back(s);
     *out = b;
     return PFC_OK;
@@ -783,7 +869,7 @@ extern "C" int pfc_batch_destroy(pfc_batch *b) {
     b->jobs64.release(c);
     b->tasks32.release(c);
     b->tasks64.release(c);
-    b->ctrl.release(c);
+    b->tasks64c.release(c);
     b->hits.release(c);
     b->tags.release(c);
     b->hitcount.release(c);
@@ -837,7 +923,7 @@ extern "C" int pfc_batch_step(pfc_batch *b, uint32_t *active, uint32_t *queued) 
     const double ts = now_s();
     for (int pass = 0; pass < 2; ++pass) {
         const uint32_t L = build_tasks(b);
-        const bool work = !b->t32.empty() || !b->t64.empty();
+        const bool work = !b->t32.empty() || !b->t64.empty() || !b->t64c.empty();
         if (work) {
             const int rc = launch_iteration(b);
             if (rc) return rc;

@@ -100,7 +100,8 @@ int launch_gen(const GenArgs &a, int sms, cudaStream_t st);
 int launch_setup32(const ClassBuf<uint32_t> &c, const SetupArgs<uint32_t> &a, cudaStream_t st);
 int launch_setup64(const ClassBuf<uint64_t> &c, const SetupArgs<uint64_t> &a, cudaStream_t st);
 int launch_walk32(const ClassBuf<uint32_t> &c, const WalkArgs &a, const HitBuf &h, cudaStream_t st);
-int launch_walk64(const ClassBuf<uint64_t> &c, const WalkArgs &a, const HitBuf &h, cudaStream_t st);
+// lazy: every candidate is below 2^63 (the walk then takes lazy one-word steps)
+int launch_walk64(const ClassBuf<uint64_t> &c, const WalkArgs &a, const HitBuf &h, cudaStream_t st, bool lazy);
 // compositorial multipliers of n in [lo, hi): n when composite, 1 when prime
 // (bit k of primebits <-> n = nmin + k); `out` is padded with 1 to a multiple of 16
 int launch_cmult(uint32_t *out, const uint32_t *primebits, uint32_t nmin, uint32_t lo, uint32_t hi,

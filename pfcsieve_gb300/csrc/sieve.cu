@@ -148,8 +148,8 @@ static int launch_walk(const ClassBuf<typename T::W> &c, const WalkArgs &a, cons
 int launch_walk32(const ClassBuf<uint32_t> &c, const WalkArgs &a, const HitBuf &h, cudaStream_t st) {
     return launch_walk<Cls32>(c, a, h, st);
 }
-int launch_walk64(const ClassBuf<uint64_t> &c, const WalkArgs &a, const HitBuf &h, cudaStream_t st) {
-    return launch_walk<Cls64>(c, a, h, st);
+int launch_walk64(const ClassBuf<uint64_t> &c, const WalkArgs &a, const HitBuf &h, cudaStream_t st, bool lazy) {
+    return lazy ? launch_walk<Cls64L>(c, a, h, st) : launch_walk<Cls64>(c, a, h, st);
 }
 
 int launch_cmult(uint32_t *out, const uint32_t *primebits, uint32_t nmin, uint32_t lo, uint32_t hi,

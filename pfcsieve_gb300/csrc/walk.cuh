@@ -31,24 +31,38 @@ namespace pfc {
 
 constexpr unsigned kFull = 0xffffffffu;
 
+// Size-class traits.  Each class supplies: the fast step and its hit filter
+// (a superset test: every true hit passes, rare false alarms are dropped by
+// the exact replay), the targets of the drift walk, the restore constant for
+// r fast steps, the exact canonical step used by the replay, and the setup
+// and checksum helpers.
+
 struct Cls32 {
     using W = uint32_t;
     using M = Mont32;
     static constexpr int B = 8;           // block length with two candidates per thread
     static constexpr int B_FUSED = 16;    // block length of the fused -! -c walk
     static constexpr int NC = 2;          // candidates per thread in single-chain walks
-    static constexpr bool kSigned = true; // walk residues signed in (-p, p), p < 2^31
-    // fast walk step and its hit test: x = +-T (mod p) <=> |x| in {T, p - T}
+    struct Tgt {
+        W t, nt;
+    };
+    // walk residues signed in (-p, p), p < 2^31; after j+1 steps from r*R,
+    // x = r' * R^-j, so the targets are T_j = R^-j
+    __device__ static __forceinline__ W target0(const M &) { return 1; }
+    __device__ static __forceinline__ W next_target(const M &m, W t) { return m.mul(t, 1); }
+    __device__ static __forceinline__ Tgt mk(const M &m, W t) { return {t, m.p - t}; }
     __device__ static __forceinline__ W fstep(const M &m, W x, uint32_t n) {
         return (W)redc31s((int32_t)x, n, (int32_t)m.p, m.pinv);
     }
-    __device__ static __forceinline__ bool fhit(W x, W t, W nt) {
+    // x = +-T (mod p) <=> |x| in {T, p - T}
+    __device__ static __forceinline__ bool fhit(W x, const Tgt &g) {
         const uint32_t ax = (uint32_t)abs((int32_t)x);
-        return (ax == t) | (ax == nt);
+        return (ax == g.t) | (ax == g.nt);
     }
-    __device__ static __forceinline__ W canon(const M &m, W x) { return (int32_t)x < 0 ? x + m.p : x; }
-    // x*K*R^-1 for the block restore (K < p < 2^31)
+    // r fast steps leave r' * R^(1-r): multiply by K = R^(r+1) (and R^-1)
+    __device__ static __forceinline__ W K(const M &m, int r) { return m.mont_R_pow((uint64_t)r); }
     __device__ static __forceinline__ W restore(const M &m, W x, W K) { return fstep(m, x, K); }
+    __device__ static __forceinline__ W canon(const M &m, W x) { return (int32_t)x < 0 ? x + m.p : x; }
     __device__ static __forceinline__ W step(const M &m, W s, uint32_t n) { return redc32(s, n, m.p, m.pinv); }
     __device__ static __forceinline__ W word(const M &m, W s, W w) { return redc32(s, w, m.p, m.pinv); }
     // checksum form: residue * 2^64 mod p from its class-32 Montgomery form
@@ -56,22 +70,72 @@ struct Cls32 {
     __device__ static __forceinline__ uint64_t mont64_of(const M &m, uint32_t v) { return m.mul(m.mul(v, m.r2), m.r2); }
 };
 
+// p >= 2^31, canonical residues, R = 2^64 (any p < 2^64)
 struct Cls64 {
     using W = uint64_t;
     using M = Mont64;
     static constexpr int B = 8;
     static constexpr int B_FUSED = 8;
     static constexpr int NC = 1;
-    static constexpr bool kSigned = false;
+    struct Tgt {
+        W t, nt;
+    };
+    __device__ static __forceinline__ W target0(const M &) { return 1; }
+    __device__ static __forceinline__ W next_target(const M &m, W t) { return m.mul(t, 1); }
+    __device__ static __forceinline__ Tgt mk(const M &m, W t) { return {t, m.p - t}; }
     __device__ static __forceinline__ W fstep(const M &m, W x, uint32_t n) { return redc64_u32(x, n, m.p, m.pinv); }
-    __device__ static __forceinline__ bool fhit(W x, W t, W nt) { return (x == t) | (x == nt); }
-    __device__ static __forceinline__ W canon(const M &, W x) { return x; }
+    __device__ static __forceinline__ bool fhit(W x, const Tgt &g) { return (x == g.t) | (x == g.nt); }
+    __device__ static __forceinline__ W K(const M &m, int r) { return m.mont_R_pow((uint64_t)r); }
     __device__ static __forceinline__ W restore(const M &m, W x, W K) { return m.mul(x, K); }
+    __device__ static __forceinline__ W canon(const M &, W x) { return x; }
     __device__ static __forceinline__ W step(const M &m, W s, uint32_t n) { return redc64_u32(s, n, m.p, m.pinv); }
     __device__ static __forceinline__ W word(const M &m, W s, W w) { return redc64(s, w, m.p, m.pinv); }
     __device__ static __forceinline__ uint64_t term(const M &, W s) { return s; }
     __device__ static __forceinline__ uint64_t mont64_of(const M &m, uint32_t v) { return m.to_mont(v); }
 };
+
+// 2^31 < p < 2^63: the walk takes lazy one-word steps (R' = 2^32, residues in
+// [0, 2p), redc64l) from the R = 2^64 setup values.  After j+1 steps from
+// r*2^64, x = r' * 2^64 * 2^(-32(j+1)) (mod p), so the targets are
+// U_j = 2^(32-32j) mod p; x = +-U (mod p) with x in [0, 2p) means x is one of
+// U, U + p, p - U, 2p - U, and the fast filter compares the low 32 bits of x
+// with those four (a false alarm costs one replay).
+struct Cls64L {
+    using W = uint64_t;
+    using M = Mont64;
+    static constexpr int B = 8;
+    static constexpr int B_FUSED = 8;
+    static constexpr int NC = 1;
+    struct Tgt {
+        uint32_t a, b, c, d;
+    };
+    __device__ static __forceinline__ W canon(const M &m, W x) { return x >= m.p ? x - m.p : x; }
+    __device__ static __forceinline__ W target0(const M &m) { return canon(m, redc64l(m.one, 1u, m.p, m.q32)); }
+    __device__ static __forceinline__ W next_target(const M &m, W t) { return canon(m, redc64l(t, 1u, m.p, m.q32)); }
+    __device__ static __forceinline__ Tgt mk(const M &m, W t) {
+        return {(uint32_t)t, (uint32_t)(t + m.p), (uint32_t)(m.p - t), (uint32_t)(2 * m.p - t)};
+    }
+    __device__ static __forceinline__ W fstep(const M &m, W x, uint32_t n) { return redc64l(x, n, m.p, m.q32); }
+    __device__ static __forceinline__ bool fhit(W x, const Tgt &g) {
+        const uint32_t lo = (uint32_t)x;
+        return (lo == g.a) | (lo == g.b) | (lo == g.c) | (lo == g.d);
+    }
+    // r lazy steps leave r' * 2^64 * 2^(-32r): K = 2^(32r) * 2^64 mod p, the
+    // Montgomery form of 2^(32r), from Mont(2^(64k)) = mont_R_pow(k)
+    __device__ static __forceinline__ W K(const M &m, int r) {
+        const W k = m.mont_R_pow((uint64_t)((r + 1) >> 1));
+        return (r & 1) ? canon(m, redc64l(k, 1u, m.p, m.q32)) : k;
+    }
+    // x < 2p and K < p with p < 2^63 keep x*K < p*2^64: canonical result
+    __device__ static __forceinline__ W restore(const M &m, W x, W K) { return m.mul(x, K); }
+    __device__ static __forceinline__ W step(const M &m, W s, uint32_t n) { return canon(m, redc64l(s, n, m.p, m.q32)); }
+    __device__ static __forceinline__ W word(const M &m, W s, W w) { return redc64(s, w, m.p, m.pinv); }
+    __device__ static __forceinline__ uint64_t term(const M &, W s) { return s; }
+    __device__ static __forceinline__ uint64_t mont64_of(const M &m, uint32_t v) { return m.to_mont(v); }
+};
+
+// largest p a class-64 segment may hold for the lazy walk
+constexpr uint64_t kLazyLimit = 1ull << 63;
 
 template <class W>
 __device__ __forceinline__ W ldg(const W *p) { return __ldg(p); }
@@ -151,9 +215,9 @@ __device__ __noinline__ void replay_chain(const typename T::M m, typename T::W x
                                           const HitBuf h) {
     using W = typename T::W;
     x = T::canon(m, x);
-    W t = 1;
+    W t = T::target0(m);
     for (int j = 0; j < len; ++j) {
-        if (j) t = m.mul(t, 1);
+        if (j) t = T::next_target(m, t);
         const uint32_t mul = mult ? __ldg(mult + (k - base) + j) : k + j;
         x = T::step(m, x, mul);
         const bool hit = active && mul != 1u && (x == t || x == m.p - t);
@@ -168,23 +232,25 @@ __device__ __noinline__ void replay_chain(const typename T::M m, typename T::W x
 //     chain (multiplier table a.mult2) of one candidate, sharing its targets;
 //   otherwise NC candidates (1 or 2) on the same multiplier sequence.
 // x holds canonical Montgomery-form residues on entry and on exit.  Inactive
-// streams hold 0, which never matches a target (targets are in [1, p-1]), so
-// they never trigger a replay.
+// streams hold 0, which never matches a target (targets are nonzero mod p),
+// so they never trigger a replay.
 template <class T, int NC, bool FUSED>
 __device__ __forceinline__ void walk_streams(const typename T::M (&m)[NC], typename T::W (&x)[FUSED ? 2 : NC],
                                              const bool (&act)[NC], const WalkArgs &a, const HitBuf &h) {
     using W = typename T::W;
     constexpr int B = FUSED ? T::B_FUSED : T::B;
     constexpr int NS = FUSED ? 2 : NC;
-    W tg[NC][B], ntg[NC][B], K[NC];
+    typename T::Tgt tg[NC][B];
+    W K[NC];
 #pragma unroll
     for (int s = 0; s < NC; ++s) {
-        tg[s][0] = 1;
+        W t = T::target0(m[s]);
 #pragma unroll
-        for (int j = 1; j < B; ++j) tg[s][j] = m[s].mul(tg[s][j - 1], 1);
-#pragma unroll
-        for (int j = 0; j < B; ++j) ntg[s][j] = m[s].p - tg[s][j];
-        K[s] = m[s].mont_R_pow(B);
+        for (int j = 0; j < B; ++j) {
+            tg[s][j] = T::mk(m[s], t);
+            if (j + 1 < B) t = T::next_target(m[s], t);
+        }
+        K[s] = T::K(m[s], B);
     }
 
     const uint32_t *mult0 = FUSED ? nullptr : a.mult;
@@ -205,12 +271,12 @@ __device__ __forceinline__ void walk_streams(const typename T::M (&m)[NC], typen
             if (FUSED) {
                 x[0] = T::fstep(m[0], x[0], mv[j]);
                 x[NS - 1] = T::fstep(m[0], x[NS - 1], cv[j]);
-                any |= T::fhit(x[0], tg[0][j], ntg[0][j]) | T::fhit(x[NS - 1], tg[0][j], ntg[0][j]);
+                any |= T::fhit(x[0], tg[0][j]) | T::fhit(x[NS - 1], tg[0][j]);
             } else {
 #pragma unroll
                 for (int s = 0; s < NC; ++s) {
                     x[s] = T::fstep(m[s], x[s], mv[j]);
-                    any |= T::fhit(x[s], tg[s][j], ntg[s][j]);
+                    any |= T::fhit(x[s], tg[s][j]);
                 }
             }
         }
@@ -223,7 +289,7 @@ __device__ __forceinline__ void walk_streams(const typename T::M (&m)[NC], typen
                 for (int s = 0; s < NC; ++s) replay_chain<T>(m[s], xs[s], mult0, a.base, k, B, a.type, act[s], h);
             }
         }
-        // back to Montgomery form (class 32: |x*K| < p^2 < p*2^31)
+        // back to Montgomery form
         if (FUSED) {
             x[0] = T::restore(m[0], x[0], K[0]);
             x[NS - 1] = T::restore(m[0], x[NS - 1], K[0]);
@@ -233,16 +299,8 @@ __device__ __forceinline__ void walk_streams(const typename T::M (&m)[NC], typen
         }
     }
 
-    // canonical form for the tail, the state store and the check kernel
-    if (FUSED) {
-        x[0] = T::canon(m[0], x[0]);
-        x[NS - 1] = T::canon(m[0], x[NS - 1]);
-    } else {
-#pragma unroll
-        for (int s = 0; s < NC; ++s) x[s] = T::canon(m[s], x[s]);
-    }
     const int r = (int)(a.hi - k);
-    if (r > 0) {  // tail of fewer than B steps
+    if (r > 0) {  // tail of fewer than B steps, same filter and replay
         W xs[NS];
 #pragma unroll
         for (int s = 0; s < NS; ++s) xs[s] = x[s];
@@ -253,15 +311,14 @@ __device__ __forceinline__ void walk_streams(const typename T::M (&m)[NC], typen
                 const uint32_t mul0 = mult0 ? __ldg(mult0 + (k - a.base) + j) : k + j;
                 if (FUSED) {
                     const uint32_t mul1 = __ldg(mult1 + (k - a.base) + j);
-                    x[0] = T::step(m[0], x[0], mul0);
-                    x[NS - 1] = T::step(m[0], x[NS - 1], mul1);
-                    any |= (x[0] == tg[0][j]) | (x[0] == ntg[0][j]) | (x[NS - 1] == tg[0][j]) |
-                           (x[NS - 1] == ntg[0][j]);
+                    x[0] = T::fstep(m[0], x[0], mul0);
+                    x[NS - 1] = T::fstep(m[0], x[NS - 1], mul1);
+                    any |= T::fhit(x[0], tg[0][j]) | T::fhit(x[NS - 1], tg[0][j]);
                 } else {
 #pragma unroll
                     for (int s = 0; s < NC; ++s) {
-                        x[s] = T::step(m[s], x[s], mul0);
-                        any |= (x[s] == tg[s][j]) | (x[s] == ntg[s][j]);
+                        x[s] = T::fstep(m[s], x[s], mul0);
+                        any |= T::fhit(x[s], tg[s][j]);
                     }
                 }
             }
@@ -277,16 +334,24 @@ __device__ __forceinline__ void walk_streams(const typename T::M (&m)[NC], typen
         }
 #pragma unroll
         for (int s = 0; s < NC; ++s) {
-            const W Kr = m[s].mont_R_pow((uint64_t)r);
+            const W Kr = T::K(m[s], r);
             if (FUSED) {
-                x[0] = m[0].mul(x[0], Kr);
-                x[NS - 1] = m[0].mul(x[NS - 1], Kr);
+                x[0] = T::restore(m[0], x[0], Kr);
+                x[NS - 1] = T::restore(m[0], x[NS - 1], Kr);
             } else {
-                x[s] = m[s].mul(x[s], Kr);
+                x[s] = T::restore(m[s], x[s], Kr);
             }
         }
     }
 
+    // canonical form for the state store and the check
+    if (FUSED) {
+        x[0] = T::canon(m[0], x[0]);
+        x[NS - 1] = T::canon(m[0], x[NS - 1]);
+    } else {
+#pragma unroll
+        for (int s = 0; s < NC; ++s) x[s] = T::canon(m[s], x[s]);
+    }
 }
 
 }  // namespace pfc
