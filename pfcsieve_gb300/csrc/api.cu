@@ -31,7 +31,8 @@ struct pfc_job {
     uint64_t pmin = 0, pmax = 0;
 
     DevProg<uint32_t> a32, b32;
-    DevProg<uint64_t> a64, b64;
+    DevProg<uint64_t> a64, b64;   // class 64 at or above 2^64/3 (64-bit words)
+    DevProg<W128> aw, bw;         // class 64 below 2^64/3 (128-bit words)
     uint64_t setup_mulmods32 = 0, setup_mulmods64 = 0;
     DArr<uint32_t> primebits;
     DArr<uint32_t> qlist;
@@ -152,6 +153,8 @@ static int job_release(pfc_job *j) {
     j->b32.release(c);
     j->a64.release(c);
     j->b64.release(c);
+    j->aw.release(c);
+    j->bw.release(c);
     j->primebits.release(c);
     j->qlist.release(c);
     j->cmult.release(c);
@@ -162,6 +165,17 @@ static int job_release(pfc_job *j) {
     if (j->h_stats) cudaFreeHost(j->h_stats);
     j->h_stats = nullptr;
     return PFC_OK;
+}
+
+// the setup programs of a search for one word type: F, C, P one program (a);
+// the combined search a = (n-1)!/(n-1)#, b = the primorial words after it
+template <class W>
+static bool build_progs(unsigned mode, uint32_t startN, const std::vector<uint32_t> &primes,
+                        const std::vector<uint32_t> &below, HostProg<W> &a, HostProg<W> &b) {
+    if (mode == PFC_FACTORIAL) return build_power_prog(startN, 0, primes, a);
+    if (mode == PFC_COMPOSITORIAL) return build_power_prog(startN, 1, primes, a);
+    if (mode == PFC_PRIMORIAL) return build_product_prog(below, a);
+    return build_power_prog(startN, 1, primes, a) && build_product_prog(below, b);
 }
 
 extern "C" int pfc_job_create(pfc_ctx *c, unsigned mode, uint32_t nmin, uint32_t nmax, uint64_t pmin,
@@ -190,26 +204,24 @@ extern "C" int pfc_job_create(pfc_ctx *c, unsigned mode, uint32_t nmin, uint32_t
     const std::vector<uint32_t> below(primes.begin(), std::upper_bound(primes.begin(), primes.end(), startN));
     HostProg<uint32_t> a32, b32;
     HostProg<uint64_t> a64, b64;
-    bool ok = true;
-    if (mode == PFC_FACTORIAL) {
-        ok = build_power_prog(startN, 0, primes, a32) && build_power_prog(startN, 0, primes, a64);
-    } else if (mode == PFC_COMPOSITORIAL) {
-        ok = build_power_prog(startN, 1, primes, a32) && build_power_prog(startN, 1, primes, a64);
-    } else if (mode == PFC_PRIMORIAL) {
-        ok = build_product_prog(below, a32) && build_product_prog(below, a64);
-    } else {
-        ok = build_power_prog(startN, 1, primes, a32) && build_power_prog(startN, 1, primes, a64) &&
-             build_product_prog(below, b32) && build_product_prog(below, b64);
-    }
+    HostProg<W128> aw, bw;
+    const bool need32 = pmin < kClassSplit;
+    const bool needw = pmax > kClassSplit && pmin < kLazyEnd;
+    const bool need64 = pmax > kLazyEnd;
+    bool ok = (!need32 || build_progs(mode, startN, primes, below, a32, b32)) &&
+              (!needw || build_progs(mode, startN, primes, below, aw, bw)) &&
+              (!need64 || build_progs(mode, startN, primes, below, a64, b64));
     if (!ok) {
         delete j;
         return PFC_ERR_ARG;
     }
     j->setup_mulmods32 = a32.mulmods() + b32.mulmods();
-    j->setup_mulmods64 = a64.mulmods() + b64.mulmods();
+    j->setup_mulmods64 = need64 ? a64.mulmods() + b64.mulmods() : aw.mulmods() + bw.mulmods();
 
     cudaError_t e = j->a32.upload(c, a32);
     if (e == cudaSuccess) e = j->a64.upload(c, a64);
+    if (e == cudaSuccess) e = j->aw.upload(c, aw);
+    if (e == cudaSuccess) e = j->bw.upload(c, bw);
     if (e == cudaSuccess) e = j->b32.upload(c, b32);
     if (e == cudaSuccess) e = j->b64.upload(c, b64);
     if (e == cudaSuccess && (mode & PFC_COMPOSITORIAL)) e = j->primebits.upload(c, prime_bitmap(nmin, nmax, primes));
@@ -315,8 +327,16 @@ static int enqueue_setup(pfc_job *j) {
     s64.a = j->a64.view;
     s64.b = j->b64.view;
     s64.nnext0 = 0;
+    SetupArgs<W128> sw;
+    sw.mode = j->mode;
+    sw.a = j->aw.view;
+    sw.b = j->bw.view;
+    sw.nnext0 = 0;
     if (j->use32) c->launches += launch_setup32(j->c32.view(counts_ptr(j)), s32, c->st);
-    if (j->use64) c->launches += launch_setup64(j->c64.view(counts_ptr(j) + 1), s64, c->st);
+    if (j->use64) {
+        if (j->seg_hi <= kLazyEnd) c->launches += launch_setup64w(j->c64.view(counts_ptr(j) + 1), sw, c->st);
+        else c->launches += launch_setup64(j->c64.view(counts_ptr(j) + 1), s64, c->st);
+    }
     CK(cudaGetLastError());
     j->stage = 2;
     j->next_it = iter_begin(j);
@@ -346,7 +366,7 @@ static int enqueue_iter_range(pfc_job *j, uint32_t lo, uint32_t hi) {
     const HitBuf h = hitbuf(j);
     auto walk = [&](const WalkArgs &w) {
         if (j->use32) c->launches += launch_walk32(j->c32.view(counts_ptr(j)), w, h, c->st);
-        if (j->use64) c->launches += launch_walk64(j->c64.view(counts_ptr(j) + 1), w, h, c->st, j->seg_hi <= (1ull << 63));
+        if (j->use64) c->launches += launch_walk64(j->c64.view(counts_ptr(j) + 1), w, h, c->st, j->seg_hi <= kLazyWalkEnd);
     };
     WalkArgs w;
     w.lo = lo;

@@ -4,9 +4,10 @@
 //   class 32: p < 2^31, Montgomery with R = 2^32: one 32x32->64 multiply
 //             (IMAD.WIDE) plus an IMAD and an IMAD.HI per multiplication;
 //             walk residues are signed, in (-p, p) (redc31s).
-//   class 64: p >= 2^31, Montgomery with R = 2^64; walks with p < 2^63 use
-//             lazy one-word steps with R = 2^32 and residues in [0, 2p)
-//             (redc64l).
+//   class 64: p >= 2^31, Montgomery with R = 2^64; below 2^64/3 the walk
+//             takes lazy one-word steps with R = 2^32 and residues in
+//             [0, 2p) (redc64l), and the setup multiplies by 128-bit table
+//             words in four lazy rounds (mul_word128).
 //
 // The reference keeps every residue in Montgomery form with R = 2^64
 // (kernels/iterate.cl:44-50: m_mul(a,b) = a*b/2^64 mod p in [0,p)).  Values
@@ -155,6 +156,55 @@ __device__ __forceinline__ uint64_t redc64l(uint64_t x, uint32_t n, uint64_t p, 
         : "=l"(r)
         : "l"(x), "r"(n), "l"(p), "r"(q));
     return r;
+}
+
+// One lazy Montgomery round with an accumulator, for multiplying by a
+// multi-limb word (p < 2^64/3, s < 2p, c < 3p, any 32-bit limb w):
+//   c' = (c + s*w + m*p) / 2^32,  m = lo(c + s*w) * (-p^-1) mod 2^32,
+// c' < (3p + 2p*2^32 + 2^32 p) / 2^32 < 3p + 1, so c' < 3p again.
+__device__ __forceinline__ uint64_t cios_round(uint64_t c, uint64_t s, uint32_t w, uint64_t p, uint32_t q) {
+    uint64_t r;
+    asm("{\n\t"
+        ".reg .u32 s0, s1, c0, c1, a0, a1, b0, b1, m, h, d0, d1, p0, p1, z;\n\t"
+        ".reg .u64 A, Bv, D, C1;\n\t"
+        "mov.b64 {s0, s1}, %1;\n\t"
+        "mov.b64 {c0, c1}, %2;\n\t"
+        "mov.b64 {p0, p1}, %4;\n\t"
+        "cvt.u64.u32 A, c0;\n\t"
+        "mad.wide.u32 A, s0, %3, A;\n\t"
+        "mov.b64 {a0, a1}, A;\n\t"
+        "cvt.u64.u32 Bv, a1;\n\t"
+        "mad.wide.u32 Bv, s1, %3, Bv;\n\t"
+        "cvt.u64.u32 C1, c1;\n\t"
+        "add.u64 Bv, Bv, C1;\n\t"
+        "mul.lo.u32 m, a0, %5;\n\t"
+        "mul.hi.u32 h, m, p0;\n\t"
+        "cvt.u64.u32 D, h;\n\t"
+        "mad.wide.u32 D, m, p1, D;\n\t"
+        "mov.b64 {b0, b1}, Bv;\n\t"
+        "mov.b64 {d0, d1}, D;\n\t"
+        "add.cc.u32 z, a0, 0xffffffff;\n\t"
+        "addc.cc.u32 b0, b0, d0;\n\t"
+        "addc.u32 b1, b1, d1;\n\t"
+        "mov.b64 %0, {b0, b1};\n\t"
+        "}"
+        : "=l"(r)
+        : "l"(s), "l"(c), "r"(w), "l"(p), "r"(q));
+    return r;
+}
+
+// s*W*2^-128 (mod p) for a 128-bit word W given as four 32-bit limbs
+// (little-endian), s in [0, 2p), p < 2^64/3: one plain lazy round (c = 0)
+// and three accumulating rounds, then one conditional subtraction: result in
+// [0, 2p).  Two multiplications by 64-bit words would cost about twice the
+// multiply-pipe time for the same number of factor bits.
+__device__ __forceinline__ uint64_t mul_word128(uint64_t s, uint32_t w0, uint32_t w1, uint32_t w2, uint32_t w3,
+                                                uint64_t p, uint32_t q) {
+    uint64_t c = redc64l(s, w0, p, q);
+    c = cios_round(c, s, w1, p, q);
+    c = cios_round(c, s, w2, p, q);
+    c = cios_round(c, s, w3, p, q);
+    return c >= 2 * p ? c - p : c;
 }
 
 struct Mont64 {

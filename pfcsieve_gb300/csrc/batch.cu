@@ -52,7 +52,7 @@ struct JobDev {
     uint32_t nsetup, nwalk;   // timeline: [0, nsetup) setup positions, then nwalk walk steps
     const SetupSeg *segs;     // runs of the setup timeline
     uint32_t nsegs;
-    const W *words;           // table words of the setup programs
+    const void *words;        // table words of the setup programs (the class's setup word type)
     uint64_t corr_a, corr_b;  // drift corrections (first program; second of the combined search)
     const uint32_t *cmult;    // compositorial multipliers of [nmin, nmax)
     const uint32_t *qlist;    // primorial: primes in [nmin, nmax)
@@ -95,13 +95,14 @@ __device__ __forceinline__ void run_setup(const typename T::M (&m)[NC], typename
         if (g.y == 0) {
             for (uint32_t k = 0; k < cnt; ++k) {
 #pragma unroll
-                for (int c = 0; c < NC; ++c) acc[c] = m[c].mul(acc[c], acc[c]);
+                for (int c = 0; c < NC; ++c) acc[c] = T::sq(m[c], acc[c]);
             }
         } else if (g.y == 1) {
-            const W *wp = J.words + g.z + off;
+            using SW = typename T::SW;
+            const SW *wp = static_cast<const SW *>(J.words) + g.z + off;
             uint32_t k = 0;
             for (; k + 4 <= cnt; k += 4) {
-                const W w0 = __ldg(wp + k), w1 = __ldg(wp + k + 1), w2 = __ldg(wp + k + 2), w3 = __ldg(wp + k + 3);
+                const SW w0 = ldg(wp + k), w1 = ldg(wp + k + 1), w2 = ldg(wp + k + 2), w3 = ldg(wp + k + 3);
 #pragma unroll
                 for (int c = 0; c < NC; ++c) {
                     acc[c] = T::word(m[c], acc[c], w0);
@@ -111,7 +112,7 @@ __device__ __forceinline__ void run_setup(const typename T::M (&m)[NC], typename
                 }
             }
             for (; k < cnt; ++k) {
-                const W w = __ldg(wp + k);
+                const SW w = ldg(wp + k);
 #pragma unroll
                 for (int c = 0; c < NC; ++c) acc[c] = T::word(m[c], acc[c], w);
             }
@@ -293,7 +294,8 @@ struct BatchJob {
     // host tables, built by prepare_job
     int prep_rc = PFC_OK;
     std::vector<uint32_t> words32, cmult, qlist;
-    std::vector<uint64_t> words64;
+    std::vector<uint64_t> words64;   // class 64 at or above 2^64/3
+    std::vector<W128> words128;      // class 64 below 2^64/3
     std::vector<SetupSeg> segs32, segs64;
     uint32_t nsetup32 = 0, nsetup64 = 0;
     uint64_t c32a = 0, c32b = 0, c64a = 0, c64b = 0;
@@ -303,6 +305,7 @@ struct BatchJob {
     // device
     DArr<uint32_t> d_words32, d_cmult, d_qlist;
     DArr<uint64_t> d_words64;
+    DArr<W128> d_words128;
     DArr<SetupSeg> d_segs32, d_segs64;
     DevClass<uint32_t> c32;
     DevClass<uint64_t> c64;
@@ -346,6 +349,16 @@ static uint32_t append_prog(const HostProg<W> &h, uint32_t pos, std::vector<Setu
     return pos;
 }
 
+// the setup programs of a search for one word type (as pfc_job_create)
+template <class W>
+static bool build_progs(unsigned mode, uint32_t startN, const std::vector<uint32_t> &primes,
+                        const std::vector<uint32_t> &below, HostProg<W> &a, HostProg<W> &b) {
+    if (mode == PFC_FACTORIAL) return build_power_prog(startN, 0, primes, a);
+    if (mode == PFC_COMPOSITORIAL) return build_power_prog(startN, 1, primes, a);
+    if (mode == PFC_PRIMORIAL) return build_product_prog(below, a);
+    return build_power_prog(startN, 1, primes, a) && build_product_prog(below, b);
+}
+
 static uint32_t prime_limit(const BatchJob *j) {
     const uint32_t startN = j->nmin - 1;
     return (j->mode & PFC_COMPOSITORIAL) ? j->nmax : std::max(startN, j->nmax - 1);
@@ -357,32 +370,32 @@ static void prepare_job(BatchJob *j, const std::vector<uint32_t> &cache) {
     const uint32_t startN = j->nmin - 1;
     const std::vector<uint32_t> primes(cache.begin(), std::upper_bound(cache.begin(), cache.end(), prime_limit(j)));
     const std::vector<uint32_t> below(primes.begin(), std::upper_bound(primes.begin(), primes.end(), startN));
+    const unsigned mode = j->mode;
+    const bool fc = mode == (PFC_FACTORIAL | PFC_COMPOSITORIAL);
+    const bool wide = j->pmax <= kLazyEnd;  // class 64 with 128-bit words
     HostProg<uint32_t> a32, b32;
     HostProg<uint64_t> a64, b64;
-    bool ok;
-    const unsigned mode = j->mode;
-    if (mode == PFC_FACTORIAL) ok = build_power_prog(startN, 0, primes, a32) && build_power_prog(startN, 0, primes, a64);
-    else if (mode == PFC_COMPOSITORIAL) ok = build_power_prog(startN, 1, primes, a32) && build_power_prog(startN, 1, primes, a64);
-    else if (mode == PFC_PRIMORIAL) ok = build_product_prog(below, a32) && build_product_prog(below, a64);
-    else
-        ok = build_power_prog(startN, 1, primes, a32) && build_power_prog(startN, 1, primes, a64) &&
-             build_product_prog(below, b32) && build_product_prog(below, b64);
+    HostProg<W128> aw, bw;
+    const bool ok = build_progs(mode, startN, primes, below, a32, b32) &&
+                    (wide ? build_progs(mode, startN, primes, below, aw, bw)
+                          : build_progs(mode, startN, primes, below, a64, b64));
     if (!ok) {
         j->prep_rc = PFC_ERR_ARG;
         return;
     }
     j->nsetup32 = append_prog(a32, 0, j->segs32, j->words32);
-    j->nsetup64 = append_prog(a64, 0, j->segs64, j->words64);
+    j->nsetup64 = wide ? append_prog(aw, 0, j->segs64, j->words128) : append_prog(a64, 0, j->segs64, j->words64);
     j->c32a = a32.corr;
-    j->c64a = a64.corr;
-    if (mode == (PFC_FACTORIAL | PFC_COMPOSITORIAL)) {
+    j->c64a = wide ? aw.corr : a64.corr;
+    if (fc) {
         // fork: the compositorial residue is complete here
         j->segs32.push_back({j->nsetup32++, 2u, 0u, 1u});
         j->segs64.push_back({j->nsetup64++, 2u, 0u, 1u});
         j->nsetup32 = append_prog(b32, j->nsetup32, j->segs32, j->words32);
-        j->nsetup64 = append_prog(b64, j->nsetup64, j->segs64, j->words64);
+        j->nsetup64 = wide ? append_prog(bw, j->nsetup64, j->segs64, j->words128)
+                           : append_prog(b64, j->nsetup64, j->segs64, j->words64);
         j->c32b = b32.corr;
-        j->c64b = b64.corr;
+        j->c64b = wide ? bw.corr : b64.corr;
     }
     if (mode & PFC_COMPOSITORIAL) {
         // n at composite n, 1 at prime n (iterate.cl:137-140, 181-184), padded for vector loads
@@ -484,6 +497,7 @@ void release_device(pfc_batch *b, BatchJob *j) {
     pfc_ctx *c = b->ctx;
     j->d_words32.release(c);
     j->d_words64.release(c);
+    j->d_words128.release(c);
     j->d_segs32.release(c);
     j->d_segs64.release(c);
     j->d_cmult.release(c);
@@ -521,6 +535,7 @@ int upload_job(pfc_batch *b, BatchJob *j) {
     pfc_ctx *c = b->ctx;
     cudaError_t e = j->d_words32.upload(c, j->words32);
     if (e == cudaSuccess) e = j->d_words64.upload(c, j->words64);
+    if (e == cudaSuccess) e = j->d_words128.upload(c, j->words128);
     if (e == cudaSuccess) e = j->d_segs32.upload(c, j->segs32);
     if (e == cudaSuccess) e = j->d_segs64.upload(c, j->segs64);
     if (e == cudaSuccess) e = j->d_cmult.upload(c, j->cmult);
@@ -535,7 +550,7 @@ int upload_job(pfc_batch *b, BatchJob *j) {
 }
 
 template <class W>
-JobDev<W> job_view(pfc_batch *b, BatchJob *j, const DevClass<W> &cls, int which, const DArr<W> &words,
+JobDev<W> job_view(pfc_batch *b, BatchJob *j, const DevClass<W> &cls, int which, const void *words,
                    const DArr<SetupSeg> &segs, size_t nsegs, uint64_t ca, uint64_t cb, uint32_t nsetup) {
     JobDev<W> d;
     memset(&d, 0, sizeof(d));
@@ -546,7 +561,7 @@ JobDev<W> job_view(pfc_batch *b, BatchJob *j, const DevClass<W> &cls, int which,
     d.nwalk = j->nwalk;
     d.segs = segs.p;
     d.nsegs = (uint32_t)nsegs;
-    d.words = words.p;
+    d.words = words;
     d.corr_a = ca;
     d.corr_b = cb;
     d.cmult = j->d_cmult.p;
@@ -617,9 +632,10 @@ int admit_prepared(pfc_batch *b) {
         const uint32_t per64 = 256u * Cls64::NC;
         for (uint32_t k = 0; k < n32; k += per32) j->b32.push_back({k, std::min(per32, n32 - k), 0});
         for (uint32_t k = 0; k < n64; k += per64) j->b64.push_back({k, std::min(per64, n64 - k), 0});
-        v32[f] = job_view<uint32_t>(b, j, j->c32, 0, j->d_words32, j->d_segs32, j->segs32.size(), j->c32a, j->c32b,
-                                    j->nsetup32);
-        v64[f] = job_view<uint64_t>(b, j, j->c64, 1, j->d_words64, j->d_segs64, j->segs64.size(), j->c64a, j->c64b,
+        v32[f] = job_view<uint32_t>(b, j, j->c32, 0, j->d_words32.p, j->d_segs32, j->segs32.size(), j->c32a,
+                                    j->c32b, j->nsetup32);
+        const void *w64 = j->pmax <= kLazyEnd ? (const void *)j->d_words128.p : (const void *)j->d_words64.p;
+        v64[f] = job_view<uint64_t>(b, j, j->c64, 1, w64, j->d_segs64, j->segs64.size(), j->c64a, j->c64b,
                                     j->nsetup64);
         CK(cudaMemcpyAsync(b->jobs32.p + j->slot, &v32[f], sizeof(v32[f]), cudaMemcpyHostToDevice, c->st));
         CK(cudaMemcpyAsync(b->jobs64.p + j->slot, &v64[f], sizeof(v64[f]), cudaMemcpyHostToDevice, c->st));
@@ -629,6 +645,7 @@ int admit_prepared(pfc_batch *b) {
     for (BatchJob *j : fresh) {
         free_vec(j->words32);  // on the device now
         free_vec(j->words64);
+        free_vec(j->words128);
         free_vec(j->segs32);
         free_vec(j->segs64);
         free_vec(j->cmult);
@@ -657,7 +674,7 @@ uint32_t build_tasks(pfc_batch *b) {
     // longest first: windows with setup work, full walk windows, short ends
     std::vector<Task> part[3][3];  // [list][kind]
     for (BatchJob *j : b->running) {
-        const int l64 = j->pmax <= kLazyLimit ? 1 : 2;
+        const int l64 = j->pmax <= kLazyEnd ? 1 : 2;
         for (int cls = 0; cls < 2; ++cls) {
             const std::vector<Block> &blocks = cls ? j->b64 : j->b32;
             const uint32_t tot = cls ? j->tot64 : j->tot32, ns = cls ? j->nsetup64 : j->nsetup32;

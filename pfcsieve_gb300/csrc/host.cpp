@@ -83,13 +83,26 @@ uint64_t HostProg<W>::mulmods() const {
 }
 
 template <class W>
+static inline u128 word_max() { return (u128)(W)~(W)0; }
+template <>
+inline u128 word_max<W128>() { return ~(u128)0; }
+template <class W>
+static inline W to_word(u128 v) { return (W)v; }
+template <>
+inline W128 to_word<W128>(u128 v) { return W128{(uint64_t)v, (uint64_t)(v >> 64)}; }
+// R = 2^64 powers a word removes (R = 2^32 for the class-32 words)
+template <class W>
+static constexpr int word_drift() { return sizeof(W) == 16 ? 2 : 1; }
+
+// greedy: consecutive factors multiplied while the product fits a word
+template <class W>
 static void pack_words(const std::vector<uint32_t> &f, std::vector<W> &words) {
-    const u128 lim = (u128)(W)~(W)0;
+    const u128 lim = word_max<W>();
     size_t i = 0;
     while (i < f.size()) {
         u128 acc = f[i++];
-        while (i < f.size() && acc * f[i] <= lim) acc *= f[i++];
-        words.push_back((W)acc);
+        while (i < f.size() && acc <= lim / f[i]) acc *= f[i++];
+        words.push_back(to_word<W>(acc));
     }
 }
 
@@ -106,7 +119,7 @@ static bool finish_prog(HostProg<W> &p) {
             d = 2 * d - 1;
             if (-d > lim) return false;
         }
-        d -= (__int128)(p.groups[g + 1] - p.groups[g]);
+        d -= (__int128)word_drift<W>() * (p.groups[g + 1] - p.groups[g]);
     }
     for (uint32_t k = 0; k < p.final_sq; ++k) {
         d = 2 * d - 1;
@@ -162,10 +175,13 @@ bool build_product_prog(const std::vector<uint32_t> &factors, HostProg<W> &out) 
 
 template struct HostProg<uint32_t>;
 template struct HostProg<uint64_t>;
+template struct HostProg<W128>;
 template bool build_power_prog<uint32_t>(uint32_t, uint32_t, const std::vector<uint32_t> &, HostProg<uint32_t> &);
 template bool build_power_prog<uint64_t>(uint32_t, uint32_t, const std::vector<uint32_t> &, HostProg<uint64_t> &);
+template bool build_power_prog<W128>(uint32_t, uint32_t, const std::vector<uint32_t> &, HostProg<W128> &);
 template bool build_product_prog<uint32_t>(const std::vector<uint32_t> &, HostProg<uint32_t> &);
 template bool build_product_prog<uint64_t>(const std::vector<uint32_t> &, HostProg<uint64_t> &);
+template bool build_product_prog<W128>(const std::vector<uint32_t> &, HostProg<W128> &);
 
 // ------------------------------------------------------- host Montgomery
 

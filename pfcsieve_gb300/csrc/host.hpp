@@ -6,13 +6,21 @@
 
 namespace pfc {
 
+// 128-bit setup table word (class 64 below 2^64/3): little-endian, read on the
+// device as four 32-bit limbs
+struct alignas(16) W128 {
+    uint64_t lo, hi;
+};
+
 // primes p with lo <= p <= hi (segmented odd-only sieve; replaces the
 // primesieve_generate_primes calls of cl_sieve.cpp:850,996,1000,1158,1472,
 // 1476,1498)
 std::vector<uint32_t> primes_between(uint32_t lo, uint32_t hi);
 
 // Setup program on the host: words, groups {begin, end, squarings}, final
-// squarings and the drift correction exponent (see kernels.cuh Prog).
+// squarings and the drift correction exponent (see kernels.cuh Prog).  Each
+// 32- or 64-bit word lowers the power of R of the device value by one, each
+// 128-bit word by two.
 template <class W>
 struct HostProg {
     std::vector<W> words;

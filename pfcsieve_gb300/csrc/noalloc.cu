@@ -287,7 +287,7 @@ extern "C" int pfc_segment_noalloc(unsigned mode, uint32_t nmin, uint32_t nmax, 
             }
         }
         if (use32) launch_walk32(c32, w, h, st);
-        if (use64) launch_walk64(c64, w, h, st, p_hi <= (1ull << 63));
+        if (use64) launch_walk64(c64, w, h, st, p_hi <= kLazyWalkEnd);
         a = b;
     }
 

@@ -12,7 +12,7 @@ namespace pfc {
 // --------------------------------------------------------------------- setup
 
 template <class T>
-__global__ void __launch_bounds__(256) setup_kernel(ClassBuf<typename T::W> c, SetupArgs<typename T::W> a) {
+__global__ void __launch_bounds__(256) setup_kernel(ClassBuf<typename T::W> c, SetupArgs<typename T::SW> a) {
     using W = typename T::W;
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     const uint32_t cnt = min(*c.count, c.cap);
@@ -131,6 +131,11 @@ int launch_setup32(const ClassBuf<uint32_t> &c, const SetupArgs<uint32_t> &a, cu
 int launch_setup64(const ClassBuf<uint64_t> &c, const SetupArgs<uint64_t> &a, cudaStream_t st) {
     if (!c.cap) return 0;
     setup_kernel<Cls64><<<grid_for(c.cap), 256, 0, st>>>(c, a);
+    return 1;
+}
+int launch_setup64w(const ClassBuf<uint64_t> &c, const SetupArgs<W128> &a, cudaStream_t st) {
+    if (!c.cap) return 0;
+    setup_kernel<Cls64L><<<grid_for(c.cap), 256, 0, st>>>(c, a);
     return 1;
 }
 

@@ -64,7 +64,10 @@ struct Cls32 {
     __device__ static __forceinline__ W restore(const M &m, W x, W K) { return fstep(m, x, K); }
     __device__ static __forceinline__ W canon(const M &m, W x) { return (int32_t)x < 0 ? x + m.p : x; }
     __device__ static __forceinline__ W step(const M &m, W s, uint32_t n) { return redc32(s, n, m.p, m.pinv); }
-    __device__ static __forceinline__ W word(const M &m, W s, W w) { return redc32(s, w, m.p, m.pinv); }
+    // setup: table words of the class (SW) and squarings
+    using SW = uint32_t;
+    __device__ static __forceinline__ W word(const M &m, W s, SW w) { return redc32(s, w, m.p, m.pinv); }
+    __device__ static __forceinline__ W sq(const M &m, W s) { return m.mul(s, s); }
     // checksum form: residue * 2^64 mod p from its class-32 Montgomery form
     __device__ static __forceinline__ uint64_t term(const M &m, W s) { return m.mul(s, m.r2); }
     __device__ static __forceinline__ uint64_t mont64_of(const M &m, uint32_t v) { return m.mul(m.mul(v, m.r2), m.r2); }
@@ -89,12 +92,14 @@ struct Cls64 {
     __device__ static __forceinline__ W restore(const M &m, W x, W K) { return m.mul(x, K); }
     __device__ static __forceinline__ W canon(const M &, W x) { return x; }
     __device__ static __forceinline__ W step(const M &m, W s, uint32_t n) { return redc64_u32(s, n, m.p, m.pinv); }
-    __device__ static __forceinline__ W word(const M &m, W s, W w) { return redc64(s, w, m.p, m.pinv); }
+    using SW = uint64_t;
+    __device__ static __forceinline__ W word(const M &m, W s, SW w) { return redc64(s, w, m.p, m.pinv); }
+    __device__ static __forceinline__ W sq(const M &m, W s) { return m.mul(s, s); }
     __device__ static __forceinline__ uint64_t term(const M &, W s) { return s; }
     __device__ static __forceinline__ uint64_t mont64_of(const M &m, uint32_t v) { return m.to_mont(v); }
 };
 
-// 2^31 < p < 2^63: the walk takes lazy one-word steps (R' = 2^32, residues in
+// 2^31 < p < 2^64/3: the walk takes lazy one-word steps (R' = 2^32, residues in
 // [0, 2p), redc64l) from the R = 2^64 setup values.  After j+1 steps from
 // r*2^64, x = r' * 2^64 * 2^(-32(j+1)) (mod p), so the targets are
 // U_j = 2^(32-32j) mod p; x = +-U (mod p) with x in [0, 2p) means x is one of
@@ -129,24 +134,35 @@ struct Cls64L {
     // x < 2p and K < p with p < 2^63 keep x*K < p*2^64: canonical result
     __device__ static __forceinline__ W restore(const M &m, W x, W K) { return m.mul(x, K); }
     __device__ static __forceinline__ W step(const M &m, W s, uint32_t n) { return canon(m, redc64l(s, n, m.p, m.q32)); }
-    __device__ static __forceinline__ W word(const M &m, W s, W w) { return redc64(s, w, m.p, m.pinv); }
+    // setup (p < 2^64/3): 128-bit table words, each lowering the power of
+    // R = 2^64 by two; values stay in [0, 2p), canonical before a squaring
+    using SW = W128;
+    __device__ static __forceinline__ W word(const M &m, W s, const SW &w) {
+        return mul_word128(s, (uint32_t)w.lo, (uint32_t)(w.lo >> 32), (uint32_t)w.hi, (uint32_t)(w.hi >> 32), m.p,
+                           m.q32);
+    }
+    __device__ static __forceinline__ W sq(const M &m, W s) {
+        s = canon(m, s);
+        return m.mul(s, s);
+    }
     __device__ static __forceinline__ uint64_t term(const M &, W s) { return s; }
     __device__ static __forceinline__ uint64_t mont64_of(const M &m, uint32_t v) { return m.to_mont(v); }
 };
 
-// largest p a class-64 segment may hold for the lazy walk
-constexpr uint64_t kLazyLimit = 1ull << 63;
-
 template <class W>
 __device__ __forceinline__ W ldg(const W *p) { return __ldg(p); }
+__device__ __forceinline__ W128 ldg(const W128 *p) {
+    const uint4 v = __ldg(reinterpret_cast<const uint4 *>(p));
+    return W128{(uint64_t)v.x | ((uint64_t)v.y << 32), (uint64_t)v.z | ((uint64_t)v.w << 32)};
+}
 
 // Evaluate a setup program from Montgomery-form `acc` (see kernels.cuh Prog).
 template <class T>
-__device__ typename T::W run_prog(const typename T::M &m, const Prog<typename T::W> &pg, typename T::W acc) {
+__device__ typename T::W run_prog(const typename T::M &m, const Prog<typename T::SW> &pg, typename T::W acc) {
     for (uint32_t g = 0; g < pg.ngroups; ++g) {
         const uint32_t b = __ldg(pg.groups + 3 * g), e = __ldg(pg.groups + 3 * g + 1);
         const uint32_t sq = __ldg(pg.groups + 3 * g + 2);
-        for (uint32_t k = 0; k < sq; ++k) acc = m.mul(acc, acc);
+        for (uint32_t k = 0; k < sq; ++k) acc = T::sq(m, acc);
         uint32_t i = b;
         for (; i + 4 <= e; i += 4) {
             acc = T::word(m, acc, ldg(pg.words + i));
@@ -156,7 +172,7 @@ __device__ typename T::W run_prog(const typename T::M &m, const Prog<typename T:
         }
         for (; i < e; ++i) acc = T::word(m, acc, ldg(pg.words + i));
     }
-    for (uint32_t k = 0; k < pg.final_sq; ++k) acc = m.mul(acc, acc);
+    for (uint32_t k = 0; k < pg.final_sq; ++k) acc = T::sq(m, acc);
     return m.mul(acc, m.mont_R_pow(pg.corr));
 }
 

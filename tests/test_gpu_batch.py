@@ -31,6 +31,11 @@ MIX = [
     (4, 101, 102, 10**6, 2 * 10**6),
     (2, 114, 126, 10**7, 10**7 + 10**6),
     (1, 500, 500, 10**6, 10**6 + 10**5),
+    # class-64 regimes: below, across and above 2^64/3, across 2^63
+    (5, 2000, 6000, 0x5555555555555556 - 200000, 0x5555555555555556),
+    (2, 2000, 30000, 0x5555555555555556 - 100000, 0x5555555555555556 + 100000),
+    (4, 2000, 6000, 2**63 - 100000, 2**63 + 100000),
+    (1, 2000, 6000, 2**64 - 200000, 2**64 - 1),
 ]
 
 

@@ -104,6 +104,28 @@ def test_random_segments_vs_oracle(ctx, seed):
     assert termsum == osum
 
 
+# class-64 arithmetic regimes: 128-bit setup words and lazy walk below
+# 2^64/3, 64-bit setup words with the lazy walk up to 2^63, canonical above
+LAZY_END = 0x5555555555555556
+
+
+@pytest.mark.parametrize("lo", [LAZY_END - 120000, LAZY_END - 60000, 2**63 - 60000, 2**63 - 120000,
+                                2**64 - 200000, 2**33])
+@pytest.mark.parametrize("mode", [1, 2, 4, 5])
+def test_class64_regimes_vs_oracle(ctx, mode, lo):
+    nmin, nmax = 3000, 7000
+    hi = min(lo + 120000, 2**64 - 1)
+    p, s0, s1, hits, termsum, _ = run_segment(ctx, mode, nmin, nmax, lo, hi)
+    cands = o.candidates(lo, hi)
+    assert np.array_equal(p, cands)
+    ohits, osum, terms = o.sieve(mode, nmin, nmax, cands, THREADS, want_terms=True)
+    assert np.array_equal(s0, terms[:, 0])
+    if mode == 5:
+        assert np.array_equal(s1, terms[:, 2])
+    assert np.array_equal(hits, ohits)
+    assert termsum == osum
+
+
 def test_wilson_and_small_p(ctx):
     """p <= n: residues fall to 0 and (p-1)!+1 hits are real (self-test 3/6/10/14)."""
     for mode in (1, 2, 4, 5):
