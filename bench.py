@@ -18,10 +18,23 @@ region).  `e2e` is the same metric through pfcsieve_gb300.sieve(), the call a
 user makes: table build and upload, all segments, hit drain, CPU
 re-verification of every hit, 2-PRP filter and checksum, timed on the host.
 
-The roofline object covers the iterate kernel (the dominant one): achieved =
-algorithmic 32-bit multiply operations (4 per class-32 Montgomery
-multiplication, 16 per class-64 one) / kernel time; peak = 32-bit IMAD
-throughput measured in this run by pfc_bench_int_peak.
+The roofline object covers the iterate (walk) kernel, the dominant one.  The
+walk is bound by the integer multiply pipe: each step of a residue chain needs
+a fixed set of multiplies (class 32: one 32x32->64 multiply-add, one
+multiply-low, one multiply-high; class 64 below 2^64/3: three multiply-adds,
+one multiply-low, one multiply-high).  Each kind's throughput is measured in
+this run (pfc_bench_int_peak); `achieved` is the walk's steps per second x the
+IMAD-equivalent cost of a step (each multiply weighted by IMAD rate / its own
+rate), `peak` is the IMAD rate, so `frac` is the fraction of time the multiply
+pipe would be busy with the algorithm's own multiplies.
+
+Unless --no-mixed, the line also carries `batched`: a sample of the mixed
+workload (searches drawn by pfcsieve_gb300.serving.mixed_jobs, seed 0) run as
+one batch (pfc_batch_*) and one search at a time (pfc_job_run), with every
+search's totals and hits compared between the two, and the same searches
+served by the request loop with Poisson arrivals (200 per second, seed 1):
+p50 and p99 latency from arrival to result, against the same arrivals served
+one at a time.  --workload mixed makes that comparison the headline line.
 
 --impl reference times the reference algorithm's CPU form (the oracle port of
 the reference kernels, OpenMP over all host threads) on a bounded sample of
@@ -53,6 +66,10 @@ WORKLOADS = {
                       desc="-! n=[101,20000) p=[1e7,1.1e7)"),
     "primorial": dict(mode=2, nmin=101, nmax=10**6, pmin=2**62, pmax=2**62 + 5 * 10**7,
                       desc="-# n=[101,1e6) p=[2^62,2^62+5e7)"),
+    # batches of uneven searches (pfcsieve_gb300.serving.mixed_jobs)
+    "mixed": dict(mode=0, nmin=0, nmax=0, pmin=0, pmax=0,
+                  desc="mixed searches: modes !,#,c; n-range log-uniform [1e3,1e6] from n0 in [101,1e7); "
+                       "p-range log-uniform [1e5,1e8] from p0 log-uniform [1e8,2^63]; seed 0"),
     # reduced case of the combined search for ncu captures (same kernels)
     "combined-small": dict(mode=5, nmin=101, nmax=20000, pmin=10**9, pmax=10**9 + 10**7,
                            desc="-! -c n=[101,20000) p=[1e9,1.01e9)"),
@@ -70,6 +87,9 @@ def parse():
     ap.add_argument("--cpu-sample", type=int, default=0,
                     help="candidates in the CPU baseline sample (0 = auto)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-mixed", action="store_true", help="skip the batched-vs-plain comparison")
+    ap.add_argument("--mixed-jobs", type=int, default=32,
+                    help="searches of the mixed workload sample (the full set is 512)")
     return ap.parse_args()
 
 
@@ -246,6 +266,98 @@ def n_composites(nmin, nmax):
     return int(len(seg) - seg.sum()), int(seg.sum())
 
 
+def step_recipe(cls32, lazy):
+    """Multiplies of one walk step (see arith.cuh): redc31s, redc64l, redc64_u32."""
+    if cls32:
+        return {"imad_wide": 1, "imad": 1, "mul_hi": 1}
+    if lazy:
+        return {"imad_wide": 3, "imad": 1, "mul_hi": 1}
+    return {"imad_wide": 7, "imad": 2}
+
+
+def hit_order(f):
+    """Hits sorted by (p, |n|, type, nc), for comparing two runs."""
+    if len(f) == 0:
+        return f
+    return f[np.lexsort((f["nc"], f["type"], np.abs(f["nc"].astype(np.int64)), f["p"]))]
+
+
+def run_mixed(ctx, njobs, warmup, steps=1):
+    """Mixed-workload sample: one batch vs one search at a time, results
+    compared search by search, then the request loop under Poisson arrivals."""
+    import pfcsieve_gb300 as pfc
+    from pfcsieve_gb300 import serving as sv
+
+    jobs = sv.mixed_jobs(512, seed=0)[:njobs]
+    sv.run_batched(ctx, jobs[:4], keep_hits=False)       # warm-up: kernels loaded, pools grown
+    runs = []
+    for _ in range(max(1, steps)):
+        runs.append(sv.run_batched(ctx, jobs))
+    out_b, t_b, timing = min(runs, key=lambda r: r[1])
+    out_p, t_p, service, create = sv.run_plain(ctx, jobs)
+    same = all((out_b[i].term_checksum, out_b[i].primecount) == (out_p[i].term_checksum, out_p[i].primecount)
+               and np.array_equal(hit_order(out_b[i].hits), hit_order(out_p[i].hits))
+               for i in range(len(jobs)))
+    # the user's result of every search: verified factors and checksum
+    t = time.perf_counter()
+    for i, s in enumerate(jobs):
+        pfc.finalize(s.mode, s.nmax, out_b[i].hits, threads=os.cpu_count() or 1)
+    t_fin = time.perf_counter() - t
+    pairs = sum(out_b[i].primecount * (s.nmax - s.nmin) for i, s in enumerate(jobs))
+    arrivals = sv.poisson_arrivals(len(jobs), 200.0, seed=1)
+    out_s, lat, makespan = sv.serve(ctx, jobs, arrivals)
+    same_s = all((out_s[i].term_checksum, out_s[i].primecount) == (out_p[i].term_checksum, out_p[i].primecount)
+                 for i in range(len(jobs)))
+    lat_p = sv.fcfs_latencies(arrivals, service)
+    return {
+        "workload": "first %d of the 512 mixed searches (seed 0)" % len(jobs),
+        "pairs": int(pairs),
+        "batched_pairs_per_s": pairs / t_b,
+        "batched_gpu_pairs_per_s": pairs / timing["gpu_s"],
+        "plain_pairs_per_s": pairs / t_p,
+        "batched_over_plain": t_p / t_b,
+        "batched_s": t_b, "plain_s": t_p, "plain_table_build_s": create, "finalize_s": t_fin,
+        "iterations": int(timing["iterations"]), "tasks": int(timing["tasks"]),
+        "identical_results": bool(same and same_s),
+        "serving": {"arrivals_per_s": 200.0, "makespan_s": makespan,
+                    "p50_s": float(np.percentile(lat, 50)), "p99_s": float(np.percentile(lat, 99)),
+                    "plain_fcfs_p50_s": float(np.percentile(lat_p, 50)),
+                    "plain_fcfs_p99_s": float(np.percentile(lat_p, 99)),
+                    "throughput_pairs_per_s": pairs / makespan},
+    }
+
+
+def run_mixed_line(args, local):
+    """--workload mixed: the batched-vs-plain comparison as the headline."""
+    import pfcsieve_gb300 as pfc
+    ctx = pfc.Context(local, budget=120 * 10**9)
+    name, sms = ctx.device_info()
+    launches0 = ctx.launches
+    h2d0, d2h0 = ctx.transfer_bytes()
+    clk = ClockSampler(local)
+    clk.start()
+    r = run_mixed(ctx, args.mixed_jobs, args.warmup, steps=args.steps)
+    clocks = clk.stop()
+    h2d1, d2h1 = ctx.transfer_bytes()
+    launches = ctx.launches - launches0
+    ctx.close()
+    steps = args.steps + 2   # batched runs, the plain run, the served run
+    line = {
+        "metric": METRIC, "value": r["batched_pairs_per_s"], "unit": UNIT, "n_gpus": 1,
+        "steps": args.steps, "warmup": 1, "ms_per_step": r["batched_s"] * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "u32/u64",
+        "data": "synthetic (seeded search bounds)",
+        "config": {"workload": WORKLOADS["mixed"]["desc"], "searches": args.mixed_jobs,
+                   "l2": "per-search state streams through L2; tables re-read per task",
+                   "parallelism": "1 GPU, batched", "device": name, "sms": sms},
+        "e2e": {"value": r["pairs"] / (r["batched_s"] + r["finalize_s"]), "unit": UNIT,
+                "h2d_bytes_per_step": (h2d1 - h2d0) // steps, "d2h_bytes_per_step": (d2h1 - d2h0) // steps},
+        "gpu_launches": int(launches), "clocks": clocks, "batched": r,
+        "roofline": None, "cpu_baseline": None,
+    }
+    print(json.dumps(line), flush=True)
+
+
 def run_ours(args, wl, world, rank, local, dist):
     import torch
 
@@ -316,13 +428,16 @@ def run_ours(args, wl, world, rank, local, dist):
     else:
         steps_per_cand = wl["nmax"] - wl["nmin"]
     cls32 = hi <= 2**31
-    ops_per_mulmod = 4 if cls32 else 16
-    alg_ops = cands_per_step * steps_per_cand * ops_per_mulmod
+    lazy = hi <= 0x5555555555555556
+    peaks = {k: pfc.int_peak(local, v) for k, v in
+             (("imad", 0), ("mul_hi", 1), ("imad_wide", 2), ("iadd_xor", 3))}
+    recipe = step_recipe(cls32, lazy)
+    imad_eq = sum(n * peaks["imad"] / peaks[k] for k, n in recipe.items())
+    walk_steps = cands_per_step * steps_per_cand
     it_s = float(np.mean(it_ms)) * 1e-3
-    peak = pfc.int_peak(local, 0)
-    peaks_all = {k: pfc.int_peak(local, v) / 1e12 for k, v in
-                 (("imad", 0), ("mul_hi", 1), ("imad_wide", 2), ("iadd_xor", 3))}
-    achieved = alg_ops / it_s
+    peak = peaks["imad"]
+    achieved = walk_steps * imad_eq / it_s
+    alg_ops = walk_steps * imad_eq
     # DRAM bytes of the walk launches of one step, from the committed ncu
     # capture of this workload (profiles/walk_kernel_traffic.json)
     traffic = None
@@ -353,6 +468,10 @@ def run_ours(args, wl, world, rank, local, dist):
                "seconds_per_step": float(np.mean(walls)),
                "factors": int(res.factorcount), "checksum": res.checksum_hex()}
 
+    batched = None
+    if rank == 0 and not args.no_mixed:
+        batched = run_mixed(ctx, args.mixed_jobs, args.warmup)
+
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         n = args.cpu_sample or auto_sample(wl)
@@ -374,18 +493,22 @@ def run_ours(args, wl, world, rank, local, dist):
                        "l2": "256 MB buffer overwritten before each step (candidate state < L2)",
                        "parallelism": "p-range shards, one per GPU" if world > 1 else "1 GPU",
                        "device": name, "sms": sms},
-            "roofline": {"bound": "int (IMAD pipe)", "achieved": achieved / 1e12, "peak": peak / 1e12,
-                         "unit": "Tops/s (32-bit integer multiply-add)", "frac": achieved / peak,
-                         "traffic": traffic,
-                         "kernel": "walk_kernel<%s>" % ("Cls32" if cls32 else "Cls64"),
+            "roofline": {"bound": "int (multiply pipe)", "achieved": achieved / 1e12, "peak": peak / 1e12,
+                         "unit": "Tops/s IMAD-equivalent (IMAD.WIDE, IMAD.HI weighted by measured rates)",
+                         "frac": achieved / peak, "traffic": traffic,
+                         "kernel": "walk_kernel<%s>" % ("Cls32" if cls32 else ("Cls64L" if lazy else "Cls64")),
+                         "walk_steps_per_step": int(walk_steps),
+                         "multiplies_per_walk_step": recipe,
+                         "imad_equivalent_per_walk_step": imad_eq,
                          "alg_ops_per_step": alg_ops,
-                         "ops_per_mulmod": ops_per_mulmod,
                          "kernel_ms_per_step": it_s * 1e3,
                          "peak_source": "measured in this run (pfc_bench_int_peak, 32-bit IMAD chains)",
-                         "int_peaks_tops": peaks_all},
+                         "int_peaks_tops": {k: v / 1e12 for k, v in peaks.items()}},
             "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(launches), "clocks": clocks,
             "checksum_terms": "%016X" % termsum,
         }
+        if batched is not None:
+            line["batched"] = batched
         print(json.dumps(line), flush=True)
 
 
@@ -395,7 +518,12 @@ def main():
     world, rank, local = dist_env()
     dist = dist_init(world)
     if args.impl == "reference":
+        if args.workload == "mixed":
+            wl = WORKLOADS["combined"]
         run_reference(args, wl, world, rank)
+    elif args.workload == "mixed":
+        if rank == 0:
+            run_mixed_line(args, local)
     else:
         run_ours(args, wl, world, rank, local, dist)
     if dist is not None:

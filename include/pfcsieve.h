@@ -261,10 +261,20 @@ int pfc_batch_take_hits(pfc_batch *b, uint64_t id, pfc_factor *buf, size_t cap, 
 int pfc_batch_release(pfc_batch *b, uint64_t id);
 /* Iterations run so far. */
 uint64_t pfc_batch_iterations(pfc_batch *b);
-/* Work of one iteration in candidate-steps (default 4e11; a class-64
- * candidate step counts 3): smaller values give new searches and finished
- * results a shorter wait, larger ones less host overhead per step. */
+/* Work of one iteration in candidate-steps (default 1e11, about 0.1 s of
+ * GPU time; a class-64 candidate step counts 3): smaller values give new
+ * searches and finished results a shorter wait, larger ones less host
+ * overhead per step. */
 int pfc_batch_set_iteration_work(pfc_batch *b, double candidate_steps);
+
+/* Scheduling policy.  THROUGHPUT (default): every search advances the same
+ * number of positions per iteration; a batch submitted at once ends soonest.
+ * LATENCY: half of each iteration goes to the searches with the least work
+ * left (shortest remaining work first), for request streams where the
+ * median wait matters. */
+#define PFC_BATCH_THROUGHPUT 0
+#define PFC_BATCH_LATENCY    1
+int pfc_batch_set_policy(pfc_batch *b, int policy);
 
 /* Where a batch's time went, summed over its steps. */
 typedef struct {

@@ -33,6 +33,9 @@ PFC_ERR_NO_DEVICE = -9
 LIB_PATH = _build.LIB
 
 
+BATCH_THROUGHPUT, BATCH_LATENCY = 0, 1
+
+
 class JobDesc(ctypes.Structure):
     """pfc_job_desc: one search submitted to a batch."""
     _fields_ = [("mode", ctypes.c_uint), ("nmin", ctypes.c_uint32), ("nmax", ctypes.c_uint32),
@@ -110,6 +113,7 @@ def lib():
             "pfc_batch_release": (ctypes.c_int, [vp, u64]),
             "pfc_batch_iterations": (u64, [vp]),
             "pfc_batch_set_iteration_work": (ctypes.c_int, [vp, ctypes.c_double]),
+            "pfc_batch_set_policy": (ctypes.c_int, [vp, ctypes.c_int]),
             "pfc_batch_timing": (ctypes.c_int, [vp, P(BatchTimes)]),
         }
         for name, (res, args) in sig.items():
@@ -284,7 +288,7 @@ class Batch:
     (admit queued searches, advance every admitted one, retire finished ones);
     result(id) gives the raw totals and hits of a finished search."""
 
-    def __init__(self, ctx, iteration_work=None):
+    def __init__(self, ctx, iteration_work=None, policy=None):
         self.ctx = ctx
         h = ctypes.c_void_p()
         _ck(lib().pfc_batch_create(ctx.h, ctypes.byref(h)), "pfc_batch_create")
@@ -292,6 +296,8 @@ class Batch:
         if iteration_work is not None:
             _ck(lib().pfc_batch_set_iteration_work(self.h, float(iteration_work)),
                 "pfc_batch_set_iteration_work")
+        if policy is not None:
+            _ck(lib().pfc_batch_set_policy(self.h, int(policy)), "pfc_batch_set_policy")
 
     def close(self):
         if self.h:

@@ -24,6 +24,8 @@
 #include <algorithm>
 #include <chrono>
 #include <cmath>
+#include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <deque>
 #include <map>
@@ -311,6 +313,7 @@ struct BatchJob {
     DevClass<uint64_t> c64;
     std::vector<Block> b32, b64;
     uint32_t tot32 = 0, tot64 = 0;  // timeline lengths (setup ops + walk steps)
+    uint32_t win = 0;               // this iteration's window (0: the common window L)
     // results
     uint64_t termsum = 0, primecount = 0;
     uint32_t flags = 0;
@@ -456,13 +459,16 @@ struct pfc_batch {
     uint32_t cache_lim = 0;
     std::vector<Task> t32, t64, t64c;
     uint64_t next_id = 1;
-    double work_per_iter = 4e11;         // candidate-steps per iteration (class 64 weighs 3)
+    double work_per_iter = 1e11;         // candidate-steps per iteration (class 64 weighs 3)
+    int policy = PFC_BATCH_THROUGHPUT;
     uint64_t iterations = 0;
     // timing: kernel spans (CUDA events) and host phases (wall clock)
     cudaEvent_t ev_start = nullptr, ev_end32 = nullptr, ev_end64 = nullptr;
     double gpu_s = 0, gpu32_s = 0, gpu64_s = 0, prep_s = 0, admit_s = 0, step_s = 0;
     uint64_t tasks = 0;
     size_t t32_n = 0, t64_n = 0;   // task counts of the iteration in flight
+    uint32_t prio = 0;             // searches with their own window this iteration
+    bool trace = false;            // PFCSIEVE_BATCH_TRACE: one stderr line per iteration
 };
 
 static double now_s() {
@@ -658,39 +664,109 @@ int admit_prepared(pfc_batch *b) {
 
 // One task per unfinished block: a window of at most L timeline positions.
 // Returns the window length used.
+// Cost of timeline positions in IMAD-equivalent multiplies per candidate
+// (measured multiply-pipe rates: class-32 step 6; class-64 lazy step 10.5
+// plus its share of the block restore; a 128-bit setup word four lazy rounds)
+struct PosCost {
+    double setup, walk;
+};
+static PosCost pos_cost(const BatchJob *j, bool cls64) {
+    const double chains = j->mode == (PFC_FACTORIAL | PFC_COMPOSITORIAL) ? 2.0 : 1.0;
+    if (!cls64) return {6.0, 6.0 * chains};
+    if (j->pmax <= kLazyEnd) return {45.0, 13.0 * chains};
+    return {60.0, 30.0 * chains};
+}
+
+// remaining cost of a block from position pos
+static double block_cost(const Block &k, uint32_t ns, uint32_t tot, PosCost c) {
+    const double setup = k.pos < ns ? (double)(ns - k.pos) : 0.0;
+    const double walk = (double)tot - (double)std::max(k.pos, ns);
+    return (double)k.count * (setup * c.setup + std::max(walk, 0.0) * c.walk);
+}
+
+// One task per unfinished block.  Throughput policy: every search advances
+// a common window of L positions per iteration (all searches progress at the
+// same pace, so the largest ones are never starved and the batch ends as
+// early as the work allows).  Latency policy (shortest remaining work
+// first): searches are taken in order of remaining cost, and while the
+// priority share (half of the iteration's budget) lasts each gets its own
+// window, as wide as keeps every one of its tasks within one CTA's share of
+// the iteration (no single task outlasts the rest), at most its remainder;
+// the other searches share the rest of the budget with the common window.
+// Returns L.
 uint32_t build_tasks(pfc_batch *b) {
     for (BatchJob *j : b->ready) {
         j->state = kRunning;
         b->running.push_back(j);
     }
     b->ready.clear();
-    double cands = 0;
+    const double budget = b->work_per_iter * 6.0;   // candidate-steps -> multiplies
+    const double per_cta = budget / (3.0 * b->ctx->sms);
+    std::vector<std::pair<double, BatchJob *>> order;
+    order.reserve(b->running.size());
     for (BatchJob *j : b->running) {
-        for (const Block &k : j->b32) cands += k.pos < j->tot32 ? k.count : 0;
-        for (const Block &k : j->b64) cands += k.pos < j->tot64 ? 3.0 * k.count : 0;
+        double r = 0;
+        const PosCost c32 = pos_cost(j, false), c64 = pos_cost(j, true);
+        for (const Block &k : j->b32) r += block_cost(k, j->nsetup32, j->tot32, c32);
+        for (const Block &k : j->b64) r += block_cost(k, j->nsetup64, j->tot64, c64);
+        order.push_back({r, j});
     }
-    const double Ld = std::max(64.0, std::min(b->work_per_iter / std::max(cands, 1.0), 4194304.0));
+    std::sort(order.begin(), order.end(), [](const auto &x, const auto &y) { return x.first < y.first; });
+    const double share = b->policy == PFC_BATCH_LATENCY ? 0.5 : 0.0;
+    double prio_left = share * budget, rate = 0;   // rate: cost per common-window position
+    for (auto &o : order) {
+        BatchJob *j = o.second;
+        const PosCost c32 = pos_cost(j, false), c64 = pos_cost(j, true);
+        j->win = 0;
+        double jrate = 0, worst = 0;
+        for (const Block &k : j->b32)
+            if (k.pos < j->tot32) {
+                jrate += k.count * (k.pos < j->nsetup32 ? c32.setup : c32.walk);
+                worst = std::max(worst, k.count * std::max(c32.setup, c32.walk));
+            }
+        for (const Block &k : j->b64)
+            if (k.pos < j->tot64) {
+                jrate += k.count * (k.pos < j->nsetup64 ? c64.setup : c64.walk);
+                worst = std::max(worst, k.count * std::max(c64.setup, c64.walk));
+            }
+        if (prio_left > 0) {
+            const double w = std::min(per_cta / std::max(worst, 1.0), 4294967295.0);
+            j->win = std::max<uint32_t>(64u, (uint32_t)w);
+            prio_left -= std::min(o.first, w * jrate);
+            continue;
+        }
+        rate += jrate;
+    }
+    b->prio = 0;
+    for (auto &o : order) b->prio += o.second->win ? 1u : 0u;
+    const double Ld = std::max(64.0, std::min((1.0 - share) * budget / std::max(rate, 1.0), 4194304.0));
     const uint32_t L = ((uint32_t)Ld + 15u) & ~15u;
-    // longest first: windows with setup work, full walk windows, short ends
-    std::vector<Task> part[3][3];  // [list][kind]
+    // longest first: tasks bucketed by log2 of their estimated cost, the
+    // costliest bucket dispatched first (a counting sort, linear in tasks)
+    constexpr int kBuckets = 64;
+    std::vector<Task> part[3][kBuckets];
     for (BatchJob *j : b->running) {
         const int l64 = j->pmax <= kLazyEnd ? 1 : 2;
         for (int cls = 0; cls < 2; ++cls) {
             const std::vector<Block> &blocks = cls ? j->b64 : j->b32;
             const uint32_t tot = cls ? j->tot64 : j->tot32, ns = cls ? j->nsetup64 : j->nsetup32;
+            const PosCost c = pos_cost(j, cls != 0);
             std::vector<Task> *dst = part[cls ? l64 : 0];
             for (const Block &k : blocks) {
                 if (k.pos >= tot) continue;
-                const uint32_t hi = (uint32_t)std::min<uint64_t>((uint64_t)k.pos + L, tot);
-                const int kind = k.pos < ns ? 0 : (hi - k.pos == L ? 1 : 2);
-                dst[kind].push_back({j->slot, k.first, k.count, k.pos, hi});
+                const uint32_t hi = (uint32_t)std::min<uint64_t>((uint64_t)k.pos + (j->win ? j->win : L), tot);
+                const double setup = k.pos < ns ? (double)(std::min(hi, ns) - k.pos) : 0.0;
+                const double walk = hi > ns ? (double)(hi - std::max(k.pos, ns)) : 0.0;
+                const double cost = (double)k.count * (setup * c.setup + walk * c.walk);
+                const int bucket = std::min(kBuckets - 1, std::max(0, (int)std::log2(std::max(cost, 1.0))));
+                dst[bucket].push_back({j->slot, k.first, k.count, k.pos, hi});
             }
         }
     }
     std::vector<Task> *out[3] = {&b->t32, &b->t64, &b->t64c};
     for (int l = 0; l < 3; ++l) {
         out[l]->clear();
-        for (int kind = 0; kind < 3; ++kind) out[l]->insert(out[l]->end(), part[l][kind].begin(), part[l][kind].end());
+        for (int bk = kBuckets - 1; bk >= 0; --bk) out[l]->insert(out[l]->end(), part[l][bk].begin(), part[l][bk].end());
     }
     return L;
 }
@@ -766,9 +842,16 @@ int finish_iteration(pfc_batch *b, uint32_t L) {
             if (tv[i] < pfc_batch::kSlots && by_slot[tv[i]]) by_slot[tv[i]]->hits.push_back(hv[i]);
     }
     if (nh) CK(cudaMemsetAsync(b->hitcount.p, 0, sizeof(unsigned long long), c->st));
+    if (b->trace) {
+        float ms = 0;
+        cudaEventElapsedTime(&ms, b->ev_start, b->t64_n ? b->ev_end64 : b->ev_end32);
+        fprintf(stderr, "batch iter %llu: running %zu prio %u L %u tasks %zu/%zu hits %llu gpu %.2f ms\n",
+                (unsigned long long)b->iterations, b->running.size(), b->prio, L, b->t32_n, b->t64_n, nh, ms);
+    }
     for (BatchJob *j : b->running) {
-        for (Block &k : j->b32) k.pos = (uint32_t)std::min<uint64_t>((uint64_t)k.pos + L, j->tot32);
-        for (Block &k : j->b64) k.pos = (uint32_t)std::min<uint64_t>((uint64_t)k.pos + L, j->tot64);
+        const uint64_t w = j->win ? j->win : L;
+        for (Block &k : j->b32) k.pos = (uint32_t)std::min<uint64_t>((uint64_t)k.pos + w, j->tot32);
+        for (Block &k : j->b64) k.pos = (uint32_t)std::min<uint64_t>((uint64_t)k.pos + w, j->tot64);
     }
     return PFC_OK;
 }
@@ -869,6 +952,8 @@ extern "C" int pfc_batch_create(pfc_ctx *c, pfc_batch **out) {
         return cuda_fail(e);
     }
     for (uint32_t s = pfc_batch::kSlots; s-- > 0;) b->free_slots.push_back(s);
+    const char *tr = getenv("PFCSIEVE_BATCH_TRACE");
+    b->trace = tr && *tr && *tr != '0';
     *out = b;
     return PFC_OK;
 }
@@ -1014,6 +1099,12 @@ extern "C" int pfc_batch_timing(pfc_batch *b, pfc_batch_times *t) {
     t->admit_s = b->admit_s;
     t->iterations = b->iterations;
     t->tasks = b->tasks;
+    return PFC_OK;
+}
+
+extern "C" int pfc_batch_set_policy(pfc_batch *b, int policy) {
+    if (!b || (policy != PFC_BATCH_THROUGHPUT && policy != PFC_BATCH_LATENCY)) return PFC_ERR_ARG;
+    b->policy = policy;
     return PFC_OK;
 }
 

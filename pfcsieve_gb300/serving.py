@@ -22,7 +22,7 @@ from dataclasses import dataclass
 
 import numpy as np
 
-from . import COMPOSITORIAL, FACTORIAL, PRIMORIAL, Batch, Job, PFCError
+from . import BATCH_LATENCY, COMPOSITORIAL, FACTORIAL, PRIMORIAL, Batch, Job, PFCError
 
 MODES = (FACTORIAL, PRIMORIAL, COMPOSITORIAL)
 
@@ -123,10 +123,12 @@ def poisson_arrivals(count, rate, seed=1):
 
 def serve(ctx, searches, arrivals, iteration_work=5e10, keep_hits=False):
     """Request loop: submit each search when its arrival time has passed, step
-    the batch while anything is queued or running, and collect results.
+    the batch while anything is queued or running, and collect results.  The
+    batch runs the latency policy (shortest remaining work first) with short
+    iterations.
 
     Returns (outcomes, latencies in s, makespan in s)."""
-    with Batch(ctx, iteration_work) as b:
+    with Batch(ctx, iteration_work, policy=BATCH_LATENCY) as b:
         t0 = time.perf_counter()
         pending = list(range(len(searches)))
         running = {}

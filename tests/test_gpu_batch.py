@@ -121,3 +121,31 @@ def test_invalid_searches_are_rejected(ctx):
                     (1, 101, 200, 2, 10**6), (1, 101, 200, 10**6, 10**6)]:
             with pytest.raises(pfc.PFCError):
                 b.submit(*bad)
+
+
+def test_latency_policy_gives_the_same_results(ctx):
+    """Shortest-remaining-work-first windows change only the order of work:
+    searches submitted between iterations under the latency policy still
+    equal their stand-alone results, and the small ones finish first."""
+    with pfc.Batch(ctx, iteration_work=5e8, policy=pfc.BATCH_LATENCY) as b:
+        ids = []
+        for k, case in enumerate(MIX):
+            ids.append(b.submit(*case))
+            if k % 3 == 2:
+                b.step()
+        finished = []
+        while True:
+            active, queued = b.step()
+            for jid in ids:
+                if jid not in finished and b.status(jid).done:
+                    finished.append(jid)
+            if active == 0 and queued == 0:
+                break
+        for case, jid in zip(MIX, ids):
+            got = batched(b, jid)
+            want = alone(ctx, case)
+            assert got[:2] == want[:2], case
+            assert np.array_equal(got[2], want[2]), case
+        # the largest search of the mix (by candidates x n) is not among the first to finish
+        big = max(range(len(MIX)), key=lambda i: (MIX[i][4] - MIX[i][3]) * (MIX[i][2] - MIX[i][1]))
+        assert finished.index(ids[big]) >= len(MIX) // 2
