@@ -70,7 +70,9 @@ WORKLOADS = {
     "mixed": dict(mode=0, nmin=0, nmax=0, pmin=0, pmax=0,
                   desc="mixed searches: modes !,#,c; n-range log-uniform [1e3,1e6] from n0 in [101,1e7); "
                        "p-range log-uniform [1e5,1e8] from p0 log-uniform [1e8,2^63]; seed 0"),
-    # reduced case of the combined search for ncu captures (same kernels)
+    # reduced cases for ncu captures (same kernels)
+    "primorial-small": dict(mode=2, nmin=101, nmax=10**6, pmin=2**62, pmax=2**62 + 5 * 10**6,
+                            desc="-# n=[101,1e6) p=[2^62,2^62+5e6)"),
     "combined-small": dict(mode=5, nmin=101, nmax=20000, pmin=10**9, pmax=10**9 + 10**7,
                            desc="-! -c n=[101,20000) p=[1e9,1.01e9)"),
 }

@@ -74,6 +74,15 @@ struct Task {
     uint32_t slot, first, count, lo, hi;
 };
 
+// One iteration's window of one search in one size class: CTAs
+// [first_cta, first_cta + nblocks) take the search's candidate blocks in
+// order, each over timeline positions [lo, hi).  All blocks of a search
+// share one position (they advance together), so an iteration is described
+// by one window per search and class, not one record per block.
+struct Window {
+    uint32_t first_cta, nblocks, slot, ncand, lo, hi, pad0, pad1;
+};
+
 // Setup positions [lo, hi) of NC candidates: acc advances through the
 // program, fork receives the compositorial residue at the fork.  Same
 // operations as run_prog in the same order, resumable at any position.
@@ -251,23 +260,36 @@ __device__ void run_task(const JobDev<typename T::W> &J, const Task &t, const Hi
     if (__any_sync(kFull, bad) && (threadIdx.x & 31) == 0) atomicOr(J.flags, 1u);
 }
 
-// One CTA per task.  The task list of an iteration is ordered longest first
-// (windows with setup work, then full walk windows, then the short ends of
-// blocks), and the hardware block scheduler hands tasks to SMs as CTA slots
-// free up: a device-side work queue whose tail is spread over all SMs.  (A
-// persistent grid taking tasks from an atomic counter let the last tasks of
-// an iteration crowd onto a few SMs: 78% of the per-job path's throughput on
-// a single large search, against 100% with hardware dispatch.)
+// One CTA per task (a block of 256 candidates, 512 for two-candidate class-32
+// walks, over one window).  The windows of an iteration are ordered by the
+// cost of their tasks, longest first, and the hardware block scheduler hands
+// CTAs to SMs as slots free up: a device-side work queue whose tail is spread
+// over all SMs.  (A persistent grid taking tasks from an atomic counter let
+// the last tasks of an iteration crowd onto a few SMs: 78% of the per-job
+// path's throughput on a single large search, against 100% with hardware
+// dispatch.)  Thread 0 finds its window by binary search over first_cta.
 template <class T>
 __global__ void __launch_bounds__(256, sizeof(typename T::W) == 4 ? 4 : 2)
-    batch_kernel(const Task *tasks, const JobDev<typename T::W> *jobs, HitBuf h) {
+    batch_kernel(const Window *wins, uint32_t nwins, const JobDev<typename T::W> *jobs, HitBuf h) {
     // the task and its search record live in shared memory: every thread
     // reads the same fields, and registers stay free for the residues
     __shared__ Task st;
     __shared__ JobDev<typename T::W> sj;
     if (threadIdx.x == 0) {
-        st = tasks[blockIdx.x];
-        sj = jobs[st.slot];
+        uint32_t a = 0, b = nwins;  // wins[a].first_cta <= blockIdx.x
+        while (b - a > 1) {
+            const uint32_t mid = (a + b) >> 1;
+            if (wins[mid].first_cta <= blockIdx.x) a = mid;
+            else b = mid;
+        }
+        const Window w = wins[a];
+        sj = jobs[w.slot];
+        const uint32_t per = (sj.mode == (PFC_FACTORIAL | PFC_COMPOSITORIAL) ? 1u : (uint32_t)T::NC) * blockDim.x;
+        st.slot = w.slot;
+        st.first = (blockIdx.x - w.first_cta) * per;
+        st.count = min(per, w.ncand - st.first);
+        st.lo = w.lo;
+        st.hi = w.hi;
     }
     __syncthreads();
     HitBuf hh = h;
@@ -277,10 +299,6 @@ __global__ void __launch_bounds__(256, sizeof(typename T::W) == 4 ? 4 : 2)
 }
 
 // ------------------------------------------------------------------ host side
-
-struct Block {
-    uint32_t first, count, pos;
-};
 
 // queued -> prepared (host tables built) -> ready (on the device, candidates
 // generated) -> running (blocks in the task list) -> done
@@ -311,8 +329,9 @@ struct BatchJob {
     DArr<SetupSeg> d_segs32, d_segs64;
     DevClass<uint32_t> c32;
     DevClass<uint64_t> c64;
-    std::vector<Block> b32, b64;
-    uint32_t tot32 = 0, tot64 = 0;  // timeline lengths (setup ops + walk steps)
+    uint32_t n32 = 0, n64 = 0;      // candidates per class
+    uint32_t pos32 = 0, pos64 = 0;  // timeline position of all blocks of a class
+    uint32_t tot32 = 0, tot64 = 0;  // timeline lengths (setup positions + walk steps)
     uint32_t win = 0;               // this iteration's window (0: the common window L)
     // results
     uint64_t termsum = 0, primecount = 0;
@@ -444,7 +463,7 @@ struct pfc_batch {
     DArr<JobDev<uint32_t>> jobs32;
     DArr<JobDev<uint64_t>> jobs64;
     // task lists: class 32, class 64 below 2^63 (lazy walk), other class 64
-    DArr<Task> tasks32, tasks64, tasks64c;
+    DArr<Window> wins32, wins64, wins64c;
     DArr<pfc_factor> hits;
     DArr<uint32_t> tags;
     DArr<unsigned long long> hitcount;
@@ -457,7 +476,8 @@ struct pfc_batch {
     std::vector<uint32_t> free_slots;
     std::vector<uint32_t> prime_cache;   // primes up to cache_lim
     uint32_t cache_lim = 0;
-    std::vector<Task> t32, t64, t64c;
+    std::vector<Window> w32, w64, w64c;   // this iteration's windows per kernel
+    uint64_t ctas32 = 0, ctas64 = 0, ctas64c = 0;
     uint64_t next_id = 1;
     double work_per_iter = 1e11;         // candidate-steps per iteration (class 64 weighs 3)
     int policy = PFC_BATCH_THROUGHPUT;
@@ -634,10 +654,10 @@ int admit_prepared(pfc_batch *b) {
         const uint32_t n32 = j->use32 ? s.counts[0] : 0;
         const uint32_t n64 = j->use64 ? s.counts[1] : 0;
         j->primecount = (uint64_t)n32 + n64;
-        const uint32_t per32 = (j->mode == (PFC_FACTORIAL | PFC_COMPOSITORIAL)) ? 256u : 256u * Cls32::NC;
-        const uint32_t per64 = 256u * Cls64::NC;
-        for (uint32_t k = 0; k < n32; k += per32) j->b32.push_back({k, std::min(per32, n32 - k), 0});
-        for (uint32_t k = 0; k < n64; k += per64) j->b64.push_back({k, std::min(per64, n64 - k), 0});
+        j->n32 = n32;
+        j->n64 = n64;
+        j->pos32 = n32 ? 0 : j->tot32;
+        j->pos64 = n64 ? 0 : j->tot64;
         v32[f] = job_view<uint32_t>(b, j, j->c32, 0, j->d_words32.p, j->d_segs32, j->segs32.size(), j->c32a,
                                     j->c32b, j->nsetup32);
         const void *w64 = j->pmax <= kLazyEnd ? (const void *)j->d_words128.p : (const void *)j->d_words64.p;
@@ -677,14 +697,21 @@ static PosCost pos_cost(const BatchJob *j, bool cls64) {
     return {60.0, 30.0 * chains};
 }
 
-// remaining cost of a block from position pos
-static double block_cost(const Block &k, uint32_t ns, uint32_t tot, PosCost c) {
-    const double setup = k.pos < ns ? (double)(ns - k.pos) : 0.0;
-    const double walk = (double)tot - (double)std::max(k.pos, ns);
-    return (double)k.count * (setup * c.setup + std::max(walk, 0.0) * c.walk);
+// remaining cost of n candidates at position pos of a timeline
+static double class_cost(uint32_t n, uint32_t pos, uint32_t ns, uint32_t tot, PosCost c) {
+    if (pos >= tot) return 0.0;
+    const double setup = pos < ns ? (double)(ns - pos) : 0.0;
+    const double walk = (double)tot - (double)std::max(pos, ns);
+    return (double)n * (setup * c.setup + walk * c.walk);
 }
 
-// One task per unfinished block.  Throughput policy: every search advances
+// candidates per CTA of a class
+static uint32_t per_cta(const BatchJob *j, bool cls64) {
+    if (cls64) return 256u * Cls64L::NC;
+    return j->mode == (PFC_FACTORIAL | PFC_COMPOSITORIAL) ? 256u : 256u * Cls32::NC;
+}
+
+// One window per search and class.  Throughput policy: every search advances
 // a common window of L positions per iteration (all searches progress at the
 // same pace, so the largest ones are never starved and the batch ends as
 // early as the work allows).  Latency policy (shortest remaining work
@@ -693,7 +720,8 @@ static double block_cost(const Block &k, uint32_t ns, uint32_t tot, PosCost c) {
 // window, as wide as keeps every one of its tasks within one CTA's share of
 // the iteration (no single task outlasts the rest), at most its remainder;
 // the other searches share the rest of the budget with the common window.
-// Returns L.
+// Windows are then ordered by the cost of one of their tasks, longest first.
+// Host work is linear in the number of searches.  Returns L.
 uint32_t build_tasks(pfc_batch *b) {
     for (BatchJob *j : b->ready) {
         j->state = kRunning;
@@ -701,14 +729,12 @@ uint32_t build_tasks(pfc_batch *b) {
     }
     b->ready.clear();
     const double budget = b->work_per_iter * 6.0;   // candidate-steps -> multiplies
-    const double per_cta = budget / (3.0 * b->ctx->sms);
+    const double cta_share = budget / (3.0 * b->ctx->sms);
     std::vector<std::pair<double, BatchJob *>> order;
     order.reserve(b->running.size());
     for (BatchJob *j : b->running) {
-        double r = 0;
-        const PosCost c32 = pos_cost(j, false), c64 = pos_cost(j, true);
-        for (const Block &k : j->b32) r += block_cost(k, j->nsetup32, j->tot32, c32);
-        for (const Block &k : j->b64) r += block_cost(k, j->nsetup64, j->tot64, c64);
+        const double r = class_cost(j->n32, j->pos32, j->nsetup32, j->tot32, pos_cost(j, false)) +
+                         class_cost(j->n64, j->pos64, j->nsetup64, j->tot64, pos_cost(j, true));
         order.push_back({r, j});
     }
     std::sort(order.begin(), order.end(), [](const auto &x, const auto &y) { return x.first < y.first; });
@@ -717,20 +743,18 @@ uint32_t build_tasks(pfc_batch *b) {
     for (auto &o : order) {
         BatchJob *j = o.second;
         const PosCost c32 = pos_cost(j, false), c64 = pos_cost(j, true);
-        j->win = 0;
         double jrate = 0, worst = 0;
-        for (const Block &k : j->b32)
-            if (k.pos < j->tot32) {
-                jrate += k.count * (k.pos < j->nsetup32 ? c32.setup : c32.walk);
-                worst = std::max(worst, k.count * std::max(c32.setup, c32.walk));
-            }
-        for (const Block &k : j->b64)
-            if (k.pos < j->tot64) {
-                jrate += k.count * (k.pos < j->nsetup64 ? c64.setup : c64.walk);
-                worst = std::max(worst, k.count * std::max(c64.setup, c64.walk));
-            }
+        if (j->pos32 < j->tot32) {
+            jrate += j->n32 * (j->pos32 < j->nsetup32 ? c32.setup : c32.walk);
+            worst = std::max(worst, per_cta(j, false) * std::max(c32.setup, c32.walk));
+        }
+        if (j->pos64 < j->tot64) {
+            jrate += j->n64 * (j->pos64 < j->nsetup64 ? c64.setup : c64.walk);
+            worst = std::max(worst, per_cta(j, true) * std::max(c64.setup, c64.walk));
+        }
+        j->win = 0;
         if (prio_left > 0) {
-            const double w = std::min(per_cta / std::max(worst, 1.0), 4294967295.0);
+            const double w = std::min(cta_share / std::max(worst, 1.0), 4294967295.0);
             j->win = std::max<uint32_t>(64u, (uint32_t)w);
             prio_left -= std::min(o.first, w * jrate);
             continue;
@@ -741,46 +765,55 @@ uint32_t build_tasks(pfc_batch *b) {
     for (auto &o : order) b->prio += o.second->win ? 1u : 0u;
     const double Ld = std::max(64.0, std::min((1.0 - share) * budget / std::max(rate, 1.0), 4194304.0));
     const uint32_t L = ((uint32_t)Ld + 15u) & ~15u;
-    // longest first: tasks bucketed by log2 of their estimated cost, the
-    // costliest bucket dispatched first (a counting sort, linear in tasks)
-    constexpr int kBuckets = 64;
-    std::vector<Task> part[3][kBuckets];
+
+    std::vector<std::pair<double, Window>> lists[3];
     for (BatchJob *j : b->running) {
-        const int l64 = j->pmax <= kLazyEnd ? 1 : 2;
         for (int cls = 0; cls < 2; ++cls) {
-            const std::vector<Block> &blocks = cls ? j->b64 : j->b32;
-            const uint32_t tot = cls ? j->tot64 : j->tot32, ns = cls ? j->nsetup64 : j->nsetup32;
+            const uint32_t pos = cls ? j->pos64 : j->pos32, tot = cls ? j->tot64 : j->tot32;
+            const uint32_t ns = cls ? j->nsetup64 : j->nsetup32, n = cls ? j->n64 : j->n32;
+            if (pos >= tot || n == 0) continue;
+            const uint32_t hi = (uint32_t)std::min<uint64_t>((uint64_t)pos + (j->win ? j->win : L), tot);
             const PosCost c = pos_cost(j, cls != 0);
-            std::vector<Task> *dst = part[cls ? l64 : 0];
-            for (const Block &k : blocks) {
-                if (k.pos >= tot) continue;
-                const uint32_t hi = (uint32_t)std::min<uint64_t>((uint64_t)k.pos + (j->win ? j->win : L), tot);
-                const double setup = k.pos < ns ? (double)(std::min(hi, ns) - k.pos) : 0.0;
-                const double walk = hi > ns ? (double)(hi - std::max(k.pos, ns)) : 0.0;
-                const double cost = (double)k.count * (setup * c.setup + walk * c.walk);
-                const int bucket = std::min(kBuckets - 1, std::max(0, (int)std::log2(std::max(cost, 1.0))));
-                dst[bucket].push_back({j->slot, k.first, k.count, k.pos, hi});
-            }
+            const uint32_t per = per_cta(j, cls != 0);
+            const double setup = pos < ns ? (double)(std::min(hi, ns) - pos) : 0.0;
+            const double walk = hi > ns ? (double)(hi - std::max(pos, ns)) : 0.0;
+            const double cost = (double)std::min(per, n) * (setup * c.setup + walk * c.walk);
+            Window w{};
+            w.nblocks = (n + per - 1) / per;
+            w.slot = j->slot;
+            w.ncand = n;
+            w.lo = pos;
+            w.hi = hi;
+            const int l = cls == 0 ? 0 : (j->pmax <= kLazyEnd ? 1 : 2);
+            lists[l].push_back({cost, w});
         }
     }
-    std::vector<Task> *out[3] = {&b->t32, &b->t64, &b->t64c};
+    std::vector<Window> *out[3] = {&b->w32, &b->w64, &b->w64c};
+    uint64_t *ctas[3] = {&b->ctas32, &b->ctas64, &b->ctas64c};
     for (int l = 0; l < 3; ++l) {
+        std::sort(lists[l].begin(), lists[l].end(), [](const auto &x, const auto &y) { return x.first > y.first; });
         out[l]->clear();
-        for (int bk = kBuckets - 1; bk >= 0; --bk) out[l]->insert(out[l]->end(), part[l][bk].begin(), part[l][bk].end());
+        uint64_t first = 0;
+        for (auto &e : lists[l]) {
+            e.second.first_cta = (uint32_t)first;
+            first += e.second.nblocks;
+            out[l]->push_back(e.second);
+        }
+        *ctas[l] = first;
     }
     return L;
 }
 
 int launch_iteration(pfc_batch *b) {
     pfc_ctx *c = b->ctx;
-    const size_t n32 = b->t32.size(), n64 = b->t64.size(), n64c = b->t64c.size();
-    if (b->tasks32.n < n32) CK(b->tasks32.alloc(c, n32 + n32 / 2 + 64));
-    if (b->tasks64.n < n64) CK(b->tasks64.alloc(c, n64 + n64 / 2 + 64));
-    if (b->tasks64c.n < n64c) CK(b->tasks64c.alloc(c, n64c + n64c / 2 + 64));
-    if (n32) CK(cudaMemcpyAsync(b->tasks32.p, b->t32.data(), n32 * sizeof(Task), cudaMemcpyHostToDevice, c->st));
-    if (n64) CK(cudaMemcpyAsync(b->tasks64.p, b->t64.data(), n64 * sizeof(Task), cudaMemcpyHostToDevice, c->st));
-    if (n64c) CK(cudaMemcpyAsync(b->tasks64c.p, b->t64c.data(), n64c * sizeof(Task), cudaMemcpyHostToDevice, c->st));
-    c->h2d += (n32 + n64 + n64c) * sizeof(Task);
+    const size_t n32 = b->w32.size(), n64 = b->w64.size(), n64c = b->w64c.size();
+    if (b->wins32.n < n32) CK(b->wins32.alloc(c, n32 + n32 / 2 + 64));
+    if (b->wins64.n < n64) CK(b->wins64.alloc(c, n64 + n64 / 2 + 64));
+    if (b->wins64c.n < n64c) CK(b->wins64c.alloc(c, n64c + n64c / 2 + 64));
+    if (n32) CK(cudaMemcpyAsync(b->wins32.p, b->w32.data(), n32 * sizeof(Window), cudaMemcpyHostToDevice, c->st));
+    if (n64) CK(cudaMemcpyAsync(b->wins64.p, b->w64.data(), n64 * sizeof(Window), cudaMemcpyHostToDevice, c->st));
+    if (n64c) CK(cudaMemcpyAsync(b->wins64c.p, b->w64c.data(), n64c * sizeof(Window), cudaMemcpyHostToDevice, c->st));
+    c->h2d += (n32 + n64 + n64c) * sizeof(Window);
     CK(cudaEventRecord(b->ev_start, c->st));
     CK(cudaStreamWaitEvent(b->st32, b->ev_start, 0));
     CK(cudaStreamWaitEvent(b->st64, b->ev_start, 0));
@@ -789,16 +822,16 @@ int launch_iteration(pfc_batch *b) {
     h.count = b->hitcount.p;
     h.cap = b->hits.n;
     h.tag = b->tags.p;
-    if (n32) {
-        batch_kernel<Cls32><<<(unsigned)n32, 256, 0, b->st32>>>(b->tasks32.p, b->jobs32.p, h);
+    if (b->ctas32) {
+        batch_kernel<Cls32><<<(unsigned)b->ctas32, 256, 0, b->st32>>>(b->wins32.p, (uint32_t)n32, b->jobs32.p, h);
         c->launches++;
     }
-    if (n64) {
-        batch_kernel<Cls64L><<<(unsigned)n64, 256, 0, b->st64>>>(b->tasks64.p, b->jobs64.p, h);
+    if (b->ctas64) {
+        batch_kernel<Cls64L><<<(unsigned)b->ctas64, 256, 0, b->st64>>>(b->wins64.p, (uint32_t)n64, b->jobs64.p, h);
         c->launches++;
     }
-    if (n64c) {
-        batch_kernel<Cls64><<<(unsigned)n64c, 256, 0, b->st64>>>(b->tasks64c.p, b->jobs64.p, h);
+    if (b->ctas64c) {
+        batch_kernel<Cls64><<<(unsigned)b->ctas64c, 256, 0, b->st64>>>(b->wins64c.p, (uint32_t)n64c, b->jobs64.p, h);
         c->launches++;
     }
     CK(cudaGetLastError());
@@ -807,15 +840,15 @@ int launch_iteration(pfc_batch *b) {
     CK(cudaStreamWaitEvent(c->st, b->ev_end32, 0));
     CK(cudaEventRecord(b->ev_end64, b->st64));
     CK(cudaStreamWaitEvent(c->st, b->ev_end64, 0));
-    b->tasks += n32 + n64 + n64c;
-    b->t32_n = n32;
-    b->t64_n = n64 + n64c;
+    b->tasks += b->ctas32 + b->ctas64 + b->ctas64c;
+    b->t32_n = b->ctas32;
+    b->t64_n = b->ctas64 + b->ctas64c;
     CK(cudaMemcpyAsync(b->h_hitcount, b->hitcount.p, sizeof(unsigned long long), cudaMemcpyDeviceToHost, c->st));
     return PFC_OK;
 }
 
 // After the iteration: route the hits by slot (on overflow, every search of
-// the iteration is redone alone at the end) and advance the blocks.
+// the iteration is redone alone at the end) and advance the positions.
 int finish_iteration(pfc_batch *b, uint32_t L) {
     pfc_ctx *c = b->ctx;
     CK(cudaStreamSynchronize(c->st));
@@ -850,8 +883,8 @@ int finish_iteration(pfc_batch *b, uint32_t L) {
     }
     for (BatchJob *j : b->running) {
         const uint64_t w = j->win ? j->win : L;
-        for (Block &k : j->b32) k.pos = (uint32_t)std::min<uint64_t>((uint64_t)k.pos + w, j->tot32);
-        for (Block &k : j->b64) k.pos = (uint32_t)std::min<uint64_t>((uint64_t)k.pos + w, j->tot64);
+        j->pos32 = (uint32_t)std::min<uint64_t>((uint64_t)j->pos32 + w, j->tot32);
+        j->pos64 = (uint32_t)std::min<uint64_t>((uint64_t)j->pos64 + w, j->tot64);
     }
     return PFC_OK;
 }
@@ -889,9 +922,7 @@ int retire_finished(pfc_batch *b) {
     pfc_ctx *c = b->ctx;
     std::vector<BatchJob *> done, still;
     for (BatchJob *j : b->running) {
-        bool fin = true;
-        for (const Block &k : j->b32) fin &= k.pos >= j->tot32;
-        for (const Block &k : j->b64) fin &= k.pos >= j->tot64;
+        const bool fin = j->pos32 >= j->tot32 && j->pos64 >= j->tot64;
         (fin ? done : still).push_back(j);
     }
     if (done.empty()) return PFC_OK;
@@ -903,8 +934,6 @@ int retire_finished(pfc_batch *b) {
         j->flags = s.flags;
         release_device(b, j);
         b->free_slots.push_back(j->slot);
-        j->b32.clear();
-        j->b64.clear();
         j->state = kDone;
         if (j->rerun) {
             j->hits.clear();
@@ -969,9 +998,9 @@ extern "C" int pfc_batch_destroy(pfc_batch *b) {
     b->stats.release(c);
     b->jobs32.release(c);
     b->jobs64.release(c);
-    b->tasks32.release(c);
-    b->tasks64.release(c);
-    b->tasks64c.release(c);
+    b->wins32.release(c);
+    b->wins64.release(c);
+    b->wins64c.release(c);
     b->hits.release(c);
     b->tags.release(c);
     b->hitcount.release(c);
@@ -1025,7 +1054,7 @@ extern "C" int pfc_batch_step(pfc_batch *b, uint32_t *active, uint32_t *queued) 
     const double ts = now_s();
     for (int pass = 0; pass < 2; ++pass) {
         const uint32_t L = build_tasks(b);
-        const bool work = !b->t32.empty() || !b->t64.empty() || !b->t64c.empty();
+        const bool work = b->ctas32 + b->ctas64 + b->ctas64c > 0;
         if (work) {
             const int rc = launch_iteration(b);
             if (rc) return rc;
