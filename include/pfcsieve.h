@@ -165,6 +165,18 @@ uint64_t pfc_job_pairs(pfc_job *job);
  * cls64 = 0, else p >= 2^32), excluding the final correction. */
 uint64_t pfc_job_setup_mulmods(pfc_job *job, int cls64);
 
+/* Check the job's tables on the device against slow products, as the
+ * reference checks its power and product tables once per run
+ * (kernels/verifyslow.cl, kernels/verify.cl, cl_sieve.cpp:917-970,1100-1140,
+ * 1270-1310).  Each setup-program form the job built is run by the setup
+ * kernel on a test prime (2^31 - 1, 2^62 - 57, 2^64 - 59) and compared with
+ * the products over k in [2, nmin - 1] of the primes and the composites,
+ * found by a device Miller-Rabin test; the primorial's prime list and the
+ * compositorial's prime flags of [nmin, nmax) are checked by product and
+ * count.  PFC_ERR_VALIDATION on a mismatch; *table_bytes (may be NULL)
+ * receives the size of the tables checked.  Synchronises. */
+int pfc_job_verify_tables(pfc_job *job, uint64_t *table_bytes);
+
 /* ------------------------------------------------- host-side post-processing */
 
 /* Sort hits by (p, |n|, type), re-verify each on the CPU with naive products

@@ -97,6 +97,7 @@ def lib():
             "pfc_segment_state": (ctypes.c_int, [vp, vp, vp, vp, sz, P(sz)]),
             "pfc_job_pairs": (u64, [vp]),
             "pfc_job_setup_mulmods": (u64, [vp, ctypes.c_int]),
+            "pfc_job_verify_tables": (ctypes.c_int, [vp, P(u64)]),
             "pfc_finalize_factors": (ctypes.c_int, [ctypes.c_uint, u32, vp, sz, ctypes.c_int,
                                                     ctypes.c_int, P(sz), P(u64)]),
             "pfc_is_prime": (ctypes.c_int, [u64]),
@@ -279,6 +280,12 @@ class Job:
 
     def setup_mulmods(self, cls64):
         return lib().pfc_job_setup_mulmods(self.h, int(cls64))
+
+    def verify_tables(self):
+        """Device self-check of the job's tables; returns the bytes checked."""
+        n = ctypes.c_uint64(0)
+        _ck(lib().pfc_job_verify_tables(self.h, ctypes.byref(n)), "pfc_job_verify_tables")
+        return n.value
 
 
 class Batch:

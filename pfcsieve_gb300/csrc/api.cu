@@ -650,3 +650,129 @@ extern "C" uint64_t pfc_job_pairs(pfc_job *j) { return j ? j->pairs : 0; }
 extern "C" uint64_t pfc_job_setup_mulmods(pfc_job *j, int cls64) {
     return j ? (cls64 ? j->setup_mulmods64 : j->setup_mulmods32) : 0;
 }
+
+// ------------------------------------------------------- table self-check
+
+static uint64_t mulmod_h(uint64_t a, uint64_t b, uint64_t p) { return (uint64_t)((unsigned __int128)a * b % p); }
+static uint64_t powmod_h(uint64_t a, uint64_t e, uint64_t p) {
+    uint64_t r = 1 % p;
+    a %= p;
+    for (; e; e >>= 1) {
+        if (e & 1) r = mulmod_h(r, a, p);
+        a = mulmod_h(a, a, p);
+    }
+    return r;
+}
+
+// Run the job's setup programs of one word form on the single candidate p and
+// return its residues in plain form (s1: the combined search's compositorial).
+template <class W, class SW>
+static int setup_on_prime(pfc_job *j, const DevProg<SW> &a, const DevProg<SW> &b, uint64_t p, uint64_t &s0,
+                          uint64_t &s1) {
+    pfc_ctx *c = j->ctx;
+    DevClass<W> cls;
+    DArr<uint32_t> cnt;
+    CK(cls.ensure(c, 1));
+    cudaError_t e = cnt.alloc(c, 1);
+    const W pw = (W)p;
+    const uint32_t one = 1;
+    if (e == cudaSuccess) e = cudaMemcpyAsync(cls.p.p, &pw, sizeof(W), cudaMemcpyHostToDevice, c->st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(cnt.p, &one, sizeof(one), cudaMemcpyHostToDevice, c->st);
+    SetupArgs<SW> sa;
+    sa.mode = j->mode;
+    sa.a = a.view;
+    sa.b = b.view;
+    sa.nnext0 = 0;
+    if (e == cudaSuccess) {
+        const ClassBuf<W> view = cls.view(cnt.p);
+        if constexpr (sizeof(W) == 4) c->launches += launch_setup32(view, sa, c->st);
+        else if constexpr (sizeof(SW) == 16) c->launches += launch_setup64w(view, sa, c->st);
+        else c->launches += launch_setup64(view, sa, c->st);
+        e = cudaGetLastError();
+    }
+    W h0 = 0, h1 = 0;
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&h0, cls.s0.p, sizeof(W), cudaMemcpyDeviceToHost, c->st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&h1, cls.s1.p, sizeof(W), cudaMemcpyDeviceToHost, c->st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->st);
+    cls.release(c);
+    cnt.release(c);
+    CK(e);
+    // Montgomery form with R = 2^32 (class 32) or 2^64 -> plain
+    const uint64_t rinv = powmod_h(2, (p - 1) - (sizeof(W) == 4 ? 32 : 64), p);
+    s0 = mulmod_h((uint64_t)h0, rinv, p);
+    s1 = mulmod_h((uint64_t)h1, rinv, p);
+    return PFC_OK;
+}
+
+extern "C" int pfc_job_verify_tables(pfc_job *j, uint64_t *table_bytes) {
+    if (!j) return PFC_ERR_ARG;
+    pfc_ctx *c = j->ctx;
+    CK(cudaSetDevice(c->device));
+    CK(cudaStreamSynchronize(c->st));
+    const uint32_t startN = j->nmin - 1;
+    // slow side for the setup programs: k in [2, n0 - 1]
+    SlowProducts sp;
+    int rc = slow_products(c, 2, (uint64_t)startN + 1, sp);
+    if (rc) return rc;
+    uint64_t bytes = 0;
+    struct Form {
+        int form, t;   // setup form, test prime index
+        bool built;
+    } forms[3] = {{0, 0, j->a32.words.p != nullptr && j->pmin < kClassSplit},
+                  {1, 1, j->aw.words.p != nullptr && j->pmax > kClassSplit && j->pmin < kLazyEnd},
+                  {2, 2, j->a64.words.p != nullptr && j->pmax > kLazyEnd}};
+    for (const Form &f : forms) {
+        if (!f.built) continue;
+        const uint64_t p = kVerifyPrime[f.t];
+        uint64_t s0 = 0, s1 = 0;
+        if (f.form == 0) {
+            rc = setup_on_prime<uint32_t, uint32_t>(j, j->a32, j->b32, p, s0, s1);
+            bytes += (j->a32.words.n + j->b32.words.n) * 4;
+        } else if (f.form == 1) {
+            rc = setup_on_prime<uint64_t, W128>(j, j->aw, j->bw, p, s0, s1);
+            bytes += (j->aw.words.n + j->bw.words.n) * 16;
+        } else {
+            rc = setup_on_prime<uint64_t, uint64_t>(j, j->a64, j->b64, p, s0, s1);
+            bytes += (j->a64.words.n + j->b64.words.n) * 8;
+        }
+        if (rc) return rc;
+        const uint64_t P = sp.P[f.t], C = sp.C[f.t], F = mulmod_h(P, C, p);
+        bool ok;
+        switch (j->mode) {
+            case PFC_FACTORIAL: ok = s0 == F; break;
+            case PFC_PRIMORIAL: ok = s0 == P; break;
+            case PFC_COMPOSITORIAL: ok = s0 == C; break;
+            default: ok = s0 == F && s1 == C; break;
+        }
+        if (!ok) return PFC_ERR_VALIDATION;
+    }
+    // walk tables of [nmin, nmax): the primorial's prime list, the
+    // compositorial's prime flags, read back from the device
+    if (j->mode != PFC_FACTORIAL && j->nmax > j->nmin) {
+        SlowProducts rp;
+        rc = slow_products(c, j->nmin, j->nmax, rp);
+        if (rc) return rc;
+        const uint64_t p = kVerifyPrime[2];
+        uint64_t prod = 1, count = 0;
+        if (j->mode == PFC_PRIMORIAL) {
+            std::vector<uint32_t> q(j->h_qlist.size());
+            if (!q.empty())
+                CK(cudaMemcpy(q.data(), j->qlist.p, q.size() * sizeof(uint32_t), cudaMemcpyDeviceToHost));
+            for (uint32_t v : q) prod = mulmod_h(prod, v, p);
+            count = q.size();
+            bytes += q.size() * 4;
+        } else {
+            std::vector<uint32_t> bits(j->primebits.n);
+            CK(cudaMemcpy(bits.data(), j->primebits.p, bits.size() * sizeof(uint32_t), cudaMemcpyDeviceToHost));
+            for (uint32_t k = 0; k < j->nmax - j->nmin; ++k)
+                if ((bits[k >> 5] >> (k & 31)) & 1u) {
+                    prod = mulmod_h(prod, j->nmin + k, p);
+                    ++count;
+                }
+            bytes += bits.size() * 4;
+        }
+        if (count != rp.count || prod != rp.P[2]) return PFC_ERR_VALIDATION;
+    }
+    if (table_bytes) *table_bytes = bytes;
+    return PFC_OK;
+}

@@ -471,6 +471,23 @@ static void run_search(pfc_ctx *ctx, workStatus &st, Search &sd) {
     int rc = pfc_job_create(ctx, mode_bits(st), st.nmin, st.nmax, st.pmin, st.pmax, &job);
     if (rc == PFC_ERR_ARG && st.pmin == st.pmax) job = nullptr;   // empty p range: nothing to sieve
     else if (rc) die_status("pfc_job_create", rc);
+    if (job) {
+        // table self-check once per run (cl_sieve.cpp:917-973,1100-1137,1270-1307)
+        uint64_t bytes = 0;
+        rc = pfc_job_verify_tables(job, &bytes);
+        const char *what = st.factorial && st.compositorial ? "factorial and compositorial"
+                           : st.factorial                   ? "factorial power"
+                           : st.primorial                   ? "primorial prime and product"
+                                                            : "compositorial prime and product";
+        if (rc == PFC_ERR_VALIDATION) {
+            fprintf(stderr, "error: %s table verification failed\n", what);
+            printf("error: %s table verification failed\n", what);
+            exit(EXIT_FAILURE);
+        }
+        if (rc) die_status("pfc_job_verify_tables", rc);
+        fprintf(stderr, "Verified %s tables (%" PRIu64 " bytes)\n", what, bytes);
+        printf("Verified %s tables (%" PRIu64 " bytes)\n", what, bytes);
+    }
     fprintf(stderr, "Starting Sieve...\n");
     printf("Starting Sieve...\n");
     uint64_t term_prev = 0, count_prev = 0;

@@ -119,4 +119,18 @@ int launch_check64(const ClassBuf<uint64_t> &c, const CheckArgs &a, cudaStream_t
 // host helper: the sieve pattern table (kPatEntries masks) and prime list
 void build_pattern_table(uint64_t *pat, uint32_t *primes29);
 
+// Slow products over k in [lo, hi) modulo the self-check test primes
+// (verify.cu): products of the primes and of the composites (plain residues)
+// and the prime count.
+constexpr int kVerifyPrimes = 3;
+constexpr uint64_t kVerifyPrime[kVerifyPrimes] = {2147483647ull, 4611686018427387847ull, 18446744073709551557ull};
+struct SlowProducts {
+    uint64_t P[kVerifyPrimes], C[kVerifyPrimes], count;
+};
+}  // namespace pfc
+struct pfc_ctx;
+namespace pfc {
+int slow_products(pfc_ctx *c, uint64_t lo, uint64_t hi, SlowProducts &out);
+
+
 }  // namespace pfc

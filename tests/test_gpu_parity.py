@@ -126,6 +126,22 @@ def test_class64_regimes_vs_oracle(ctx, mode, lo):
     assert termsum == osum
 
 
+@pytest.mark.parametrize("nmin,nmax,pmin,pmax", [
+    (101, 5000, 10**6, 10**6 + 10**4),                  # class-32 words
+    (3000, 7000, 2**40, 2**40 + 10**4),                  # 128-bit words
+    (3000, 7000, 2**63, 2**63 + 10**4),                  # 64-bit words
+    (2_000_000, 2_000_100, 10**9, 2**33),                # two forms, large n0
+    (101, 102, 2**31 - 10**4, LAZY_END + 10**4),         # all three forms
+])
+@pytest.mark.parametrize("mode", [1, 2, 4, 5])
+def test_table_self_check(ctx, mode, nmin, nmax, pmin, pmax):
+    """Every setup-program form the job built, run by the setup kernel on a
+    test prime, equals the slow products; walk tables match by product and
+    count."""
+    with pfc.Job(ctx, mode, nmin, nmax, pmin, pmax) as job:
+        assert job.verify_tables() > 0
+
+
 def test_wilson_and_small_p(ctx):
     """p <= n: residues fall to 0 and (p-1)!+1 hits are real (self-test 3/6/10/14)."""
     for mode in (1, 2, 4, 5):
