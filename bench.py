@@ -20,9 +20,9 @@ re-verification of every hit, 2-PRP filter and checksum, timed on the host.
 
 The roofline object covers the iterate (walk) kernel, the dominant one.  The
 walk is bound by the integer multiply pipe: each step of a residue chain needs
-a fixed set of multiplies (class 32: one 32x32->64 multiply-add, one
-multiply-low, one multiply-high; class 64 below 2^64/3: three multiply-adds,
-one multiply-low, one multiply-high).  Each kind's throughput is measured in
+a fixed set of multiplies (class 32: two 32x32->64 multiplies and one
+multiply-low; class 64 below 2^64/3: four 32x32->64 multiplies and one
+multiply-low).  Each kind's throughput is measured in
 this run (pfc_bench_int_peak); `achieved` is the walk's steps per second x the
 IMAD-equivalent cost of a step (each multiply weighted by IMAD rate / its own
 rate), `peak` is the IMAD rate, so `frac` is the fraction of time the multiply
@@ -271,9 +271,9 @@ def n_composites(nmin, nmax):
 def step_recipe(cls32, lazy):
     """Multiplies of one walk step (see arith.cuh): redc31s, redc64l, redc64_u32."""
     if cls32:
-        return {"imad_wide": 1, "imad": 1, "mul_hi": 1}
+        return {"imad_wide": 2, "imad": 1}
     if lazy:
-        return {"imad_wide": 3, "imad": 1, "mul_hi": 1}
+        return {"imad_wide": 4, "imad": 1}
     return {"imad_wide": 7, "imad": 2}
 
 
@@ -416,6 +416,7 @@ def run_ours(args, wl, world, rank, local, dist):
     value = pairs_total / (ms_max * 1e-3)
 
     termsum, _ = job.totals()
+    setup_mm = int(job.setup_mulmods(0 if hi <= 2**31 else 1))
     cands_per_step = pairs // args.steps // (wl["nmax"] - wl["nmin"])
     job.close()
 
@@ -505,7 +506,13 @@ def run_ours(args, wl, world, rank, local, dist):
                          "alg_ops_per_step": alg_ops,
                          "kernel_ms_per_step": it_s * 1e3,
                          "peak_source": "measured in this run (pfc_bench_int_peak, 32-bit IMAD chains)",
-                         "int_peaks_tops": {k: v / 1e12 for k, v in peaks.items()}},
+                         "int_peaks_tops": {k: v / 1e12 for k, v in peaks.items()},
+                         # the reference's arithmetic costs 20 IMAD-class operations per
+                         # 64-bit Montgomery multiplication; the same steps at that cost
+                         "frac_at_20_imad_per_mulmod": walk_steps / it_s * 20 / peak},
+            "mulmods": {"walk_per_s": walk_steps * args.steps / (ms_max * 1e-3) * world,
+                        "walk_per_pair": steps_per_cand / (wl["nmax"] - wl["nmin"]),
+                        "setup_per_candidate": setup_mm},
             "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(launches), "clocks": clocks,
             "checksum_terms": "%016X" % termsum,
         }
