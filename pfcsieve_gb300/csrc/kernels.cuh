@@ -77,9 +77,9 @@ struct WalkArgs {
 // size classes: class 32 holds p < 2^31, class 64 the rest
 constexpr uint64_t kClassSplit = 1ull << 31;
 // class-64 segments whose candidates are all below kLazyEnd (3p < 2^64) set
-// up with 128-bit table words; below 2^63 the walk takes lazy steps
+// up with 128-bit table words and walk with lazy one-word steps
 constexpr uint64_t kLazyEnd = 0x5555555555555556ull;
-constexpr uint64_t kLazyWalkEnd = 1ull << 63;
+constexpr uint64_t kLazyWalkEnd = kLazyEnd;
 
 struct CheckArgs {
     unsigned mode;
@@ -107,7 +107,7 @@ int launch_setup64(const ClassBuf<uint64_t> &c, const SetupArgs<uint64_t> &a, cu
 // class 64 below 2^64/3 with 128-bit table words
 int launch_setup64w(const ClassBuf<uint64_t> &c, const SetupArgs<W128> &a, cudaStream_t st);
 int launch_walk32(const ClassBuf<uint32_t> &c, const WalkArgs &a, const HitBuf &h, cudaStream_t st);
-// lazy: every candidate is below 2^63 (the walk then takes lazy one-word steps)
+// lazy: every candidate is below 2^64/3 (the walk then takes lazy one-word steps)
 int launch_walk64(const ClassBuf<uint64_t> &c, const WalkArgs &a, const HitBuf &h, cudaStream_t st, bool lazy);
 // compositorial multipliers of n in [lo, hi): n when composite, 1 when prime
 // (bit k of primebits <-> n = nmin + k); `out` is padded with 1 to a multiple of 16

@@ -24,6 +24,7 @@
 // integer multiplies (IMAD.WIDE, IMAD, IMAD.HI), one compare and conditional
 // add for the reduction, and two compares for the hit test.
 #pragma once
+#include <type_traits>
 #include "arith.cuh"
 #include "kernels.cuh"
 
@@ -40,22 +41,38 @@ constexpr unsigned kFull = 0xffffffffu;
 struct Cls32 {
     using W = uint32_t;
     using M = Mont32;
-    static constexpr int B = 8;           // block length with two candidates per thread
+    static constexpr int B = 16;          // block length with two candidates per thread
     static constexpr int B_FUSED = 16;    // block length of the fused -! -c walk
     static constexpr int NC = 2;          // candidates per thread in single-chain walks
-    struct Tgt {
+    // targets: one register per step (p - T formed in the test) for the
+    // two-candidate walks, which are register-bound; two for the fused walk,
+    // which is issue-bound and saves the add
+    struct TgtA {
+        W t;
+    };
+    struct TgtB {
         W t, nt;
     };
+    template <bool FUSED>
+    using Tgt = typename std::conditional<FUSED, TgtB, TgtA>::type;
     // walk residues signed in (-p, p), p < 2^31; after j+1 steps from r*R,
     // x = r' * R^-j, so the targets are T_j = R^-j
     __device__ static __forceinline__ W target0(const M &) { return 1; }
     __device__ static __forceinline__ W next_target(const M &m, W t) { return m.mul(t, 1); }
-    __device__ static __forceinline__ Tgt mk(const M &m, W t) { return {t, m.p - t}; }
+    __device__ static __forceinline__ void mk(const M &, W t, TgtA &g) { g.t = t; }
+    __device__ static __forceinline__ void mk(const M &m, W t, TgtB &g) {
+        g.t = t;
+        g.nt = m.p - t;
+    }
     __device__ static __forceinline__ W fstep(const M &m, W x, uint32_t n) {
         return (W)redc31s((int32_t)x, n, (int32_t)m.p, m.pinv);
     }
-    // x = +-T (mod p) <=> |x| in {T, p - T}
-    __device__ static __forceinline__ bool fhit(W x, const Tgt &g) {
+    // x = +-T (mod p) <=> |x| in {T, p - T} <=> |x| == T or |x| + T == p
+    __device__ static __forceinline__ bool fhit(const M &m, W x, const TgtA &g) {
+        const uint32_t ax = (uint32_t)abs((int32_t)x);
+        return (ax == g.t) | (ax + g.t == m.p);
+    }
+    __device__ static __forceinline__ bool fhit(const M &, W x, const TgtB &g) {
         const uint32_t ax = (uint32_t)abs((int32_t)x);
         return (ax == g.t) | (ax == g.nt);
     }
@@ -80,14 +97,19 @@ struct Cls64 {
     static constexpr int B = 8;
     static constexpr int B_FUSED = 8;
     static constexpr int NC = 1;
-    struct Tgt {
+    struct TgtB {
         W t, nt;
     };
+    template <bool FUSED>
+    using Tgt = TgtB;
     __device__ static __forceinline__ W target0(const M &) { return 1; }
     __device__ static __forceinline__ W next_target(const M &m, W t) { return m.mul(t, 1); }
-    __device__ static __forceinline__ Tgt mk(const M &m, W t) { return {t, m.p - t}; }
+    __device__ static __forceinline__ void mk(const M &m, W t, TgtB &g) {
+        g.t = t;
+        g.nt = m.p - t;
+    }
     __device__ static __forceinline__ W fstep(const M &m, W x, uint32_t n) { return redc64_u32(x, n, m.p, m.pinv); }
-    __device__ static __forceinline__ bool fhit(W x, const Tgt &g) { return (x == g.t) | (x == g.nt); }
+    __device__ static __forceinline__ bool fhit(const M &, W x, const TgtB &g) { return (x == g.t) | (x == g.nt); }
     __device__ static __forceinline__ W K(const M &m, int r) { return m.mont_R_pow((uint64_t)r); }
     __device__ static __forceinline__ W restore(const M &m, W x, W K) { return m.mul(x, K); }
     __device__ static __forceinline__ W canon(const M &, W x) { return x; }
@@ -108,22 +130,25 @@ struct Cls64 {
 struct Cls64L {
     using W = uint64_t;
     using M = Mont64;
-    static constexpr int B = 8;
-    static constexpr int B_FUSED = 8;
+    static constexpr int B = 16;
+    static constexpr int B_FUSED = 16;
     static constexpr int NC = 1;
-    struct Tgt {
-        uint32_t a, b, c, d;
+    struct TgtA {
+        uint32_t u;  // low 32 bits of U; the four lifts are formed in the test
     };
+    template <bool FUSED>
+    using Tgt = TgtA;
     __device__ static __forceinline__ W canon(const M &m, W x) { return x >= m.p ? x - m.p : x; }
     __device__ static __forceinline__ W target0(const M &m) { return canon(m, redc64l(m.one, 1u, m.p, m.q32)); }
     __device__ static __forceinline__ W next_target(const M &m, W t) { return canon(m, redc64l(t, 1u, m.p, m.q32)); }
-    __device__ static __forceinline__ Tgt mk(const M &m, W t) {
-        return {(uint32_t)t, (uint32_t)(t + m.p), (uint32_t)(m.p - t), (uint32_t)(2 * m.p - t)};
-    }
+    __device__ static __forceinline__ void mk(const M &, W t, TgtA &g) { g.u = (uint32_t)t; }
     __device__ static __forceinline__ W fstep(const M &m, W x, uint32_t n) { return redc64l(x, n, m.p, m.q32); }
-    __device__ static __forceinline__ bool fhit(W x, const Tgt &g) {
-        const uint32_t lo = (uint32_t)x;
-        return (lo == g.a) | (lo == g.b) | (lo == g.c) | (lo == g.d);
+    // low words: x in {U, U + p} <=> lo(x) - lo(U) in {0, lo(p)};
+    //            x in {p - U, 2p - U} <=> lo(x) + lo(U) in {lo(p), lo(2p)}
+    __device__ static __forceinline__ bool fhit(const M &m, W x, const TgtA &g) {
+        const uint32_t lo = (uint32_t)x, pl = (uint32_t)m.p;
+        const uint32_t d = lo - g.u, e = lo + g.u;
+        return (d == 0u) | (d == pl) | (e == pl) | (e == 2u * pl);
     }
     // r lazy steps leave r' * 2^64 * 2^(-32r): K = 2^(32r) * 2^64 mod p, the
     // Montgomery form of 2^(32r), from Mont(2^(64k)) = mont_R_pow(k)
@@ -131,8 +156,13 @@ struct Cls64L {
         const W k = m.mont_R_pow((uint64_t)((r + 1) >> 1));
         return (r & 1) ? canon(m, redc64l(k, 1u, m.p, m.q32)) : k;
     }
-    // x < 2p and K < p with p < 2^63 keep x*K < p*2^64: canonical result
-    __device__ static __forceinline__ W restore(const M &m, W x, W K) { return m.mul(x, K); }
+    // x*K*2^-64 by two lazy one-limb rounds (x < 2p, any K < 2^64, 3p < 2^64),
+    // back to [0, 2p) by one conditional subtraction
+    __device__ static __forceinline__ W restore(const M &m, W x, W K) {
+        uint64_t c = redc64l(x, (uint32_t)K, m.p, m.q32);
+        c = cios_round(c, x, (uint32_t)(K >> 32), m.p, m.q32);
+        return c >= 2 * m.p ? c - m.p : c;
+    }
     __device__ static __forceinline__ W step(const M &m, W s, uint32_t n) { return canon(m, redc64l(s, n, m.p, m.q32)); }
     // setup (p < 2^64/3): 128-bit table words, each lowering the power of
     // R = 2^64 by two; values stay in [0, 2p), canonical before a squaring
@@ -256,14 +286,14 @@ __device__ __forceinline__ void walk_streams(const typename T::M (&m)[NC], typen
     using W = typename T::W;
     constexpr int B = FUSED ? T::B_FUSED : T::B;
     constexpr int NS = FUSED ? 2 : NC;
-    typename T::Tgt tg[NC][B];
+    typename T::template Tgt<FUSED> tg[NC][B];
     W K[NC];
 #pragma unroll
     for (int s = 0; s < NC; ++s) {
         W t = T::target0(m[s]);
 #pragma unroll
         for (int j = 0; j < B; ++j) {
-            tg[s][j] = T::mk(m[s], t);
+            T::mk(m[s], t, tg[s][j]);
             if (j + 1 < B) t = T::next_target(m[s], t);
         }
         K[s] = T::K(m[s], B);
@@ -287,12 +317,12 @@ __device__ __forceinline__ void walk_streams(const typename T::M (&m)[NC], typen
             if (FUSED) {
                 x[0] = T::fstep(m[0], x[0], mv[j]);
                 x[NS - 1] = T::fstep(m[0], x[NS - 1], cv[j]);
-                any |= T::fhit(x[0], tg[0][j]) | T::fhit(x[NS - 1], tg[0][j]);
+                any |= T::fhit(m[0], x[0], tg[0][j]) | T::fhit(m[0], x[NS - 1], tg[0][j]);
             } else {
 #pragma unroll
                 for (int s = 0; s < NC; ++s) {
                     x[s] = T::fstep(m[s], x[s], mv[j]);
-                    any |= T::fhit(x[s], tg[s][j]);
+                    any |= T::fhit(m[s], x[s], tg[s][j]);
                 }
             }
         }
@@ -329,12 +359,12 @@ __device__ __forceinline__ void walk_streams(const typename T::M (&m)[NC], typen
                     const uint32_t mul1 = __ldg(mult1 + (k - a.base) + j);
                     x[0] = T::fstep(m[0], x[0], mul0);
                     x[NS - 1] = T::fstep(m[0], x[NS - 1], mul1);
-                    any |= T::fhit(x[0], tg[0][j]) | T::fhit(x[NS - 1], tg[0][j]);
+                    any |= T::fhit(m[0], x[0], tg[0][j]) | T::fhit(m[0], x[NS - 1], tg[0][j]);
                 } else {
 #pragma unroll
                     for (int s = 0; s < NC; ++s) {
                         x[s] = T::fstep(m[s], x[s], mul0);
-                        any |= T::fhit(x[s], tg[s][j]);
+                        any |= T::fhit(m[s], x[s], tg[s][j]);
                     }
                 }
             }
