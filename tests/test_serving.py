@@ -1,0 +1,69 @@
+"""Host logic of the mixed workload and the request loop (no GPU needed).
+
+* mixed_jobs draws the mixed workload deterministically from its seed and
+  keeps every search inside the ranges the C ABI accepts;
+* poisson_arrivals is a seeded Poisson process at the requested rate;
+* fcfs_latencies is the latency of a single first-come-first-served server,
+  checked against a direct event simulation.
+"""
+import math
+
+import numpy as np
+import pytest
+
+serving = pytest.importorskip("pfcsieve_gb300.serving")
+
+
+def test_mixed_jobs_are_deterministic_and_in_range():
+    a = serving.mixed_jobs(512, seed=0)
+    b = serving.mixed_jobs(512, seed=0)
+    assert a == b
+    assert serving.mixed_jobs(512, seed=1) != a
+    assert len(a) == 512
+    for s in a:
+        assert s.mode in (1, 2, 4)
+        assert 101 <= s.nmin < 10**7
+        assert 10**3 <= s.nmax - s.nmin <= 10**6
+        assert s.nmax < 2**31
+        assert 10**5 <= s.pmax - s.pmin <= 10**8
+        assert 10**8 <= s.pmin <= 2**63
+        assert s.pmax < 2**64
+
+
+def test_mixed_jobs_distribution():
+    jobs = serving.mixed_jobs(4096, seed=3)
+    modes = np.bincount([s.mode for s in jobs], minlength=5)
+    for m in (1, 2, 4):
+        assert abs(modes[m] / len(jobs) - 1 / 3) < 0.04
+    # log-uniform lengths: the median is near the geometric mean of the bounds
+    nl = np.median([math.log10(s.nmax - s.nmin) for s in jobs])
+    pl = np.median([math.log10(s.pmax - s.pmin) for s in jobs])
+    assert abs(nl - 4.5) < 0.15 and abs(pl - 6.5) < 0.15
+
+
+def test_first_searches_of_a_seed_are_a_prefix():
+    """The benchmark's sample is the first k searches of the 512-search set."""
+    assert serving.mixed_jobs(512, seed=0)[:32] == serving.mixed_jobs(32, seed=0)
+
+
+def test_poisson_arrivals():
+    t = serving.poisson_arrivals(20000, 200.0, seed=1)
+    assert np.all(np.diff(t) > 0)
+    gaps = np.diff(np.concatenate([[0.0], t]))
+    assert abs(gaps.mean() - 1 / 200.0) < 2e-4
+    assert abs(gaps.std() - 1 / 200.0) < 3e-4          # exponential: std == mean
+    assert np.array_equal(t, serving.poisson_arrivals(20000, 200.0, seed=1))
+
+
+def test_fcfs_latencies_match_an_event_simulation():
+    rng = np.random.default_rng(5)
+    arr = np.cumsum(rng.exponential(0.1, 300))
+    svc = rng.exponential(0.12, 300)
+    lat = serving.fcfs_latencies(arr, svc)
+    clock = 0.0
+    for i in range(300):
+        start = max(clock, arr[i])
+        clock = start + svc[i]
+        assert abs(lat[i] - (clock - arr[i])) < 1e-9
+    # an idle server: latency is the service time
+    assert np.allclose(serving.fcfs_latencies([0.0, 10.0], [1.0, 2.0]), [1.0, 2.0])
