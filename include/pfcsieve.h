@@ -284,6 +284,12 @@ int pfc_batch_set_iteration_work(pfc_batch *b, double candidate_steps);
  * LATENCY: half of each iteration goes to the searches with the least work
  * left (shortest remaining work first), for request streams where the
  * median wait matters. */
+/* Capacity of the batch's shared hit list per iteration (default 2^20
+ * records), settable while no search is on the device.  When the hits of an
+ * iteration exceed it, every search of that iteration is redone alone with
+ * pfc_job_run after it finishes, so results never depend on this size. */
+int pfc_batch_set_hit_capacity(pfc_batch *b, uint32_t records);
+
 #define PFC_BATCH_THROUGHPUT 0
 #define PFC_BATCH_LATENCY    1
 int pfc_batch_set_policy(pfc_batch *b, int policy);

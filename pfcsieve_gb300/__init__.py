@@ -115,6 +115,7 @@ def lib():
             "pfc_batch_iterations": (u64, [vp]),
             "pfc_batch_set_iteration_work": (ctypes.c_int, [vp, ctypes.c_double]),
             "pfc_batch_set_policy": (ctypes.c_int, [vp, ctypes.c_int]),
+            "pfc_batch_set_hit_capacity": (ctypes.c_int, [vp, u32]),
             "pfc_batch_timing": (ctypes.c_int, [vp, P(BatchTimes)]),
         }
         for name, (res, args) in sig.items():
@@ -352,6 +353,9 @@ class Batch:
 
     def release(self, job_id):
         _ck(lib().pfc_batch_release(self.h, job_id), "pfc_batch_release")
+
+    def set_hit_capacity(self, records):
+        _ck(lib().pfc_batch_set_hit_capacity(self.h, int(records)), "pfc_batch_set_hit_capacity")
 
     @property
     def iterations(self):

@@ -15,6 +15,7 @@
 #include <cstdio>
 #include <cstring>
 #include <new>
+#include <type_traits>
 #include <vector>
 
 #include "devmem.hpp"
@@ -32,7 +33,7 @@ struct pfc_job {
 
     DevProg<uint32_t> a32, b32;
     DevProg<uint64_t> a64, b64;   // class 64 at or above 2^64/3 (64-bit words)
-    DevProg<W128> aw, bw;         // class 64 below 2^64/3 (128-bit words)
+    DevProg<WideWord> aw, bw;     // class 64 below 2^64/3 (256-bit words)
     uint64_t setup_mulmods32 = 0, setup_mulmods64 = 0;
     DArr<uint32_t> primebits;
     DArr<uint32_t> qlist;
@@ -204,7 +205,7 @@ extern "C" int pfc_job_create(pfc_ctx *c, unsigned mode, uint32_t nmin, uint32_t
     const std::vector<uint32_t> below(primes.begin(), std::upper_bound(primes.begin(), primes.end(), startN));
     HostProg<uint32_t> a32, b32;
     HostProg<uint64_t> a64, b64;
-    HostProg<W128> aw, bw;
+    HostProg<WideWord> aw, bw;
     const bool need32 = pmin < kClassSplit;
     const bool needw = pmax > kClassSplit && pmin < kLazyEnd;
     const bool need64 = pmax > kLazyEnd;
@@ -327,7 +328,7 @@ static int enqueue_setup(pfc_job *j) {
     s64.a = j->a64.view;
     s64.b = j->b64.view;
     s64.nnext0 = 0;
-    SetupArgs<W128> sw;
+    SetupArgs<WideWord> sw;
     sw.mode = j->mode;
     sw.a = j->aw.view;
     sw.b = j->bw.view;
@@ -686,7 +687,7 @@ static int setup_on_prime(pfc_job *j, const DevProg<SW> &a, const DevProg<SW> &b
     if (e == cudaSuccess) {
         const ClassBuf<W> view = cls.view(cnt.p);
         if constexpr (sizeof(W) == 4) c->launches += launch_setup32(view, sa, c->st);
-        else if constexpr (sizeof(SW) == 16) c->launches += launch_setup64w(view, sa, c->st);
+        else if constexpr (std::is_same<SW, WideWord>::value) c->launches += launch_setup64w(view, sa, c->st);
         else c->launches += launch_setup64(view, sa, c->st);
         e = cudaGetLastError();
     }
@@ -729,8 +730,8 @@ extern "C" int pfc_job_verify_tables(pfc_job *j, uint64_t *table_bytes) {
             rc = setup_on_prime<uint32_t, uint32_t>(j, j->a32, j->b32, p, s0, s1);
             bytes += (j->a32.words.n + j->b32.words.n) * 4;
         } else if (f.form == 1) {
-            rc = setup_on_prime<uint64_t, W128>(j, j->aw, j->bw, p, s0, s1);
-            bytes += (j->aw.words.n + j->bw.words.n) * 16;
+            rc = setup_on_prime<uint64_t, WideWord>(j, j->aw, j->bw, p, s0, s1);
+            bytes += (j->aw.words.n + j->bw.words.n) * sizeof(WideWord);
         } else {
             rc = setup_on_prime<uint64_t, uint64_t>(j, j->a64, j->b64, p, s0, s1);
             bytes += (j->a64.words.n + j->b64.words.n) * 8;

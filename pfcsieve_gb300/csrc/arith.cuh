@@ -6,8 +6,8 @@
 //             walk residues are signed, in (-p, p) (redc31s).
 //   class 64: p >= 2^31, Montgomery with R = 2^64; below 2^64/3 the walk
 //             takes lazy one-word steps with R = 2^32 and residues in
-//             [0, 2p) (redc64l), and the setup multiplies by 128-bit table
-//             words in four lazy rounds (mul_word128).
+//             [0, 2p) (redc64l), and the setup multiplies by 256-bit table
+//             words in eight lazy rounds (mul_wide_word).
 //
 // The reference keeps every residue in Montgomery form with R = 2^64
 // (kernels/iterate.cl:44-50: m_mul(a,b) = a*b/2^64 mod p in [0,p)).  Values
@@ -201,17 +201,16 @@ __device__ __forceinline__ uint64_t cios_round(uint64_t c, uint64_t s, uint32_t 
     return r;
 }
 
-// s*W*2^-128 (mod p) for a 128-bit word W given as four 32-bit limbs
-// (little-endian), s in [0, 2p), p < 2^64/3: one plain lazy round (c = 0)
-// and three accumulating rounds, then one conditional subtraction: result in
-// [0, 2p).  Two multiplications by 64-bit words would cost about twice the
-// multiply-pipe time for the same number of factor bits.
-__device__ __forceinline__ uint64_t mul_word128(uint64_t s, uint32_t w0, uint32_t w1, uint32_t w2, uint32_t w3,
-                                                uint64_t p, uint32_t q) {
-    uint64_t c = redc64l(s, w0, p, q);
-    c = cios_round(c, s, w1, p, q);
-    c = cios_round(c, s, w2, p, q);
-    c = cios_round(c, s, w3, p, q);
+// s*W*2^(-32L) (mod p) for an L-limb word W (32-bit limbs, little-endian),
+// s in [0, 2p), p < 2^64/3: one plain lazy round (c = 0) and L-1
+// accumulating rounds, then one conditional subtraction: result in [0, 2p).
+// The multiply-pipe cost per factor bit is about half that of multiplying by
+// 64-bit words with the 64x64 Montgomery product.
+template <int L>
+__device__ __forceinline__ uint64_t mul_wide_word(uint64_t s, const uint32_t (&w)[L], uint64_t p, uint32_t q) {
+    uint64_t c = redc64l(s, w[0], p, q);
+#pragma unroll
+    for (int k = 1; k < L; ++k) c = cios_round(c, s, w[k], p, q);
     return c >= 2 * p ? c - p : c;
 }
 

@@ -315,7 +315,7 @@ struct BatchJob {
     int prep_rc = PFC_OK;
     std::vector<uint32_t> words32, cmult, qlist;
     std::vector<uint64_t> words64;   // class 64 at or above 2^64/3
-    std::vector<W128> words128;      // class 64 below 2^64/3
+    std::vector<WideWord> wordsw;      // class 64 below 2^64/3
     std::vector<SetupSeg> segs32, segs64;
     uint32_t nsetup32 = 0, nsetup64 = 0;
     uint64_t c32a = 0, c32b = 0, c64a = 0, c64b = 0;
@@ -325,7 +325,7 @@ struct BatchJob {
     // device
     DArr<uint32_t> d_words32, d_cmult, d_qlist;
     DArr<uint64_t> d_words64;
-    DArr<W128> d_words128;
+    DArr<WideWord> d_wordsw;
     DArr<SetupSeg> d_segs32, d_segs64;
     DevClass<uint32_t> c32;
     DevClass<uint64_t> c64;
@@ -394,10 +394,10 @@ static void prepare_job(BatchJob *j, const std::vector<uint32_t> &cache) {
     const std::vector<uint32_t> below(primes.begin(), std::upper_bound(primes.begin(), primes.end(), startN));
     const unsigned mode = j->mode;
     const bool fc = mode == (PFC_FACTORIAL | PFC_COMPOSITORIAL);
-    const bool wide = j->pmax <= kLazyEnd;  // class 64 with 128-bit words
+    const bool wide = j->pmax <= kLazyEnd;  // class 64 with 256-bit words
     HostProg<uint32_t> a32, b32;
     HostProg<uint64_t> a64, b64;
-    HostProg<W128> aw, bw;
+    HostProg<WideWord> aw, bw;
     const bool ok = build_progs(mode, startN, primes, below, a32, b32) &&
                     (wide ? build_progs(mode, startN, primes, below, aw, bw)
                           : build_progs(mode, startN, primes, below, a64, b64));
@@ -406,7 +406,7 @@ static void prepare_job(BatchJob *j, const std::vector<uint32_t> &cache) {
         return;
     }
     j->nsetup32 = append_prog(a32, 0, j->segs32, j->words32);
-    j->nsetup64 = wide ? append_prog(aw, 0, j->segs64, j->words128) : append_prog(a64, 0, j->segs64, j->words64);
+    j->nsetup64 = wide ? append_prog(aw, 0, j->segs64, j->wordsw) : append_prog(a64, 0, j->segs64, j->words64);
     j->c32a = a32.corr;
     j->c64a = wide ? aw.corr : a64.corr;
     if (fc) {
@@ -414,7 +414,7 @@ static void prepare_job(BatchJob *j, const std::vector<uint32_t> &cache) {
         j->segs32.push_back({j->nsetup32++, 2u, 0u, 1u});
         j->segs64.push_back({j->nsetup64++, 2u, 0u, 1u});
         j->nsetup32 = append_prog(b32, j->nsetup32, j->segs32, j->words32);
-        j->nsetup64 = wide ? append_prog(bw, j->nsetup64, j->segs64, j->words128)
+        j->nsetup64 = wide ? append_prog(bw, j->nsetup64, j->segs64, j->wordsw)
                            : append_prog(b64, j->nsetup64, j->segs64, j->words64);
         j->c32b = b32.corr;
         j->c64b = wide ? bw.corr : b64.corr;
@@ -523,7 +523,7 @@ void release_device(pfc_batch *b, BatchJob *j) {
     pfc_ctx *c = b->ctx;
     j->d_words32.release(c);
     j->d_words64.release(c);
-    j->d_words128.release(c);
+    j->d_wordsw.release(c);
     j->d_segs32.release(c);
     j->d_segs64.release(c);
     j->d_cmult.release(c);
@@ -561,7 +561,7 @@ int upload_job(pfc_batch *b, BatchJob *j) {
     pfc_ctx *c = b->ctx;
     cudaError_t e = j->d_words32.upload(c, j->words32);
     if (e == cudaSuccess) e = j->d_words64.upload(c, j->words64);
-    if (e == cudaSuccess) e = j->d_words128.upload(c, j->words128);
+    if (e == cudaSuccess) e = j->d_wordsw.upload(c, j->wordsw);
     if (e == cudaSuccess) e = j->d_segs32.upload(c, j->segs32);
     if (e == cudaSuccess) e = j->d_segs64.upload(c, j->segs64);
     if (e == cudaSuccess) e = j->d_cmult.upload(c, j->cmult);
@@ -660,7 +660,7 @@ int admit_prepared(pfc_batch *b) {
         j->pos64 = n64 ? 0 : j->tot64;
         v32[f] = job_view<uint32_t>(b, j, j->c32, 0, j->d_words32.p, j->d_segs32, j->segs32.size(), j->c32a,
                                     j->c32b, j->nsetup32);
-        const void *w64 = j->pmax <= kLazyEnd ? (const void *)j->d_words128.p : (const void *)j->d_words64.p;
+        const void *w64 = j->pmax <= kLazyEnd ? (const void *)j->d_wordsw.p : (const void *)j->d_words64.p;
         v64[f] = job_view<uint64_t>(b, j, j->c64, 1, w64, j->d_segs64, j->segs64.size(), j->c64a, j->c64b,
                                     j->nsetup64);
         CK(cudaMemcpyAsync(b->jobs32.p + j->slot, &v32[f], sizeof(v32[f]), cudaMemcpyHostToDevice, c->st));
@@ -671,7 +671,7 @@ int admit_prepared(pfc_batch *b) {
     for (BatchJob *j : fresh) {
         free_vec(j->words32);  // on the device now
         free_vec(j->words64);
-        free_vec(j->words128);
+        free_vec(j->wordsw);
         free_vec(j->segs32);
         free_vec(j->segs64);
         free_vec(j->cmult);
@@ -686,14 +686,14 @@ int admit_prepared(pfc_batch *b) {
 // Returns the window length used.
 // Cost of timeline positions in IMAD-equivalent multiplies per candidate
 // (measured multiply-pipe rates: class-32 step 6; class-64 lazy step 10.5
-// plus its share of the block restore; a 128-bit setup word four lazy rounds)
+// plus its share of the block restore; a 256-bit setup word eight lazy rounds)
 struct PosCost {
     double setup, walk;
 };
 static PosCost pos_cost(const BatchJob *j, bool cls64) {
     const double chains = j->mode == (PFC_FACTORIAL | PFC_COMPOSITORIAL) ? 2.0 : 1.0;
     if (!cls64) return {6.0, 6.0 * chains};
-    if (j->pmax <= kLazyEnd) return {45.0, 13.0 * chains};
+    if (j->pmax <= kLazyEnd) return {85.0, 12.0 * chains};
     return {60.0, 30.0 * chains};
 }
 
@@ -1128,6 +1128,16 @@ extern "C" int pfc_batch_timing(pfc_batch *b, pfc_batch_times *t) {
     t->admit_s = b->admit_s;
     t->iterations = b->iterations;
     t->tasks = b->tasks;
+    return PFC_OK;
+}
+
+extern "C" int pfc_batch_set_hit_capacity(pfc_batch *b, uint32_t records) {
+    if (!b || records == 0 || !b->running.empty() || !b->ready.empty()) return b ? PFC_ERR_STATE : PFC_ERR_ARG;
+    pfc_ctx *c = b->ctx;
+    CK(cudaSetDevice(c->device));
+    CK(cudaStreamSynchronize(c->st));
+    CK(b->hits.alloc(c, records));
+    CK(b->tags.alloc(c, records));
     return PFC_OK;
 }
 

@@ -84,15 +84,11 @@ uint64_t HostProg<W>::mulmods() const {
 
 template <class W>
 static inline u128 word_max() { return (u128)(W)~(W)0; }
-template <>
-inline u128 word_max<W128>() { return ~(u128)0; }
 template <class W>
 static inline W to_word(u128 v) { return (W)v; }
-template <>
-inline W128 to_word<W128>(u128 v) { return W128{(uint64_t)v, (uint64_t)(v >> 64)}; }
 // R = 2^64 powers a word removes (R = 2^32 for the class-32 words)
 template <class W>
-static constexpr int word_drift() { return sizeof(W) == 16 ? 2 : 1; }
+static constexpr int word_drift() { return sizeof(W) == sizeof(WideWord) ? kWideLimbs / 2 : 1; }
 
 // greedy: consecutive factors multiplied while the product fits a word
 template <class W>
@@ -103,6 +99,30 @@ static void pack_words(const std::vector<uint32_t> &f, std::vector<W> &words) {
         u128 acc = f[i++];
         while (i < f.size() && acc <= lim / f[i]) acc *= f[i++];
         words.push_back(to_word<W>(acc));
+    }
+}
+
+// 256-bit words: the product kept as eight 32-bit limbs, a factor joining
+// while the product still fits
+template <>
+void pack_words<WideWord>(const std::vector<uint32_t> &f, std::vector<WideWord> &words) {
+    size_t i = 0;
+    while (i < f.size()) {
+        WideWord acc{};
+        acc.limb[0] = f[i++];
+        while (i < f.size()) {
+            WideWord next{};
+            uint64_t carry = 0;
+            for (int k = 0; k < kWideLimbs; ++k) {
+                const uint64_t t = (uint64_t)acc.limb[k] * f[i] + carry;
+                next.limb[k] = (uint32_t)t;
+                carry = t >> 32;
+            }
+            if (carry) break;  // would not fit in 256 bits
+            acc = next;
+            ++i;
+        }
+        words.push_back(acc);
     }
 }
 
@@ -175,13 +195,13 @@ bool build_product_prog(const std::vector<uint32_t> &factors, HostProg<W> &out) 
 
 template struct HostProg<uint32_t>;
 template struct HostProg<uint64_t>;
-template struct HostProg<W128>;
+template struct HostProg<WideWord>;
 template bool build_power_prog<uint32_t>(uint32_t, uint32_t, const std::vector<uint32_t> &, HostProg<uint32_t> &);
 template bool build_power_prog<uint64_t>(uint32_t, uint32_t, const std::vector<uint32_t> &, HostProg<uint64_t> &);
-template bool build_power_prog<W128>(uint32_t, uint32_t, const std::vector<uint32_t> &, HostProg<W128> &);
+template bool build_power_prog<WideWord>(uint32_t, uint32_t, const std::vector<uint32_t> &, HostProg<WideWord> &);
 template bool build_product_prog<uint32_t>(const std::vector<uint32_t> &, HostProg<uint32_t> &);
 template bool build_product_prog<uint64_t>(const std::vector<uint32_t> &, HostProg<uint64_t> &);
-template bool build_product_prog<W128>(const std::vector<uint32_t> &, HostProg<W128> &);
+template bool build_product_prog<WideWord>(const std::vector<uint32_t> &, HostProg<WideWord> &);
 
 // ------------------------------------------------------- host Montgomery
 

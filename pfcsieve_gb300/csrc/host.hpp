@@ -6,10 +6,11 @@
 
 namespace pfc {
 
-// 128-bit setup table word (class 64 below 2^64/3): little-endian, read on the
-// device as four 32-bit limbs
-struct alignas(16) W128 {
-    uint64_t lo, hi;
+// 256-bit setup table word (class 64 below 2^64/3): eight little-endian
+// 32-bit limbs, read on the device with two 16-byte loads
+constexpr int kWideLimbs = 8;
+struct alignas(16) WideWord {
+    uint32_t limb[kWideLimbs];
 };
 
 // primes p with lo <= p <= hi (segmented odd-only sieve; replaces the
@@ -20,7 +21,7 @@ std::vector<uint32_t> primes_between(uint32_t lo, uint32_t hi);
 // Setup program on the host: words, groups {begin, end, squarings}, final
 // squarings and the drift correction exponent (see kernels.cuh Prog).  Each
 // 32- or 64-bit word lowers the power of R of the device value by one, each
-// 128-bit word by two.
+// 256-bit word by four.
 template <class W>
 struct HostProg {
     std::vector<W> words;

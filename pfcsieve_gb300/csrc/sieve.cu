@@ -133,7 +133,7 @@ int launch_setup64(const ClassBuf<uint64_t> &c, const SetupArgs<uint64_t> &a, cu
     setup_kernel<Cls64><<<grid_for(c.cap), 256, 0, st>>>(c, a);
     return 1;
 }
-int launch_setup64w(const ClassBuf<uint64_t> &c, const SetupArgs<W128> &a, cudaStream_t st) {
+int launch_setup64w(const ClassBuf<uint64_t> &c, const SetupArgs<WideWord> &a, cudaStream_t st) {
     if (!c.cap) return 0;
     setup_kernel<Cls64L><<<grid_for(c.cap), 256, 0, st>>>(c, a);
     return 1;

@@ -164,12 +164,11 @@ struct Cls64L {
         return c >= 2 * m.p ? c - m.p : c;
     }
     __device__ static __forceinline__ W step(const M &m, W s, uint32_t n) { return canon(m, redc64l(s, n, m.p, m.q32)); }
-    // setup (p < 2^64/3): 128-bit table words, each lowering the power of
-    // R = 2^64 by two; values stay in [0, 2p), canonical before a squaring
-    using SW = W128;
+    // setup (p < 2^64/3): 256-bit table words, each lowering the power of
+    // R = 2^64 by four; values stay in [0, 2p), canonical before a squaring
+    using SW = WideWord;
     __device__ static __forceinline__ W word(const M &m, W s, const SW &w) {
-        return mul_word128(s, (uint32_t)w.lo, (uint32_t)(w.lo >> 32), (uint32_t)w.hi, (uint32_t)(w.hi >> 32), m.p,
-                           m.q32);
+        return mul_wide_word<kWideLimbs>(s, w.limb, m.p, m.q32);
     }
     __device__ static __forceinline__ W sq(const M &m, W s) {
         s = canon(m, s);
@@ -181,9 +180,10 @@ struct Cls64L {
 
 template <class W>
 __device__ __forceinline__ W ldg(const W *p) { return __ldg(p); }
-__device__ __forceinline__ W128 ldg(const W128 *p) {
-    const uint4 v = __ldg(reinterpret_cast<const uint4 *>(p));
-    return W128{(uint64_t)v.x | ((uint64_t)v.y << 32), (uint64_t)v.z | ((uint64_t)v.w << 32)};
+__device__ __forceinline__ WideWord ldg(const WideWord *p) {
+    const uint4 *v = reinterpret_cast<const uint4 *>(p);
+    const uint4 a = __ldg(v), b = __ldg(v + 1);
+    return WideWord{{a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w}};
 }
 
 // Evaluate a setup program from Montgomery-form `acc` (see kernels.cuh Prog).

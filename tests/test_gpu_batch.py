@@ -149,3 +149,29 @@ def test_latency_policy_gives_the_same_results(ctx):
         # the largest search of the mix (by candidates x n) is not among the first to finish
         big = max(range(len(MIX)), key=lambda i: (MIX[i][4] - MIX[i][3]) * (MIX[i][2] - MIX[i][1]))
         assert finished.index(ids[big]) >= len(MIX) // 2
+
+
+def test_hit_overflow_reruns_the_searches_alone(ctx):
+    """A hit list too small for an iteration's hits: the searches of that
+    iteration are redone alone, and every result still equals the stand-alone
+    one.  (p <= n makes every candidate hit: Wilson's theorem.)"""
+    cases = [MIX[1], (5, 101, 6000, 3, 6000), MIX[3]]
+    with pfc.Batch(ctx) as b:
+        b.set_hit_capacity(64)
+        ids = [b.submit(*c) for c in cases]
+        b.run()
+        for case, jid in zip(cases, ids):
+            got = batched(b, jid)
+            want = alone(ctx, case)
+            assert got[:2] == want[:2], case
+            assert np.array_equal(got[2], want[2]), case
+        assert len(got[2]) > 64 or len(batched(b, ids[1])[2]) > 64
+
+
+def test_hit_capacity_is_fixed_while_searches_run(ctx):
+    with pfc.Batch(ctx, iteration_work=1e8) as b:
+        b.submit(*MIX[0])
+        b.step()
+        with pytest.raises(pfc.PFCError):
+            b.set_hit_capacity(128)
+        b.run()
