@@ -369,6 +369,9 @@ def run_ours(args, wl, world, rank, local, dist):
     lo, hi = shard(wl, rank)
     ctx = pfc.Context(local)
     name, sms = ctx.device_info()
+    ctx.autotune()
+    tuned = {"%s/%s" % (c, "fused" if f else "single"): "nc=%d b=%d" % ctx.walk_variant(i, f)[1:]
+             for i, c in ((0, "class32"), (1, "class64-lazy")) for f in (0, 1)}
     stream = torch.cuda.ExternalStream(ctx.stream, device=torch.device("cuda", local))
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
     job = pfc.Job(ctx, wl["mode"], wl["nmin"], wl["nmax"], lo, hi)
@@ -495,7 +498,7 @@ def run_ours(args, wl, world, rank, local, dist):
                        "pairs_per_step": int(pairs_total // args.steps),
                        "l2": "256 MB buffer overwritten before each step (candidate state < L2)",
                        "parallelism": "p-range shards, one per GPU" if world > 1 else "1 GPU",
-                       "device": name, "sms": sms},
+                       "device": name, "sms": sms, "walk_variants": tuned},
             "roofline": {"bound": "int (multiply pipe)", "achieved": achieved / 1e12, "peak": peak / 1e12,
                          "unit": "Tops/s IMAD-equivalent (IMAD.WIDE, IMAD.HI weighted by measured rates)",
                          "frac": achieved / peak, "traffic": traffic,

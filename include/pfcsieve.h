@@ -305,6 +305,21 @@ typedef struct {
 } pfc_batch_times;
 int pfc_batch_timing(pfc_batch *b, pfc_batch_times *t);
 
+/* ------------------------------------------------------------ autotuning */
+
+/* Walk variants: candidates per thread and block length of the walk kernel,
+ * per size class (0: p < 2^31; 1: 2^31 <= p < 2^64/3, lazy arithmetic; 2: the
+ * rest) and walk kind (fused = 1 for the combined search).  All variants give
+ * the same results.  pfc_autotune times each variant of classes 0 and 1 on a
+ * synthetic search on this device (about 0.1 s) and keeps the fastest in the
+ * context; `report` (may be NULL) receives one line per variant.  Without it
+ * the context uses variant 0, the fastest measured on GB300.  The reference
+ * sizes its launches by timing the GPU too (profileGPU, cl_sieve.cpp:669-769)
+ * but has no kernel variants. */
+int pfc_autotune(pfc_ctx *ctx, char *report, size_t cap);
+int pfc_ctx_set_walk_variant(pfc_ctx *ctx, int cls, int fused, int variant);
+int pfc_ctx_walk_variant(pfc_ctx *ctx, int cls, int fused, int *variant, int *nc, int *block);
+
 /* ------------------------------------------------------------ measurement */
 
 /* Throughput of the integer pipes on `device`, in operations per second:

@@ -116,6 +116,10 @@ def lib():
             "pfc_batch_set_iteration_work": (ctypes.c_int, [vp, ctypes.c_double]),
             "pfc_batch_set_policy": (ctypes.c_int, [vp, ctypes.c_int]),
             "pfc_batch_set_hit_capacity": (ctypes.c_int, [vp, u32]),
+            "pfc_autotune": (ctypes.c_int, [vp, ctypes.c_char_p, sz]),
+            "pfc_ctx_set_walk_variant": (ctypes.c_int, [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int]),
+            "pfc_ctx_walk_variant": (ctypes.c_int, [vp, ctypes.c_int, ctypes.c_int, P(ctypes.c_int),
+                                                    P(ctypes.c_int), P(ctypes.c_int)]),
             "pfc_batch_timing": (ctypes.c_int, [vp, P(BatchTimes)]),
         }
         for name, (res, args) in sig.items():
@@ -173,6 +177,23 @@ class Context:
         a, b = ctypes.c_uint64(0), ctypes.c_uint64(0)
         _ck(lib().pfc_ctx_transfer_bytes(self.h, ctypes.byref(a), ctypes.byref(b)), "transfer_bytes")
         return a.value, b.value
+
+    def autotune(self):
+        """Time the walk variants on this device and keep the fastest; returns
+        the report (one line per variant, * = chosen)."""
+        buf = ctypes.create_string_buffer(4096)
+        _ck(lib().pfc_autotune(self.h, buf, 4096), "pfc_autotune")
+        return buf.value.decode()
+
+    def set_walk_variant(self, cls, fused, variant):
+        _ck(lib().pfc_ctx_set_walk_variant(self.h, cls, int(fused), variant), "pfc_ctx_set_walk_variant")
+
+    def walk_variant(self, cls, fused):
+        """(variant index, candidates per thread, block length)."""
+        v, n, b = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        _ck(lib().pfc_ctx_walk_variant(self.h, cls, int(fused), ctypes.byref(v), ctypes.byref(n),
+                                       ctypes.byref(b)), "pfc_ctx_walk_variant")
+        return v.value, n.value, b.value
 
     def device_info(self):
         buf = ctypes.create_string_buffer(256)

@@ -366,8 +366,12 @@ static int enqueue_iter_range(pfc_job *j, uint32_t lo, uint32_t hi) {
     pfc_ctx *c = j->ctx;
     const HitBuf h = hitbuf(j);
     auto walk = [&](const WalkArgs &w) {
-        if (j->use32) c->launches += launch_walk32(j->c32.view(counts_ptr(j)), w, h, c->st);
-        if (j->use64) c->launches += launch_walk64(j->c64.view(counts_ptr(j) + 1), w, h, c->st, j->seg_hi <= kLazyWalkEnd);
+        const int fused = w.mult2 != nullptr;
+        const bool lazy = j->seg_hi <= kLazyWalkEnd;
+        if (j->use32) c->launches += launch_walk32(j->c32.view(counts_ptr(j)), w, h, c->st, c->walk_var[0][fused]);
+        if (j->use64)
+            c->launches += launch_walk64(j->c64.view(counts_ptr(j) + 1), w, h, c->st, lazy,
+                                         c->walk_var[lazy ? 1 : 2][fused]);
     };
     WalkArgs w;
     w.lo = lo;
@@ -775,5 +779,93 @@ extern "C" int pfc_job_verify_tables(pfc_job *j, uint64_t *table_bytes) {
         if (count != rp.count || prod != rp.P[2]) return PFC_ERR_VALIDATION;
     }
     if (table_bytes) *table_bytes = bytes;
+    return PFC_OK;
+}
+
+// ------------------------------------------------------------- autotuning
+
+extern "C" int pfc_ctx_set_walk_variant(pfc_ctx *c, int cls, int fused, int variant) {
+    if (!c || cls < 0 || cls > 2 || fused < 0 || fused > 1) return PFC_ERR_ARG;
+    if (variant < 0 || variant >= walk_variant_count(cls, fused != 0)) return PFC_ERR_ARG;
+    c->walk_var[cls][fused] = variant;
+    return PFC_OK;
+}
+
+extern "C" int pfc_ctx_walk_variant(pfc_ctx *c, int cls, int fused, int *variant, int *nc, int *block) {
+    if (!c || cls < 0 || cls > 2 || fused < 0 || fused > 1) return PFC_ERR_ARG;
+    const int v = c->walk_var[cls][fused];
+    int n = 0, b = 0;
+    if (walk_variant_shape(cls, fused != 0, v, &n, &b)) return PFC_ERR_ARG;
+    if (variant) *variant = v;
+    if (nc) *nc = n;
+    if (block) *block = b;
+    return PFC_OK;
+}
+
+// Time every walk variant of one size class and walk kind on a synthetic
+// search (the production kernels, one n-window per trial, best of three) and
+// keep the fastest.
+static int tune_one(pfc_ctx *c, int cls, int fused, char *report, size_t cap, size_t *used) {
+    const int nv = walk_variant_count(cls, fused != 0);
+    if (nv < 2) return PFC_OK;
+    constexpr uint32_t kWin = 8192, kReps = 3;
+    const uint32_t nmin = 101, nmax = nmin + kWin * (1 + nv * kReps);
+    const uint64_t lo = cls == 0 ? 1000000000ull : (1ull << 40);
+    const uint64_t hi = lo + (cls == 0 ? 5000000ull : 7000000ull);   // ~2.4e5 candidates
+    pfc_job *j = nullptr;
+    int rc = pfc_job_create(c, fused ? (PFC_FACTORIAL | PFC_COMPOSITORIAL) : PFC_FACTORIAL, nmin, nmax, lo, hi, &j);
+    if (rc) return rc;
+    rc = pfc_gen_candidates(j, lo, hi);
+    if (!rc) rc = pfc_setup(j);
+    const int saved = c->walk_var[cls][fused];
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    if (!rc && (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess)) rc = PFC_ERR_CUDA;
+    uint32_t n = nmin;
+    if (!rc) rc = pfc_iterate(j, n, n + kWin);  // warm-up
+    n += kWin;
+    std::vector<float> best(nv, 1e30f);
+    for (uint32_t r = 0; r < kReps && !rc; ++r)
+        for (int v = 0; v < nv && !rc; ++v) {
+            c->walk_var[cls][fused] = v;
+            cudaEventRecord(e0, c->st);
+            rc = pfc_iterate(j, n, n + kWin);
+            cudaEventRecord(e1, c->st);
+            n += kWin;
+            if (!rc && cudaEventSynchronize(e1) != cudaSuccess) rc = PFC_ERR_CUDA;
+            float ms = 0;
+            if (!rc) cudaEventElapsedTime(&ms, e0, e1);
+            best[v] = std::min(best[v], ms);
+        }
+    int pick = saved;
+    if (!rc) {
+        pick = 0;
+        for (int v = 1; v < nv; ++v)
+            if (best[v] < best[pick]) pick = v;
+        static const char *names[3] = {"class32", "class64-lazy", "class64"};
+        for (int v = 0; v < nv; ++v) {
+            int vn = 0, vb = 0;
+            walk_variant_shape(cls, fused != 0, v, &vn, &vb);
+            if (report && *used < cap)
+                *used += snprintf(report + *used, cap - *used, "%s %s nc=%d b=%d %.3f ms%s\n", names[cls],
+                                  fused ? "fused" : "single", vn, vb, best[v], v == pick ? " *" : "");
+        }
+    }
+    c->walk_var[cls][fused] = pick;
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    pfc_job_destroy(j);
+    return rc;
+}
+
+extern "C" int pfc_autotune(pfc_ctx *c, char *report, size_t cap) {
+    if (!c) return PFC_ERR_ARG;
+    CK(cudaSetDevice(c->device));
+    size_t used = 0;
+    if (report && cap) report[0] = 0;
+    for (int cls = 0; cls < 2; ++cls)
+        for (int fused = 0; fused < 2; ++fused) {
+            const int rc = tune_one(c, cls, fused, report, cap, &used);
+            if (rc) return rc;
+        }
     return PFC_OK;
 }

@@ -638,6 +638,10 @@ int main(int argc, char **argv) {
     int sms = 0;
     pfc_ctx_device_info(ctx, name, sizeof(name), &sms);
     printf("GPU Info:\n  Name: \t\t%s\n  Compute Units: \t%d\n", name, sms);
+    // choose the walk kernels by timing them on this device (the reference
+    // times the GPU to size its launches, profileGPU, cl_sieve.cpp:669-769)
+    rc = pfc_autotune(ctx, nullptr, 0);
+    if (rc) die_status("pfc_autotune", rc);
     if (sd.test) run_test(ctx, sd);
     else run_search(ctx, st, sd);
     pfc_ctx_destroy(ctx);

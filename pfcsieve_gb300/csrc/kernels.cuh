@@ -106,9 +106,15 @@ int launch_setup32(const ClassBuf<uint32_t> &c, const SetupArgs<uint32_t> &a, cu
 int launch_setup64(const ClassBuf<uint64_t> &c, const SetupArgs<uint64_t> &a, cudaStream_t st);
 // class 64 below 2^64/3 with 256-bit table words
 int launch_setup64w(const ClassBuf<uint64_t> &c, const SetupArgs<WideWord> &a, cudaStream_t st);
-int launch_walk32(const ClassBuf<uint32_t> &c, const WalkArgs &a, const HitBuf &h, cudaStream_t st);
+// walk launches: `variant` indexes the walk variants of the size class
+// (0 = default; see walk_variant_shape)
+int launch_walk32(const ClassBuf<uint32_t> &c, const WalkArgs &a, const HitBuf &h, cudaStream_t st, int variant);
 // lazy: every candidate is below 2^64/3 (the walk then takes lazy one-word steps)
-int launch_walk64(const ClassBuf<uint64_t> &c, const WalkArgs &a, const HitBuf &h, cudaStream_t st, bool lazy);
+int launch_walk64(const ClassBuf<uint64_t> &c, const WalkArgs &a, const HitBuf &h, cudaStream_t st, bool lazy,
+                  int variant);
+// size class 0: p < 2^31, 1: lazy class 64 (p < 2^64/3), 2: other class 64
+int walk_variant_count(int cls, bool fused);
+int walk_variant_shape(int cls, bool fused, int variant, int *nc, int *b);
 // compositorial multipliers of n in [lo, hi): n when composite, 1 when prime
 // (bit k of primebits <-> n = nmin + k); `out` is padded with 1 to a multiple of 16
 int launch_cmult(uint32_t *out, const uint32_t *primebits, uint32_t nmin, uint32_t lo, uint32_t hi,

@@ -286,8 +286,8 @@ extern "C" int pfc_segment_noalloc(unsigned mode, uint32_t nmin, uint32_t nmax, 
                 w.type = PFC_TYPE_COMPOSITORIAL;
             }
         }
-        if (use32) launch_walk32(c32, w, h, st);
-        if (use64) launch_walk64(c64, w, h, st, p_hi <= kLazyWalkEnd);
+        if (use32) launch_walk32(c32, w, h, st, 0);
+        if (use64) launch_walk64(c64, w, h, st, p_hi <= kLazyWalkEnd, 0);
         a = b;
     }
 

@@ -33,8 +33,9 @@ __global__ void __launch_bounds__(256) setup_kernel(ClassBuf<typename T::W> c, S
 
 // ------------------------------------------------------------------- walk
 
-// One walk launch over all candidates of a class (see walk_streams).
-template <class T, int NC, bool FUSED>
+// One walk launch over all candidates of a class (see walk_streams): NC
+// candidates per thread (or the two chains of one, FUSED), blocks of B steps.
+template <class T, int NC, bool FUSED, int B>
 __global__ void __launch_bounds__(256) walk_kernel(ClassBuf<typename T::W> c, WalkArgs a, HitBuf h) {
     using W = typename T::W;
     constexpr int NS = FUSED ? 2 : NC;   // streams per thread
@@ -60,7 +61,7 @@ __global__ void __launch_bounds__(256) walk_kernel(ClassBuf<typename T::W> c, Wa
 #pragma unroll
         for (int s = 0; s < NC; ++s) x[s] = act[s] ? st[idx[s]] : 0;
     }
-    walk_streams<T, NC, FUSED>(m, x, act, a, h);
+    walk_streams<T, NC, FUSED, B>(m, x, act, a, h);
     const uint32_t walked = (a.hi - a.lo) * (FUSED ? 2u : 1u);
     if (FUSED) {
         if (act[0]) {
@@ -139,22 +140,81 @@ int launch_setup64w(const ClassBuf<uint64_t> &c, const SetupArgs<WideWord> &a, c
     return 1;
 }
 
-template <class T>
-static int launch_walk(const ClassBuf<typename T::W> &c, const WalkArgs &a, const HitBuf &h, cudaStream_t st) {
-    if (!c.cap || a.hi <= a.lo) return 0;
-    if (a.mult2) {
-        walk_kernel<T, 1, true><<<grid_for(c.cap), 256, 0, st>>>(c, a, h);
+// Walk variants (candidates per thread, block length) per size class and walk
+// kind; entry 0 is the default, pfc_autotune measures the others.
+struct WalkVariant {
+    int nc, b;
+};
+static const WalkVariant kVar32[] = {{2, 16}, {2, 8}, {1, 16}};
+static const WalkVariant kVar32F[] = {{1, 16}, {1, 8}};
+static const WalkVariant kVar64L[] = {{1, 16}, {1, 8}};
+static const WalkVariant kVar64LF[] = {{1, 16}, {1, 8}};
+static const WalkVariant kVar64[] = {{1, 8}};
+static const WalkVariant kVar64F[] = {{1, 8}};
+
+static const WalkVariant *variants(int cls, bool fused, int *n) {
+    const WalkVariant *v;
+    if (cls == 0) {
+        v = fused ? kVar32F : kVar32;
+        *n = fused ? 2 : 3;
+    } else if (cls == 1) {
+        v = fused ? kVar64LF : kVar64L;
+        *n = 2;
     } else {
-        const uint32_t per_block = 256u * T::NC;
-        walk_kernel<T, T::NC, false><<<(c.cap + per_block - 1) / per_block, 256, 0, st>>>(c, a, h);
+        v = fused ? kVar64F : kVar64;
+        *n = 1;
     }
+    return v;
+}
+
+int walk_variant_count(int cls, bool fused) {
+    int n = 0;
+    variants(cls, fused, &n);
+    return n;
+}
+
+int walk_variant_shape(int cls, bool fused, int variant, int *nc, int *b) {
+    int n = 0;
+    const WalkVariant *v = variants(cls, fused, &n);
+    if (variant < 0 || variant >= n) return -1;
+    *nc = v[variant].nc;
+    *b = v[variant].b;
+    return 0;
+}
+
+template <class T, int NC, bool FUSED, int B>
+static int launch_one(const ClassBuf<typename T::W> &c, const WalkArgs &a, const HitBuf &h, cudaStream_t st) {
+    const uint32_t per_block = 256u * NC;
+    walk_kernel<T, NC, FUSED, B><<<(c.cap + per_block - 1) / per_block, 256, 0, st>>>(c, a, h);
     return 1;
 }
-int launch_walk32(const ClassBuf<uint32_t> &c, const WalkArgs &a, const HitBuf &h, cudaStream_t st) {
-    return launch_walk<Cls32>(c, a, h, st);
+
+template <class T>
+static int launch_walk(const ClassBuf<typename T::W> &c, const WalkArgs &a, const HitBuf &h, cudaStream_t st,
+                       int cls, int variant) {
+    if (!c.cap || a.hi <= a.lo) return 0;
+    int n = 0;
+    const WalkVariant *vs = variants(cls, a.mult2 != nullptr, &n);
+    const WalkVariant v = vs[(variant >= 0 && variant < n) ? variant : 0];
+    if (a.mult2) {
+        if (v.b == 8) return launch_one<T, 1, true, 8>(c, a, h, st);
+        return launch_one<T, 1, true, 16>(c, a, h, st);
+    }
+    if constexpr (T::NC == 2) {
+        if (v.nc == 2 && v.b == 8) return launch_one<T, 2, false, 8>(c, a, h, st);
+        if (v.nc == 1) return launch_one<T, 1, false, 16>(c, a, h, st);
+        return launch_one<T, 2, false, 16>(c, a, h, st);
+    } else {
+        if (v.b == 16) return launch_one<T, 1, false, 16>(c, a, h, st);
+        return launch_one<T, 1, false, 8>(c, a, h, st);
+    }
 }
-int launch_walk64(const ClassBuf<uint64_t> &c, const WalkArgs &a, const HitBuf &h, cudaStream_t st, bool lazy) {
-    return lazy ? launch_walk<Cls64L>(c, a, h, st) : launch_walk<Cls64>(c, a, h, st);
+int launch_walk32(const ClassBuf<uint32_t> &c, const WalkArgs &a, const HitBuf &h, cudaStream_t st, int variant) {
+    return launch_walk<Cls32>(c, a, h, st, 0, variant);
+}
+int launch_walk64(const ClassBuf<uint64_t> &c, const WalkArgs &a, const HitBuf &h, cudaStream_t st, bool lazy,
+                  int variant) {
+    return lazy ? launch_walk<Cls64L>(c, a, h, st, 1, variant) : launch_walk<Cls64>(c, a, h, st, 2, variant);
 }
 
 int launch_cmult(uint32_t *out, const uint32_t *primebits, uint32_t nmin, uint32_t lo, uint32_t hi,

@@ -280,11 +280,10 @@ __device__ __noinline__ void replay_chain(const typename T::M m, typename T::W x
 // x holds canonical Montgomery-form residues on entry and on exit.  Inactive
 // streams hold 0, which never matches a target (targets are nonzero mod p),
 // so they never trigger a replay.
-template <class T, int NC, bool FUSED>
+template <class T, int NC, bool FUSED, int B = (FUSED ? T::B_FUSED : T::B)>
 __device__ __forceinline__ void walk_streams(const typename T::M (&m)[NC], typename T::W (&x)[FUSED ? 2 : NC],
                                              const bool (&act)[NC], const WalkArgs &a, const HitBuf &h) {
     using W = typename T::W;
-    constexpr int B = FUSED ? T::B_FUSED : T::B;
     constexpr int NS = FUSED ? 2 : NC;
     typename T::template Tgt<FUSED> tg[NC][B];
     W K[NC];

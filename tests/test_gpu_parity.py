@@ -219,3 +219,38 @@ def test_selftest_factor_lists(ctx, cid):
     r = pfc.sieve(c["mode"], c["nmin"], c["nmax"], c["pmin"], c["pmax"], threads=THREADS, ctx=ctx)
     _, ofac = o.job(c["mode"], c["nmin"], c["nmax"], c["pmin"], c["pmax"], THREADS)
     assert np.array_equal(o.sort_factors(r.factors), o.sort_factors(ofac))
+
+
+# ---------------------------------------------- walk variants (autotuning)
+
+@pytest.mark.parametrize("cls,lo", [(0, 10**9), (1, 2**40)])
+def test_every_walk_variant_vs_oracle(cls, lo):
+    """Each compiled walk variant (candidates per thread, block length) gives
+    the oracle's residues, hits and checksum terms, in every mode."""
+    hi = lo + 300000
+    cands = o.candidates(lo, hi)
+    with pfc.Context(0) as c:
+        for fused in (0, 1):
+            modes = [5] if fused else [1, 2, 4]
+            nvar = {(0, 0): 3, (0, 1): 2, (1, 0): 2, (1, 1): 2}[(cls, fused)]
+            for mode in modes:
+                ohits, osum, terms = o.sieve(mode, 3000, 7001, cands, THREADS, want_terms=True)
+                for v in range(nvar):
+                    c.set_walk_variant(cls, fused, v)
+                    p, s0, s1, hits, termsum, _ = run_segment(c, mode, 3000, 7001, lo, hi)
+                    assert np.array_equal(s0, terms[:, 0]), (mode, v)
+                    if mode == 5:
+                        assert np.array_equal(s1, terms[:, 2]), v
+                    assert np.array_equal(hits, ohits), (mode, v)
+                    assert termsum == osum, (mode, v)
+
+
+def test_autotune_reports_and_picks_one_variant_per_kind():
+    with pfc.Context(0) as c:
+        rep = c.autotune()
+        lines = [x for x in rep.splitlines() if x]
+        assert len(lines) == 3 + 2 + 2 + 2
+        for kind in ("class32 single", "class32 fused", "class64-lazy single", "class64-lazy fused"):
+            assert sum(1 for x in lines if x.startswith(kind) and x.endswith("*")) == 1
+        v, nc, b = c.walk_variant(0, 0)
+        assert (nc, b) in ((2, 16), (2, 8), (1, 16))
