@@ -20,9 +20,9 @@
 // power of R per step, and the replay skips the test where the multiplier is
 // 1.  The fast path tests every step: at a prime n the compositorial value is
 // the previous step's, so an unmasked match there only repeats a hit already
-// seen and costs one replay, never a wrong record.  The per-step work is three
-// integer multiplies (IMAD.WIDE, IMAD, IMAD.HI), one compare and conditional
-// add for the reduction, and two compares for the hit test.
+// seen and costs one replay, never a wrong record.  The per-step work of a
+// class-32 chain is three integer multiplies (two 32x32->64, one low), one
+// subtract, and an absolute value and two compares for the hit test.
 #pragma once
 #include <type_traits>
 #include "arith.cuh"
