@@ -325,6 +325,8 @@ def run_mixed(ctx, njobs, warmup, steps=1):
                     "p50_s": float(np.percentile(lat, 50)), "p99_s": float(np.percentile(lat, 99)),
                     "plain_fcfs_p50_s": float(np.percentile(lat_p, 50)),
                     "plain_fcfs_p99_s": float(np.percentile(lat_p, 99)),
+                    # offered load: arrival rate x mean one-at-a-time service time
+                    "rho": 200.0 * float(np.mean(service)),
                     "throughput_pairs_per_s": pairs / makespan},
     }
 

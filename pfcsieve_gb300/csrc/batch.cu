@@ -333,6 +333,8 @@ struct BatchJob {
     uint32_t pos32 = 0, pos64 = 0;  // timeline position of all blocks of a class
     uint32_t tot32 = 0, tot64 = 0;  // timeline lengths (setup positions + walk steps)
     uint32_t win = 0;               // this iteration's window (0: the common window L)
+    bool wait = false;              // latency policy: no window this iteration
+    uint32_t waited = 0;            // consecutive iterations without a window
     // results
     uint64_t termsum = 0, primecount = 0;
     uint32_t flags = 0;
@@ -715,11 +717,11 @@ static uint32_t per_cta(const BatchJob *j, bool cls64) {
 // a common window of L positions per iteration (all searches progress at the
 // same pace, so the largest ones are never starved and the batch ends as
 // early as the work allows).  Latency policy (shortest remaining work
-// first): searches are taken in order of remaining cost, and while the
-// priority share (half of the iteration's budget) lasts each gets its own
+// first): searches are taken in order of remaining cost, each gets its own
 // window, as wide as keeps every one of its tasks within one CTA's share of
-// the iteration (no single task outlasts the rest), at most its remainder;
-// the other searches share the rest of the budget with the common window.
+// the iteration (no single task outlasts the rest) and as the iteration's
+// budget still open pays for; searches the budget cannot pay for wait, and
+// one that has waited 32 iterations gets a minimal window.
 // Windows are then ordered by the cost of one of their tasks, longest first.
 // Host work is linear in the number of searches.  Returns L.
 uint32_t build_tasks(pfc_batch *b) {
@@ -738,8 +740,8 @@ uint32_t build_tasks(pfc_batch *b) {
         order.push_back({r, j});
     }
     std::sort(order.begin(), order.end(), [](const auto &x, const auto &y) { return x.first < y.first; });
-    const double share = b->policy == PFC_BATCH_LATENCY ? 0.5 : 0.0;
-    double prio_left = share * budget, rate = 0;   // rate: cost per common-window position
+    const bool latency = b->policy == PFC_BATCH_LATENCY;
+    double prio_left = latency ? budget : 0.0, rate = 0;   // rate: cost per common-window position
     for (auto &o : order) {
         BatchJob *j = o.second;
         const PosCost c32 = pos_cost(j, false), c64 = pos_cost(j, true);
@@ -753,17 +755,28 @@ uint32_t build_tasks(pfc_batch *b) {
             worst = std::max(worst, per_cta(j, true) * std::max(c64.setup, c64.walk));
         }
         j->win = 0;
-        if (prio_left > 0) {
-            const double w = std::min(cta_share / std::max(worst, 1.0), 4294967295.0);
-            j->win = std::max<uint32_t>(64u, (uint32_t)w);
-            prio_left -= std::min(o.first, w * jrate);
+        j->wait = false;
+        if (!latency) {
+            rate += jrate;
             continue;
         }
-        rate += jrate;
+        // as wide as one CTA's share of the iteration allows and as the budget
+        // still open pays for; searches it cannot pay for wait, except that
+        // one that has waited 32 iterations gets a minimal window
+        const double w = std::min(cta_share / std::max(worst, 1.0), prio_left / std::max(jrate, 1.0));
+        if (w >= 64.0 || j->waited >= 32 || &o == &order.front()) {  // the smallest always advances
+            j->win = (uint32_t)std::min(std::max(w, 64.0), 4294967295.0);
+            prio_left -= std::min(o.first, (double)j->win * jrate);
+            j->waited = 0;
+        } else {
+            j->wait = true;
+            ++j->waited;
+        }
     }
+    const double prio_work = latency ? budget - std::max(prio_left, 0.0) : 0.0;
     b->prio = 0;
     for (auto &o : order) b->prio += o.second->win ? 1u : 0u;
-    const double Ld = std::max(64.0, std::min((1.0 - share) * budget / std::max(rate, 1.0), 4194304.0));
+    const double Ld = std::max(64.0, std::min(std::max(budget - prio_work, 0.0) / std::max(rate, 1.0), 4194304.0));
     const uint32_t L = ((uint32_t)Ld + 15u) & ~15u;
 
     std::vector<std::pair<double, Window>> lists[3];
@@ -771,7 +784,7 @@ uint32_t build_tasks(pfc_batch *b) {
         for (int cls = 0; cls < 2; ++cls) {
             const uint32_t pos = cls ? j->pos64 : j->pos32, tot = cls ? j->tot64 : j->tot32;
             const uint32_t ns = cls ? j->nsetup64 : j->nsetup32, n = cls ? j->n64 : j->n32;
-            if (pos >= tot || n == 0) continue;
+            if (pos >= tot || n == 0 || j->wait) continue;
             const uint32_t hi = (uint32_t)std::min<uint64_t>((uint64_t)pos + (j->win ? j->win : L), tot);
             const PosCost c = pos_cost(j, cls != 0);
             const uint32_t per = per_cta(j, cls != 0);
@@ -882,7 +895,7 @@ int finish_iteration(pfc_batch *b, uint32_t L) {
                 (unsigned long long)b->iterations, b->running.size(), b->prio, L, b->t32_n, b->t64_n, nh, ms);
     }
     for (BatchJob *j : b->running) {
-        const uint64_t w = j->win ? j->win : L;
+        const uint64_t w = j->wait ? 0 : (j->win ? j->win : L);
         j->pos32 = (uint32_t)std::min<uint64_t>((uint64_t)j->pos32 + w, j->tot32);
         j->pos64 = (uint32_t)std::min<uint64_t>((uint64_t)j->pos64 + w, j->tot64);
     }
