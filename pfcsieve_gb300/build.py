@@ -24,7 +24,7 @@ LIB = os.path.join(LIBDIR, "libpfcsieve.so")
 CLI = os.path.join(BINDIR, "pfcsieve")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-I" + INC, "-I" + CSRC]
+NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-fopenmp", "-I" + INC, "-I" + CSRC]
 CXX_FLAGS = ["-O3", "-std=c++17", "-fPIC", "-fopenmp", "-Wall", "-I" + INC, "-I" + CSRC]
 
 CU_SOURCES = ["gen.cu", "sieve.cu", "api.cu", "batch.cu", "verify.cu", "peak.cu", "noalloc.cu"]

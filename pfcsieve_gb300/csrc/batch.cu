@@ -32,6 +32,10 @@
 #include <memory>
 #include <vector>
 
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
 #include "devmem.hpp"
 #include "walk.cuh"
 
@@ -499,11 +503,18 @@ static double now_s() {
 
 namespace {
 
-// Build the host tables of the queued searches that have none yet (at most
-// as many as there are free slots), in parallel across searches.
+// Build the host tables of the queued searches that have none yet, in
+// parallel across searches: at most four per host thread per call (so the
+// first iteration starts after a few searches are ready, and the rest are
+// prepared while kernels run) and at most as many as there are free slots.
 void prepare_queued(pfc_batch *b) {
     std::vector<BatchJob *> todo;
-    size_t room = b->free_slots.size();
+#ifdef _OPENMP
+    const size_t per_call = 4 * (size_t)omp_get_max_threads();
+#else
+    const size_t per_call = 4;
+#endif
+    size_t room = std::min(b->free_slots.size(), per_call);
     for (BatchJob *j : b->queued) {
         if (todo.size() >= room) break;
         if (j->state == kQueued) todo.push_back(j);
