@@ -442,19 +442,38 @@ class SieveResult:
         return "%016X" % self.checksum
 
 
-def sieve(mode, nmin, nmax, pmin, pmax, device=0, threads=2, verify=True, ctx=None):
-    """One complete search, as the reference's cl_sieve() runs it."""
+def sieve(mode, nmin, nmax, pmin, pmax, device=0, threads=2, verify=True, ctx=None, segments=4):
+    """One complete search, as the reference's cl_sieve() runs it.
+
+    The p range is walked in at least `segments` segments (each at most the
+    size the library suggests); the CPU verification of one segment's hits
+    runs in a worker thread while the GPU works on the next (the C calls
+    release the GIL).  Segments are disjoint p ranges in increasing order, so
+    the concatenated kept factors are sorted and the checksum addends add up:
+    the result equals one verification of all hits."""
+    import concurrent.futures as cf
+
     own = ctx is None
     ctx = ctx or Context(device)
     try:
-        with Job(ctx, mode, nmin, nmax, pmin, pmax) as job:
-            hits = job.run()
+        with Job(ctx, mode, nmin, nmax, pmin, pmax) as job, cf.ThreadPoolExecutor(1) as pool:
+            span = max((pmax - pmin + segments - 1) // max(segments, 1), 1)
+            futs, nhits, lo = [], 0, pmin
+            while lo < pmax:
+                hi = min(job.segment_end(lo), lo + span, pmax)
+                job.segment(lo, hi)
+                h = job.drain_hits()
+                nhits += len(h)
+                futs.append(pool.submit(finalize, mode, nmax, h, threads, verify))
+                lo = hi
             termsum, primecount = job.totals()
             pairs = job.pairs
-        kept, add = finalize(mode, nmax, hits, threads=threads, verify=verify)
+            parts = [f.result() for f in futs]
+        kept = np.concatenate([k for k, _ in parts]) if parts else np.zeros(0, dtype=FACTOR_DTYPE)
+        add = sum(a for _, a in parts)
         return SieveResult(factorcount=len(kept), primecount=primecount,
                            checksum=(termsum + add) & 0xFFFFFFFFFFFFFFFF, pairs=pairs,
-                           factors=kept, hits=len(hits))
+                           factors=kept, hits=nhits)
     finally:
         if own:
             ctx.close()
