@@ -245,7 +245,9 @@ typedef struct pfc_batch pfc_batch;
 typedef struct {
     unsigned mode;          /* PFC_* mode bits, as for pfc_job_create */
     uint32_t nmin, nmax;    /* n range [nmin, nmax), nmin >= 101, nmax - nmin <= 2^26 */
-    uint64_t pmin, pmax;    /* p range [pmin, pmax), pmin >= 3 */
+    uint64_t pmin, pmax;    /* p range [pmin, pmax), pmin >= 3, at most ~2^28 candidates per
+                               size class (a batched search keeps all its candidates on the
+                               device; larger searches: pfc_job_run, which segments) */
 } pfc_job_desc;
 
 typedef struct {

@@ -1050,6 +1050,12 @@ extern "C" int pfc_batch_submit(pfc_batch *b, const pfc_job_desc *d, uint64_t *i
     if (!valid_mode || d->pmin < 3 || d->pmax <= d->pmin || d->nmin < 101 || d->nmax < d->nmin ||
         d->nmax > 0x7FFFFFFFu || d->nmax - d->nmin > (1u << 26))
         return PFC_ERR_ARG;
+    // a batched search keeps all its candidates on the device at once:
+    // at most 2^28 expected per size class (about 7.5 GB in class 64); larger
+    // searches go through pfc_job_run, which walks the p range in segments
+    const double e32 = est_cands(d->pmin, std::min<uint64_t>(d->pmax, kClassSplit));
+    const double e64 = est_cands(std::max<uint64_t>(d->pmin, kClassSplit), d->pmax);
+    if (e32 > (double)(1u << 28) || e64 > (double)(1u << 28)) return PFC_ERR_ARG;
     auto j = std::make_unique<BatchJob>();
     j->id = b->next_id++;
     j->mode = mode;

@@ -118,7 +118,8 @@ def test_finished_search_is_released(ctx):
 def test_invalid_searches_are_rejected(ctx):
     with pfc.Batch(ctx) as b:
         for bad in [(3, 101, 200, 10**6, 2 * 10**6), (1, 100, 200, 10**6, 2 * 10**6),
-                    (1, 101, 200, 2, 10**6), (1, 101, 200, 10**6, 10**6)]:
+                    (1, 101, 200, 2, 10**6), (1, 101, 200, 10**6, 10**6),
+                    (1, 101, 200, 2**40, 2**40 + 10**13)]:     # ~3.6e11 candidates: too many to hold
             with pytest.raises(pfc.PFCError):
                 b.submit(*bad)
 
