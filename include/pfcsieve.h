@@ -78,6 +78,14 @@ int pfc_ctx_destroy(pfc_ctx *ctx);
  * with CUDA events on the launching stream. */
 void *pfc_ctx_stream(pfc_ctx *ctx);
 
+/* pfc_segment runs the part of a segment after candidate generation (setup,
+ * walk launches, check, stats read-back) as a CUDA graph captured once per
+ * job and replayed for every segment (re-captured when a buffer or a kernel
+ * choice changes).  On by default; off (`on` = 0, or PFCSIEVE_CUDA_GRAPHS=0 in
+ * the environment when the context is created) runs the same launches on the
+ * stream.  Results are identical. */
+int pfc_ctx_set_graphs(pfc_ctx *ctx, int on);
+
 /* Number of kernels this context has launched so far. */
 uint64_t pfc_ctx_launch_count(pfc_ctx *ctx);
 

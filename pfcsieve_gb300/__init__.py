@@ -117,6 +117,7 @@ def lib():
             "pfc_batch_set_policy": (ctypes.c_int, [vp, ctypes.c_int]),
             "pfc_batch_set_hit_capacity": (ctypes.c_int, [vp, u32]),
             "pfc_autotune": (ctypes.c_int, [vp, ctypes.c_char_p, sz]),
+            "pfc_ctx_set_graphs": (ctypes.c_int, [vp, ctypes.c_int]),
             "pfc_ctx_set_walk_variant": (ctypes.c_int, [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int]),
             "pfc_ctx_walk_variant": (ctypes.c_int, [vp, ctypes.c_int, ctypes.c_int, P(ctypes.c_int),
                                                     P(ctypes.c_int), P(ctypes.c_int)]),
@@ -184,6 +185,10 @@ class Context:
         buf = ctypes.create_string_buffer(4096)
         _ck(lib().pfc_autotune(self.h, buf, 4096), "pfc_autotune")
         return buf.value.decode()
+
+    def set_graphs(self, on):
+        """Replay each job's segment body as a CUDA graph (default on)."""
+        _ck(lib().pfc_ctx_set_graphs(self.h, int(bool(on))), "pfc_ctx_set_graphs")
 
     def set_walk_variant(self, cls, fused, variant):
         _ck(lib().pfc_ctx_set_walk_variant(self.h, cls, int(fused), variant), "pfc_ctx_set_walk_variant")
@@ -445,10 +450,12 @@ class SieveResult:
 def sieve(mode, nmin, nmax, pmin, pmax, device=0, threads=2, verify=True, ctx=None, segments=4):
     """One complete search, as the reference's cl_sieve() runs it.
 
-    The p range is walked in at least `segments` segments (each at most the
-    size the library suggests); the CPU verification of one segment's hits
-    runs in a worker thread while the GPU works on the next (the C calls
-    release the GIL).  Segments are disjoint p ranges in increasing order, so
+    A search of more than about 1e11 pairs (0.1 s of GPU time or more) is
+    walked in at least `segments` segments (each at most the size the library
+    suggests) and the CPU verification of one segment's hits runs in a worker
+    thread while the GPU works on the next (the C calls release the GIL);
+    smaller searches run as library-sized segments, where fixed per-segment
+    costs would outweigh the overlap.  Segments are disjoint p ranges in increasing order, so
     the concatenated kept factors are sorted and the checksum addends add up:
     the result equals one verification of all hits."""
     import concurrent.futures as cf
@@ -457,7 +464,10 @@ def sieve(mode, nmin, nmax, pmin, pmax, device=0, threads=2, verify=True, ctx=No
     ctx = ctx or Context(device)
     try:
         with Job(ctx, mode, nmin, nmax, pmin, pmax) as job, cf.ThreadPoolExecutor(1) as pool:
-            span = max((pmax - pmin + segments - 1) // max(segments, 1), 1)
+            import math
+            pairs_est = (pmax - pmin) / math.log(max(pmin, 3)) * max(nmax - nmin, 1)
+            parts_wanted = max(segments, 1) if pairs_est >= 1e11 else 1
+            span = max((pmax - pmin + parts_wanted - 1) // parts_wanted, 1)
             futs, nhits, lo = [], 0, pmin
             while lo < pmax:
                 hi = min(job.segment_end(lo), lo + span, pmax)

@@ -13,6 +13,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <new>
 #include <type_traits>
@@ -52,6 +53,17 @@ struct pfc_job {
     uint64_t seg_lo = 0, seg_hi = 0;
     bool use32 = false, use64 = false;   // size classes the segment can hold
     uint64_t pairs = 0;
+
+    // the post-generation part of a segment captured as a CUDA graph, replayed
+    // while the key (buffers, launch shapes, kernel choices) is unchanged
+    struct GraphKey {
+        const void *p32, *p64, *hits, *cmult;
+        uint64_t cap32, cap64, hitcap;
+        int lazy, use32, use64, var[3][2];
+    };
+    cudaGraphExec_t graph = nullptr;
+    GraphKey gkey{};
+    uint64_t graph_kernels = 0;
 };
 
 // ------------------------------------------------------------------ helpers
@@ -100,6 +112,8 @@ extern "C" int pfc_ctx_create(int device, uint64_t mem_budget, pfc_ctx **out) {
     size_t fr = 0, tot = 0;
     cudaMemGetInfo(&fr, &tot);
     c->budget = mem_budget ? mem_budget : (uint64_t)(0.9 * (double)fr);
+    const char *g = getenv("PFCSIEVE_CUDA_GRAPHS");
+    c->graphs = !(g && g[0] == '0');
     cudaError_t e = cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = dalloc_bytes(c, (void **)&c->d_pat, kPatEntries * sizeof(uint64_t));
     if (e == cudaSuccess) {
@@ -150,6 +164,8 @@ static int job_release(pfc_job *j) {
     pfc_ctx *c = j->ctx;
     cudaSetDevice(c->device);
     cudaStreamSynchronize(c->st);
+    if (j->graph) cudaGraphExecDestroy(j->graph);
+    j->graph = nullptr;
     j->a32.release(c);
     j->b32.release(c);
     j->a64.release(c);
@@ -497,6 +513,86 @@ extern "C" int pfc_check(pfc_job *j) {
     return commit_segment(j);
 }
 
+// The part of a segment after candidate generation: clear the segment
+// accumulators, setup, the walk in launches sized from the buffer capacities
+// (so the sequence is the same for every segment of the job), the check and
+// the read-back of the segment's stats into pinned host memory.
+static int enqueue_segment_body(pfc_job *j) {
+    pfc_ctx *c = j->ctx;
+    CK(cudaMemsetAsync(&j->stats.p->termsum, 0, sizeof(unsigned long long), c->st));
+    CK(cudaMemsetAsync(&j->stats.p->flags, 0, sizeof(uint32_t), c->st));
+    int rc = enqueue_setup(j);
+    if (rc) return rc;
+    rc = enqueue_iter_chunked(j, iter_begin(j), iter_end(j), j->c32.p.p ? j->c32.cap : 0,
+                              j->c64.p.p ? j->c64.cap : 0);
+    if (rc) return rc;
+    j->next_it = iter_end(j);
+    rc = enqueue_check(j);
+    if (rc) return rc;
+    c->d2h += sizeof(SegStats);
+    CK(cudaMemcpyAsync(j->h_stats, j->stats.p, sizeof(SegStats), cudaMemcpyDeviceToHost, c->st));
+    return PFC_OK;
+}
+
+static int segment_body_stream(pfc_job *j) {
+    const int rc = enqueue_segment_body(j);
+    if (rc) return rc;
+    CK(cudaStreamSynchronize(j->ctx->st));
+    return PFC_OK;
+}
+
+// The same body as one CUDA graph: captured at the first segment of the job
+// and again when a buffer, a launch shape or a kernel choice changed, then
+// replayed with one launch per segment.
+static int segment_body_graph(pfc_job *j) {
+    pfc_ctx *c = j->ctx;
+    // a buffer the body would otherwise allocate while it is being captured
+    if (j->mode & PFC_COMPOSITORIAL) {
+        const uint64_t n32 = j->c32.p.p ? j->c32.cap : 0, n64 = j->c64.p.p ? j->c64.cap : 0;
+        const size_t L = std::min(chunk_len(n32 + 3 * n64, 1.5e11), kMaxChunk);
+        const size_t need = (((size_t)std::min<uint64_t>(L, iter_end(j) - iter_begin(j))) + 15) & ~(size_t)15;
+        if (j->cmult.n < need) CK(j->cmult.alloc(c, std::max<size_t>(need, 4096)));
+    }
+    pfc_job::GraphKey k{};
+    k.p32 = j->c32.p.p;
+    k.p64 = j->c64.p.p;
+    k.hits = j->hits.p;
+    k.cmult = j->cmult.p;
+    k.cap32 = j->c32.cap;
+    k.cap64 = j->c64.cap;
+    k.hitcap = j->hits.n;
+    k.lazy = j->seg_hi <= kLazyWalkEnd;
+    k.use32 = j->use32;
+    k.use64 = j->use64;
+    memcpy(k.var, c->walk_var, sizeof(k.var));
+    if (!j->graph || memcmp(&k, &j->gkey, sizeof(k)) != 0) {
+        if (j->graph) cudaGraphExecDestroy(j->graph);
+        j->graph = nullptr;
+        const uint64_t l0 = c->launches, d0 = c->d2h;
+        CK(cudaStreamBeginCapture(c->st, cudaStreamCaptureModeThreadLocal));
+        const int rc = enqueue_segment_body(j);
+        cudaGraph_t g = nullptr;
+        const cudaError_t e = cudaStreamEndCapture(c->st, &g);
+        j->graph_kernels = c->launches - l0;
+        c->launches = l0;   // counted when the graph is launched
+        c->d2h = d0;
+        if (rc) {
+            if (g) cudaGraphDestroy(g);
+            return rc;
+        }
+        CK(e);
+        const cudaError_t ei = cudaGraphInstantiate(&j->graph, g, 0);
+        cudaGraphDestroy(g);
+        CK(ei);
+        j->gkey = k;
+    }
+    CK(cudaGraphLaunch(j->graph, c->st));
+    c->launches += j->graph_kernels;
+    c->d2h += sizeof(SegStats);
+    CK(cudaStreamSynchronize(c->st));
+    return PFC_OK;
+}
+
 extern "C" int pfc_segment(pfc_job *j, uint64_t p_lo, uint64_t p_hi) {
     if (!j || p_lo < j->pmin || p_hi > j->pmax || p_hi <= p_lo) return PFC_ERR_ARG;
     pfc_ctx *c = j->ctx;
@@ -517,20 +613,12 @@ extern "C" int pfc_segment(pfc_job *j, uint64_t p_lo, uint64_t p_hi) {
         if (over32) CK(j->c32.ensure(c, (uint32_t)std::min<uint64_t>(4000000000ull, n32 + n32 / 8 + 1024)));
         if (over64) CK(j->c64.ensure(c, (uint32_t)std::min<uint64_t>(4000000000ull, n64 + n64 / 8 + 1024)));
     }
-    const uint32_t n32 = j->h_stats->counts[0], n64 = j->h_stats->counts[1];
     const unsigned long long hit_base = j->h_stats->hits;
     for (int attempt = 0;; ++attempt) {
-        CK(cudaMemsetAsync(&j->stats.p->termsum, 0, sizeof(unsigned long long), c->st));
-        CK(cudaMemsetAsync(&j->stats.p->flags, 0, sizeof(uint32_t), c->st));
-        rc = enqueue_setup(j);
+        rc = c->graphs ? segment_body_graph(j) : segment_body_stream(j);
         if (rc) return rc;
-        rc = enqueue_iter_chunked(j, iter_begin(j), iter_end(j), n32, n64);
-        if (rc) return rc;
+        j->stage = 2;
         j->next_it = iter_end(j);
-        rc = enqueue_check(j);
-        if (rc) return rc;
-        rc = read_stats(j);
-        if (rc) return rc;
         const unsigned long long nh = j->h_stats->hits;
         if (nh <= j->hits.n) break;
         if (attempt >= 2) return PFC_ERR_HIT_OVERFLOW;
@@ -867,5 +955,11 @@ extern "C" int pfc_autotune(pfc_ctx *c, char *report, size_t cap) {
             const int rc = tune_one(c, cls, fused, report, cap, &used);
             if (rc) return rc;
         }
+    return PFC_OK;
+}
+
+extern "C" int pfc_ctx_set_graphs(pfc_ctx *c, int on) {
+    if (!c) return PFC_ERR_ARG;
+    c->graphs = on != 0;
     return PFC_OK;
 }

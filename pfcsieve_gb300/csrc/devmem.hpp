@@ -21,6 +21,7 @@ struct pfc_ctx {
     uint64_t h2d = 0, d2h = 0;   // bytes copied by this context
     uint64_t *d_pat = nullptr;
     int walk_var[3][2] = {{0, 0}, {0, 0}, {0, 0}};   // walk variant per size class and kind (fused)
+    bool graphs = true;   // pfc_segment replays each job's segment body as a CUDA graph
 };
 
 namespace pfc {

@@ -254,3 +254,22 @@ def test_autotune_reports_and_picks_one_variant_per_kind():
             assert sum(1 for x in lines if x.startswith(kind) and x.endswith("*")) == 1
         v, nc, b = c.walk_variant(0, 0)
         assert (nc, b) in ((2, 16), (2, 8), (1, 16))
+
+
+@pytest.mark.parametrize("mode", [1, 2, 4, 5])
+def test_segment_graphs_equal_stream_launches(mode):
+    """Several segments of one job replayed as a CUDA graph (re-captured when
+    the candidate buffers grow and at the class-64 boundary) give the same
+    totals and hits as the same launches issued on the stream."""
+    lo, hi = 2**31 - 400000, 2**31 + 600000
+    cuts = [lo, lo + 100000, lo + 130000, lo + 400000, 2**31 + 1, 2**31 + 300000, hi]
+    out = []
+    for graphs in (False, True):
+        with pfc.Context(0) as c:
+            c.set_graphs(graphs)
+            with pfc.Job(c, mode, 2000, 9000, lo, hi) as job:
+                for a, b in zip(cuts[:-1], cuts[1:]):
+                    job.segment(a, b)
+                out.append((job.totals(), o.sort_factors(job.drain_hits())))
+    assert out[0][0] == out[1][0]
+    assert np.array_equal(out[0][1], out[1][1])
