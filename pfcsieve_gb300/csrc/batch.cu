@@ -1,24 +1,24 @@
-// batch.cu -- many sieve jobs on the GPU at once: the batched persistent
-// kernel and the iteration-level scheduler behind pfc_batch_* (continuous
-// batching).
+// batch.cu -- many sieve jobs on the GPU at once: the batch kernel and the
+// iteration-level scheduler behind pfc_batch_* (continuous batching).
 //
 // The reference runs one search per process and one kernel per stage
 // (cl_sieve.cpp:1563-1726); a small search there leaves most of a large GPU
 // idle.  Here every admitted job contributes blocks of candidates (256, or 512
 // for two-candidate class-32 walks).  Each block has a timeline: its setup
-// program as an op stream ([0, S): 0 = square, 1 = fork of the combined search,
-// any other value = a table word to multiply in), then its walk ([S, S+N): n
-// steps, or prime steps for n#).  One iteration gives every unfinished block a
-// task, a window of at most L positions of its timeline; a persistent kernel
-// per size class takes tasks from a device counter until the list is empty, so
-// jobs of every size and mode share the SMs.  Between iterations the host
-// admits new jobs as memory and slots allow, drains the hits (tagged with the
-// job slot) and retires finished jobs: requests that arrive while others run
-// join at the next iteration.
+// programs as a table of runs ([0, S): squarings, table words, the fork of
+// the combined search), then its walk ([S, S+N): n steps, or prime steps for
+// n#).  All blocks of a job share one position.  One iteration gives every
+// running job (or, under the latency policy, every job the budget pays for)
+// a window of its timeline; the iteration's windows, sorted by task cost, are
+// one launch per size class with one CTA per block, dispatched by the
+// hardware block scheduler, so jobs of every size and mode share the SMs.
+// Between iterations the host admits new jobs as memory and slots allow,
+// drains the hits (tagged with the job slot) and retires finished jobs:
+// requests that arrive while others run join at the next iteration.
 //
-// Results equal the per-job path bit for bit: the same kernels (walk.cuh), the
-// same setup values (a job's op stream evaluates the same programs) and the
-// same check terms.
+// Results equal the per-job path bit for bit: the same arithmetic (walk.cuh),
+// the same setup programs evaluated in the same order, and the same check
+// terms.
 #include <cuda_runtime.h>
 
 #include <algorithm>
