@@ -2,12 +2,13 @@
 """Benchmark of the GB300 sieve path: (p,n) pairs tested per second.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--workload combined|factorial|primorial]
+                    [--workload combined|factorial|primorial|mixed] [--no-mixed]
 
 Workload (default): the combined factorial + compositorial search (-! -c) over
 n in [101, 200000) and p in [10^9, 10^9 + 10^8): about 4.8e6 candidate primes
 x 199,899 n = 9.7e11 pairs per step.  Inputs are the scalar search bounds; the
-tables live in HBM from job creation on.
+tables live in HBM from job creation on.  The walk kernels are chosen by the
+autotuner (pfc_autotune) first; the choice is in config.walk_variants.
 
 One step = candidate generation + setup + iterate over the whole n range +
 check + hit read-back, through the C ABI stage calls on the context stream.
