@@ -142,7 +142,14 @@ __device__ __forceinline__ void run_setup(const typename T::M (&m)[NC], typename
     }
 }
 
-template <class T, int NC, bool FUSED>
+// Task kinds: a window inside a search's setup that does not end its
+// timeline, a window inside its walk, or any other (the one that crosses from
+// setup to walk, or that ends a timeline without walk steps).  The batch
+// kernel is compiled per kind so that setup-only and walk-only launches carry
+// only their own code and registers.
+enum TaskKind { kAnyTask = 0, kSetupTask = 1, kWalkTask = 2 };
+
+template <class T, int NC, bool FUSED, int KIND>
 __device__ void run_task(const JobDev<typename T::W> &J, const Task &t, const HitBuf &h) {
     using W = typename T::W;
     constexpr int NS = FUSED ? 2 : NC;
@@ -159,7 +166,7 @@ __device__ void run_task(const JobDev<typename T::W> &J, const Task &t, const Hi
     const uint32_t S = J.nsetup, N = J.nwalk;
     W x[NS];
     uint32_t walked = 0;
-    if (t.lo < S) {
+    if (KIND != kWalkTask && t.lo < S) {
         // setup part: positions [lo, min(hi, S)) of the job's programs
         W acc[NC], fork[NC];
 #pragma unroll
@@ -173,7 +180,7 @@ __device__ void run_task(const JobDev<typename T::W> &J, const Task &t, const Hi
 #pragma unroll
             for (int s = 0; s < NC; ++s) acc[s] = m[s].mul(acc[s], m[s].mont_R_pow(FUSED ? J.corr_b : J.corr_a));
         }
-        if (e < S || (t.hi == S && N > 0)) {  // setup not finished, or the walk starts in a later task
+        if (KIND == kSetupTask || e < S || (t.hi == S && N > 0)) {  // the walk starts in a later task
 #pragma unroll
             for (int s = 0; s < NC; ++s)
                 if (act[s]) {
@@ -272,8 +279,8 @@ __device__ void run_task(const JobDev<typename T::W> &J, const Task &t, const Hi
 // the last tasks of an iteration crowd onto a few SMs: 78% of the per-job
 // path's throughput on a single large search, against 100% with hardware
 // dispatch.)  Thread 0 finds its window by binary search over first_cta.
-template <class T>
-__global__ void __launch_bounds__(256, sizeof(typename T::W) == 4 ? (T::B > 8 ? 3 : 4) : 2)
+template <class T, int KIND>
+__global__ void __launch_bounds__(256, (sizeof(typename T::W) == 4 || (KIND != kAnyTask && T::B > 8)) ? 3 : 2)
     batch_kernel(const Window *wins, uint32_t nwins, const JobDev<typename T::W> *jobs, HitBuf h) {
     // the task and its search record live in shared memory: every thread
     // reads the same fields, and registers stay free for the residues
@@ -298,8 +305,8 @@ __global__ void __launch_bounds__(256, sizeof(typename T::W) == 4 ? (T::B > 8 ? 
     __syncthreads();
     HitBuf hh = h;
     hh.tagval = st.slot;
-    if (sj.mode == (PFC_FACTORIAL | PFC_COMPOSITORIAL)) run_task<T, 1, true>(sj, st, hh);
-    else run_task<T, T::NC, false>(sj, st, hh);
+    if (sj.mode == (PFC_FACTORIAL | PFC_COMPOSITORIAL)) run_task<T, 1, true, KIND>(sj, st, hh);
+    else run_task<T, T::NC, false, KIND>(sj, st, hh);
 }
 
 // ------------------------------------------------------------------ host side
@@ -463,13 +470,16 @@ using namespace pfc;
 struct pfc_batch {
     pfc_ctx *ctx = nullptr;
     static constexpr uint32_t kSlots = 4096;
-    cudaStream_t st32 = nullptr, st64 = nullptr;
+    // one launch list per class group (class 32, class 64 below 2^64/3, other
+    // class 64) and task kind, one stream per size class and kind
+    static constexpr int kLists = 3, kKinds = 3, kStreams = 6;
+    cudaStream_t st[kStreams] = {};
     cudaEvent_t ev = nullptr;
     DArr<BatchStats> stats;
     DArr<JobDev<uint32_t>> jobs32;
     DArr<JobDev<uint64_t>> jobs64;
     // task lists: class 32, class 64 below 2^63 (lazy walk), other class 64
-    DArr<Window> wins32, wins64, wins64c;
+    DArr<Window> wins[kLists][kKinds];
     DArr<pfc_factor> hits;
     DArr<uint32_t> tags;
     DArr<unsigned long long> hitcount;
@@ -482,17 +492,18 @@ struct pfc_batch {
     std::vector<uint32_t> free_slots;
     std::vector<uint32_t> prime_cache;   // primes up to cache_lim
     uint32_t cache_lim = 0;
-    std::vector<Window> w32, w64, w64c;   // this iteration's windows per kernel
-    uint64_t ctas32 = 0, ctas64 = 0, ctas64c = 0;
+    std::vector<Window> w[kLists][kKinds];   // this iteration's windows per launch
+    uint64_t ctas[kLists][kKinds] = {};
     uint64_t next_id = 1;
     double work_per_iter = 1e11;         // candidate-steps per iteration (class 64 weighs 3)
     int policy = PFC_BATCH_THROUGHPUT;
     uint64_t iterations = 0;
     // timing: kernel spans (CUDA events) and host phases (wall clock)
-    cudaEvent_t ev_start = nullptr, ev_end32 = nullptr, ev_end64 = nullptr;
+    cudaEvent_t ev_start = nullptr, ev_end[kStreams] = {};
     double gpu_s = 0, gpu32_s = 0, gpu64_s = 0, prep_s = 0, admit_s = 0, step_s = 0;
     uint64_t tasks = 0;
     size_t t32_n = 0, t64_n = 0;   // task counts of the iteration in flight
+    bool used[kStreams] = {};      // streams with launches in the iteration in flight
     uint32_t prio = 0;             // searches with their own window this iteration
     bool trace = false;            // PFCSIEVE_BATCH_TRACE: one stderr line per iteration
 };
@@ -790,7 +801,7 @@ uint32_t build_tasks(pfc_batch *b) {
     const double Ld = std::max(64.0, std::min(std::max(budget - prio_work, 0.0) / std::max(rate, 1.0), 4194304.0));
     const uint32_t L = ((uint32_t)Ld + 15u) & ~15u;
 
-    std::vector<std::pair<double, Window>> lists[3];
+    std::vector<std::pair<double, Window>> lists[pfc_batch::kLists][pfc_batch::kKinds];
     for (BatchJob *j : b->running) {
         for (int cls = 0; cls < 2; ++cls) {
             const uint32_t pos = cls ? j->pos64 : j->pos32, tot = cls ? j->tot64 : j->tot32;
@@ -809,64 +820,81 @@ uint32_t build_tasks(pfc_batch *b) {
             w.lo = pos;
             w.hi = hi;
             const int l = cls == 0 ? 0 : (j->pmax <= kLazyEnd ? 1 : 2);
-            lists[l].push_back({cost, w});
+            const int kind = (hi <= ns && hi < tot) ? kSetupTask : (pos >= ns ? kWalkTask : kAnyTask);
+            lists[l][kind].push_back({cost, w});
         }
     }
-    std::vector<Window> *out[3] = {&b->w32, &b->w64, &b->w64c};
-    uint64_t *ctas[3] = {&b->ctas32, &b->ctas64, &b->ctas64c};
-    for (int l = 0; l < 3; ++l) {
-        std::sort(lists[l].begin(), lists[l].end(), [](const auto &x, const auto &y) { return x.first > y.first; });
-        out[l]->clear();
-        uint64_t first = 0;
-        for (auto &e : lists[l]) {
-            e.second.first_cta = (uint32_t)first;
-            first += e.second.nblocks;
-            out[l]->push_back(e.second);
+    for (int l = 0; l < pfc_batch::kLists; ++l)
+        for (int k = 0; k < pfc_batch::kKinds; ++k) {
+            auto &lst = lists[l][k];
+            std::sort(lst.begin(), lst.end(), [](const auto &x, const auto &y) { return x.first > y.first; });
+            b->w[l][k].clear();
+            uint64_t first = 0;
+            for (auto &e : lst) {
+                e.second.first_cta = (uint32_t)first;
+                first += e.second.nblocks;
+                b->w[l][k].push_back(e.second);
+            }
+            b->ctas[l][k] = first;
         }
-        *ctas[l] = first;
-    }
     return L;
+}
+
+template <class T, int KIND>
+static void launch_list(pfc_batch *b, int l, const JobDev<typename T::W> *jobs, const HitBuf &h) {
+    const uint64_t n = b->ctas[l][KIND];
+    if (!n) return;
+    const int si = (l == 0 ? 0 : 3) + KIND;
+    batch_kernel<T, KIND><<<(unsigned)n, 256, 0, b->st[si]>>>(b->wins[l][KIND].p, (uint32_t)b->w[l][KIND].size(),
+                                                              jobs, h);
+    b->used[si] = true;
+    b->ctx->launches++;
 }
 
 int launch_iteration(pfc_batch *b) {
     pfc_ctx *c = b->ctx;
-    const size_t n32 = b->w32.size(), n64 = b->w64.size(), n64c = b->w64c.size();
-    if (b->wins32.n < n32) CK(b->wins32.alloc(c, n32 + n32 / 2 + 64));
-    if (b->wins64.n < n64) CK(b->wins64.alloc(c, n64 + n64 / 2 + 64));
-    if (b->wins64c.n < n64c) CK(b->wins64c.alloc(c, n64c + n64c / 2 + 64));
-    if (n32) CK(cudaMemcpyAsync(b->wins32.p, b->w32.data(), n32 * sizeof(Window), cudaMemcpyHostToDevice, c->st));
-    if (n64) CK(cudaMemcpyAsync(b->wins64.p, b->w64.data(), n64 * sizeof(Window), cudaMemcpyHostToDevice, c->st));
-    if (n64c) CK(cudaMemcpyAsync(b->wins64c.p, b->w64c.data(), n64c * sizeof(Window), cudaMemcpyHostToDevice, c->st));
-    c->h2d += (n32 + n64 + n64c) * sizeof(Window);
+    for (int l = 0; l < pfc_batch::kLists; ++l)
+        for (int k = 0; k < pfc_batch::kKinds; ++k) {
+            const size_t n = b->w[l][k].size();
+            if (!n) continue;
+            if (b->wins[l][k].n < n) CK(b->wins[l][k].alloc(c, n + n / 2 + 64));
+            CK(cudaMemcpyAsync(b->wins[l][k].p, b->w[l][k].data(), n * sizeof(Window), cudaMemcpyHostToDevice, c->st));
+            c->h2d += n * sizeof(Window);
+        }
     CK(cudaEventRecord(b->ev_start, c->st));
-    CK(cudaStreamWaitEvent(b->st32, b->ev_start, 0));
-    CK(cudaStreamWaitEvent(b->st64, b->ev_start, 0));
+    for (int i = 0; i < pfc_batch::kStreams; ++i) {
+        b->used[i] = false;
+        CK(cudaStreamWaitEvent(b->st[i], b->ev_start, 0));
+    }
     HitBuf h{};
     h.buf = b->hits.p;
     h.count = b->hitcount.p;
     h.cap = b->hits.n;
     h.tag = b->tags.p;
-    if (b->ctas32) {
-        batch_kernel<Cls32><<<(unsigned)b->ctas32, 256, 0, b->st32>>>(b->wins32.p, (uint32_t)n32, b->jobs32.p, h);
-        c->launches++;
-    }
-    if (b->ctas64) {
-        batch_kernel<Cls64L><<<(unsigned)b->ctas64, 256, 0, b->st64>>>(b->wins64.p, (uint32_t)n64, b->jobs64.p, h);
-        c->launches++;
-    }
-    if (b->ctas64c) {
-        batch_kernel<Cls64><<<(unsigned)b->ctas64c, 256, 0, b->st64>>>(b->wins64c.p, (uint32_t)n64c, b->jobs64.p, h);
-        c->launches++;
-    }
+    // setup-only and general lists first: they hold the longest tasks
+    launch_list<Cls32, kSetupTask>(b, 0, b->jobs32.p, h);
+    launch_list<Cls32, kAnyTask>(b, 0, b->jobs32.p, h);
+    launch_list<Cls32, kWalkTask>(b, 0, b->jobs32.p, h);
+    launch_list<Cls64L, kSetupTask>(b, 1, b->jobs64.p, h);
+    launch_list<Cls64L, kAnyTask>(b, 1, b->jobs64.p, h);
+    launch_list<Cls64L, kWalkTask>(b, 1, b->jobs64.p, h);
+    launch_list<Cls64, kSetupTask>(b, 2, b->jobs64.p, h);
+    launch_list<Cls64, kAnyTask>(b, 2, b->jobs64.p, h);
+    launch_list<Cls64, kWalkTask>(b, 2, b->jobs64.p, h);
     CK(cudaGetLastError());
-    // the main stream waits for both classes before the hit read-back
-    CK(cudaEventRecord(b->ev_end32, b->st32));
-    CK(cudaStreamWaitEvent(c->st, b->ev_end32, 0));
-    CK(cudaEventRecord(b->ev_end64, b->st64));
-    CK(cudaStreamWaitEvent(c->st, b->ev_end64, 0));
-    b->tasks += b->ctas32 + b->ctas64 + b->ctas64c;
-    b->t32_n = b->ctas32;
-    b->t64_n = b->ctas64 + b->ctas64c;
+    // the main stream waits for every list before the hit read-back
+    for (int i = 0; i < pfc_batch::kStreams; ++i) {
+        CK(cudaEventRecord(b->ev_end[i], b->st[i]));
+        CK(cudaStreamWaitEvent(c->st, b->ev_end[i], 0));
+    }
+    uint64_t n32 = 0, n64 = 0;
+    for (int k = 0; k < pfc_batch::kKinds; ++k) {
+        n32 += b->ctas[0][k];
+        n64 += b->ctas[1][k] + b->ctas[2][k];
+    }
+    b->tasks += n32 + n64;
+    b->t32_n = n32;
+    b->t64_n = n64;
     CK(cudaMemcpyAsync(b->h_hitcount, b->hitcount.p, sizeof(unsigned long long), cudaMemcpyDeviceToHost, c->st));
     return PFC_OK;
 }
@@ -878,11 +906,15 @@ int finish_iteration(pfc_batch *b, uint32_t L) {
     CK(cudaStreamSynchronize(c->st));
     ++b->iterations;
     float ms32 = 0, ms64 = 0;
-    CK(cudaEventElapsedTime(&ms32, b->ev_start, b->ev_end32));
-    CK(cudaEventElapsedTime(&ms64, b->ev_start, b->ev_end64));
-    b->gpu32_s += (b->t32_n ? ms32 : 0) * 1e-3;
-    b->gpu64_s += (b->t64_n ? ms64 : 0) * 1e-3;
-    b->gpu_s += std::max(b->t32_n ? ms32 : 0.f, b->t64_n ? ms64 : 0.f) * 1e-3;
+    for (int i = 0; i < pfc_batch::kStreams; ++i) {
+        if (!b->used[i]) continue;
+        float ms = 0;
+        CK(cudaEventElapsedTime(&ms, b->ev_start, b->ev_end[i]));
+        (i < 3 ? ms32 : ms64) = std::max(i < 3 ? ms32 : ms64, ms);
+    }
+    b->gpu32_s += ms32 * 1e-3;
+    b->gpu64_s += ms64 * 1e-3;
+    b->gpu_s += std::max(ms32, ms64) * 1e-3;
     const unsigned long long nh = *b->h_hitcount;
     if (nh > b->hits.n) {
         for (BatchJob *j : b->running) j->rerun = true;
@@ -900,8 +932,7 @@ int finish_iteration(pfc_batch *b, uint32_t L) {
     }
     if (nh) CK(cudaMemsetAsync(b->hitcount.p, 0, sizeof(unsigned long long), c->st));
     if (b->trace) {
-        float ms = 0;
-        cudaEventElapsedTime(&ms, b->ev_start, b->t64_n ? b->ev_end64 : b->ev_end32);
+        const float ms = std::max(ms32, ms64);
         fprintf(stderr, "batch iter %llu: running %zu prio %u L %u tasks %zu/%zu hits %llu gpu %.2f ms\n",
                 (unsigned long long)b->iterations, b->running.size(), b->prio, L, b->t32_n, b->t64_n, nh, ms);
     }
@@ -983,12 +1014,12 @@ extern "C" int pfc_batch_create(pfc_ctx *c, pfc_batch **out) {
     pfc_batch *b = new (std::nothrow) pfc_batch();
     if (!b) return PFC_ERR_NOMEM;
     b->ctx = c;
-    cudaError_t e = cudaStreamCreateWithFlags(&b->st32, cudaStreamNonBlocking);
-    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b->st64, cudaStreamNonBlocking);
+    cudaError_t e = cudaSuccess;
+    for (int i = 0; i < pfc_batch::kStreams && e == cudaSuccess; ++i)
+        e = cudaStreamCreateWithFlags(&b->st[i], cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->ev, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreate(&b->ev_start);
-    if (e == cudaSuccess) e = cudaEventCreate(&b->ev_end32);
-    if (e == cudaSuccess) e = cudaEventCreate(&b->ev_end64);
+    for (int i = 0; i < pfc_batch::kStreams && e == cudaSuccess; ++i) e = cudaEventCreate(&b->ev_end[i]);
     if (e == cudaSuccess) e = b->stats.alloc(c, pfc_batch::kSlots);
     if (e == cudaSuccess) e = b->jobs32.alloc(c, pfc_batch::kSlots);
     if (e == cudaSuccess) e = b->jobs64.alloc(c, pfc_batch::kSlots);
@@ -1015,16 +1046,15 @@ extern "C" int pfc_batch_destroy(pfc_batch *b) {
     if (!b) return PFC_ERR_ARG;
     pfc_ctx *c = b->ctx;
     cudaSetDevice(c->device);
-    if (b->st32) cudaStreamSynchronize(b->st32);
-    if (b->st64) cudaStreamSynchronize(b->st64);
+    for (int i = 0; i < pfc_batch::kStreams; ++i)
+        if (b->st[i]) cudaStreamSynchronize(b->st[i]);
     cudaStreamSynchronize(c->st);
     for (auto &kv : b->all) release_device(b, kv.second.get());
     b->stats.release(c);
     b->jobs32.release(c);
     b->jobs64.release(c);
-    b->wins32.release(c);
-    b->wins64.release(c);
-    b->wins64c.release(c);
+    for (auto &row : b->wins)
+        for (auto &d : row) d.release(c);
     b->hits.release(c);
     b->tags.release(c);
     b->hitcount.release(c);
@@ -1032,10 +1062,10 @@ extern "C" int pfc_batch_destroy(pfc_batch *b) {
     if (b->h_hitcount) cudaFreeHost(b->h_hitcount);
     if (b->ev) cudaEventDestroy(b->ev);
     if (b->ev_start) cudaEventDestroy(b->ev_start);
-    if (b->ev_end32) cudaEventDestroy(b->ev_end32);
-    if (b->ev_end64) cudaEventDestroy(b->ev_end64);
-    if (b->st32) cudaStreamDestroy(b->st32);
-    if (b->st64) cudaStreamDestroy(b->st64);
+    for (int i = 0; i < pfc_batch::kStreams; ++i) {
+        if (b->ev_end[i]) cudaEventDestroy(b->ev_end[i]);
+        if (b->st[i]) cudaStreamDestroy(b->st[i]);
+    }
     delete b;
     return PFC_OK;
 }
@@ -1084,7 +1114,9 @@ extern "C" int pfc_batch_step(pfc_batch *b, uint32_t *active, uint32_t *queued) 
     const double ts = now_s();
     for (int pass = 0; pass < 2; ++pass) {
         const uint32_t L = build_tasks(b);
-        const bool work = b->ctas32 + b->ctas64 + b->ctas64c > 0;
+        bool work = false;
+        for (auto &row : b->ctas)
+            for (uint64_t n : row) work |= n > 0;
         if (work) {
             const int rc = launch_iteration(b);
             if (rc) return rc;
