@@ -176,3 +176,27 @@ def test_hit_capacity_is_fixed_while_searches_run(ctx):
         with pytest.raises(pfc.PFCError):
             b.set_hit_capacity(128)
         b.run()
+
+
+def test_memory_budget_admission():
+    """A context whose budget holds only some of the searches at once: the
+    rest wait in the queue until running ones retire, and every result still
+    equals the stand-alone one."""
+    cases = [(1, 2000, 6000, 2**40 + k * 10**8, 2**40 + k * 10**8 + 2 * 10**7) for k in range(6)]
+    with pfc.Context(0, budget=96 << 20) as small:
+        with pfc.Batch(small) as b:
+            ids = [b.submit(*c) for c in cases]
+            max_active, saw_queue = 0, False
+            while True:
+                active, queued = b.step()
+                max_active = max(max_active, active)
+                saw_queue |= active > 0 and queued > 0
+                if active == 0 and queued == 0:
+                    break
+            assert saw_queue and max_active < len(cases)
+            got = [batched(b, jid) for jid in ids]
+    with pfc.Context(0) as big:
+        for case, g in zip(cases, got):
+            want = alone(big, case)
+            assert g[:2] == want[:2], case
+            assert np.array_equal(g[2], want[2]), case
