@@ -79,9 +79,10 @@ int pfc_ctx_destroy(pfc_ctx *ctx);
 void *pfc_ctx_stream(pfc_ctx *ctx);
 
 /* pfc_segment runs the part of a segment after candidate generation (setup,
- * walk launches, check, stats read-back) as a CUDA graph captured once per
- * job and replayed for every segment (re-captured when a buffer or a kernel
- * choice changes).  On by default; off (`on` = 0, or PFCSIEVE_CUDA_GRAPHS=0 in
+ * walk launches, check, stats read-back) as a CUDA graph captured at the
+ * job's second segment and replayed for the later ones (re-captured when a
+ * buffer or a kernel choice changes; a job's first segment runs on the
+ * stream, so one-segment searches pay no capture).  On by default; off (`on` = 0, or PFCSIEVE_CUDA_GRAPHS=0 in
  * the environment when the context is created) runs the same launches on the
  * stream.  Results are identical. */
 int pfc_ctx_set_graphs(pfc_ctx *ctx, int on);

@@ -454,31 +454,40 @@ def sieve(mode, nmin, nmax, pmin, pmax, device=0, threads=2, verify=True, ctx=No
     walked in at least `segments` segments (each at most the size the library
     suggests) and the CPU verification of one segment's hits runs in a worker
     thread while the GPU works on the next (the C calls release the GIL);
-    smaller searches run as library-sized segments, where fixed per-segment
-    costs would outweigh the overlap.  Segments are disjoint p ranges in increasing order, so
-    the concatenated kept factors are sorted and the checksum addends add up:
-    the result equals one verification of all hits."""
+    smaller searches run as library-sized segments with one verification at
+    the end, where a worker thread and extra segments would cost more than the
+    overlap gains.  Segments are disjoint p ranges in increasing order, so the
+    concatenated kept factors are sorted and the checksum addends add up: the
+    result equals one verification of all hits."""
     import concurrent.futures as cf
+    import math
 
     own = ctx is None
     ctx = ctx or Context(device)
     try:
-        with Job(ctx, mode, nmin, nmax, pmin, pmax) as job, cf.ThreadPoolExecutor(1) as pool:
-            import math
-            pairs_est = (pmax - pmin) / math.log(max(pmin, 3)) * max(nmax - nmin, 1)
-            parts_wanted = max(segments, 1) if pairs_est >= 1e11 else 1
-            span = max((pmax - pmin + parts_wanted - 1) // parts_wanted, 1)
-            futs, nhits, lo = [], 0, pmin
-            while lo < pmax:
-                hi = min(job.segment_end(lo), lo + span, pmax)
-                job.segment(lo, hi)
-                h = job.drain_hits()
-                nhits += len(h)
-                futs.append(pool.submit(finalize, mode, nmax, h, threads, verify))
-                lo = hi
-            termsum, primecount = job.totals()
-            pairs = job.pairs
-            parts = [f.result() for f in futs]
+        pairs_est = (pmax - pmin) / math.log(max(pmin, 3)) * max(nmax - nmin, 1)
+        parts_wanted = max(segments, 1) if pairs_est >= 1e11 else 1
+        with Job(ctx, mode, nmin, nmax, pmin, pmax) as job:
+            if parts_wanted == 1:
+                hits = job.run()
+                termsum, primecount = job.totals()
+                pairs = job.pairs
+                parts = [finalize(mode, nmax, hits, threads=threads, verify=verify)]
+                nhits = len(hits)
+            else:
+                span = max((pmax - pmin + parts_wanted - 1) // parts_wanted, 1)
+                with cf.ThreadPoolExecutor(1) as pool:
+                    futs, nhits, lo = [], 0, pmin
+                    while lo < pmax:
+                        hi = min(job.segment_end(lo), lo + span, pmax)
+                        job.segment(lo, hi)
+                        h = job.drain_hits()
+                        nhits += len(h)
+                        futs.append(pool.submit(finalize, mode, nmax, h, threads, verify))
+                        lo = hi
+                    termsum, primecount = job.totals()
+                    pairs = job.pairs
+                    parts = [f.result() for f in futs]
         kept = np.concatenate([k for k, _ in parts]) if parts else np.zeros(0, dtype=FACTOR_DTYPE)
         add = sum(a for _, a in parts)
         return SieveResult(factorcount=len(kept), primecount=primecount,

@@ -44,6 +44,7 @@ struct pfc_job {
     DArr<uint32_t> primebits;
     DArr<uint32_t> qlist;
     DArr<uint32_t> cmult;       // compositorial multipliers of the current chunk
+    DArr<uint32_t> ramp;        // the combined search's factorial multipliers (n) of the chunk
     std::vector<uint32_t> h_qlist;
 
     DevClass<uint32_t> c32;
@@ -62,13 +63,14 @@ struct pfc_job {
     // the post-generation part of a segment captured as a CUDA graph, replayed
     // while the key (buffers, launch shapes, kernel choices) is unchanged
     struct GraphKey {
-        const void *p32, *p64, *hits, *cmult;
+        const void *p32, *p64, *hits, *cmult, *ramp;
         uint64_t cap32, cap64, hitcap;
         int lazy, use32, use64, var[3][2];
     };
     cudaGraphExec_t graph = nullptr;
     GraphKey gkey{};
     uint64_t graph_kernels = 0;
+    uint64_t segments = 0;   // segments committed (the first one runs without a graph)
 };
 
 // ------------------------------------------------------------------ helpers
@@ -180,6 +182,7 @@ static int job_release(pfc_job *j) {
     j->primebits.release(c);
     j->qlist.release(c);
     j->cmult.release(c);
+    j->ramp.release(c);
     j->c32.release(c);
     j->c64.release(c);
     j->hits.release(c);
@@ -410,13 +413,20 @@ static int enqueue_iter_range(pfc_job *j, uint32_t lo, uint32_t hi) {
         return PFC_OK;
     }
     if (j->mode & PFC_COMPOSITORIAL) {
+        // multiplier tables of the chunk: compositorial (n or 1) and, for the
+        // fused walk, factorial (n; the plain factorial walk forms n itself,
+        // shared by its two candidates, and gains nothing from a table)
         const size_t need = ((size_t)(hi - lo) + 15) & ~(size_t)15;
-        if (j->cmult.n < need) CK(j->cmult.alloc(c, std::max<size_t>(need, 4096)));
-        c->launches += launch_cmult(j->cmult.p, j->primebits.p, j->nmin, lo, hi, c->st);
+        const bool comp = true, fact = (j->mode & PFC_FACTORIAL) != 0;
+        if (comp && j->cmult.n < need) CK(j->cmult.alloc(c, std::max<size_t>(need, 4096)));
+        if (fact && j->ramp.n < need) CK(j->ramp.alloc(c, std::max<size_t>(need, 4096)));
+        c->launches += launch_cmult(comp ? j->cmult.p : nullptr, fact ? j->ramp.p : nullptr, j->primebits.p,
+                                    j->nmin, lo, hi, c->st);
         w.base = lo;
     }
     if (j->mode == (PFC_FACTORIAL | PFC_COMPOSITORIAL)) {
         // one launch walks both chains of each candidate
+        w.mult = j->ramp.p;
         w.mult2 = j->cmult.p;
         w.type = PFC_TYPE_FACTORIAL;
         w.type2 = PFC_TYPE_COMPOSITORIAL;
@@ -502,6 +512,7 @@ static int commit_segment(pfc_job *j) {
     j->primecount += (uint64_t)s.counts[0] + s.counts[1];
     j->pairs += ((uint64_t)s.counts[0] + s.counts[1]) * (uint64_t)(j->nmax - j->nmin);
     j->stage = 3;
+    ++j->segments;
     return PFC_OK;
 }
 
@@ -556,13 +567,15 @@ static int segment_body_graph(pfc_job *j) {
         const uint64_t n32 = j->c32.p.p ? j->c32.cap : 0, n64 = j->c64.p.p ? j->c64.cap : 0;
         const size_t L = std::min(chunk_len(n32 + 3 * n64, 1.5e11), kMaxChunk);
         const size_t need = (((size_t)std::min<uint64_t>(L, iter_end(j) - iter_begin(j))) + 15) & ~(size_t)15;
-        if (j->cmult.n < need) CK(j->cmult.alloc(c, std::max<size_t>(need, 4096)));
+        if ((j->mode & PFC_COMPOSITORIAL) && j->cmult.n < need) CK(j->cmult.alloc(c, std::max<size_t>(need, 4096)));
+        if ((j->mode & PFC_FACTORIAL) && j->ramp.n < need) CK(j->ramp.alloc(c, std::max<size_t>(need, 4096)));
     }
     pfc_job::GraphKey k{};
     k.p32 = j->c32.p.p;
     k.p64 = j->c64.p.p;
     k.hits = j->hits.p;
     k.cmult = j->cmult.p;
+    k.ramp = j->ramp.p;
     k.cap32 = j->c32.cap;
     k.cap64 = j->c64.cap;
     k.hitcap = j->hits.n;
@@ -620,7 +633,9 @@ extern "C" int pfc_segment(pfc_job *j, uint64_t p_lo, uint64_t p_hi) {
     }
     const unsigned long long hit_base = j->h_stats->hits;
     for (int attempt = 0;; ++attempt) {
-        rc = c->graphs ? segment_body_graph(j) : segment_body_stream(j);
+        // a graph pays off from the second segment of a job on: capturing and
+        // instantiating it costs about as much as one small segment
+        rc = (c->graphs && j->segments > 0) ? segment_body_graph(j) : segment_body_stream(j);
         if (rc) return rc;
         j->stage = 2;
         j->next_it = iter_end(j);

@@ -116,8 +116,9 @@ int launch_walk64(const ClassBuf<uint64_t> &c, const WalkArgs &a, const HitBuf &
 int walk_variant_count(int cls, bool fused);
 int walk_variant_shape(int cls, bool fused, int variant, int *nc, int *b);
 // compositorial multipliers of n in [lo, hi): n when composite, 1 when prime
-// (bit k of primebits <-> n = nmin + k); `out` is padded with 1 to a multiple of 16
-int launch_cmult(uint32_t *out, const uint32_t *primebits, uint32_t nmin, uint32_t lo, uint32_t hi,
+// (bit k of primebits <-> n = nmin + k); `out` is padded with 1 to a multiple of
+// 16; `ramp` (may be null) receives n itself, the factorial's multipliers
+int launch_cmult(uint32_t *out, uint32_t *ramp, const uint32_t *primebits, uint32_t nmin, uint32_t lo, uint32_t hi,
                  cudaStream_t st);
 int launch_check32(const ClassBuf<uint32_t> &c, const CheckArgs &a, cudaStream_t st);
 int launch_check64(const ClassBuf<uint64_t> &c, const CheckArgs &a, cudaStream_t st);

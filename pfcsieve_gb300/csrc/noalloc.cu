@@ -272,7 +272,7 @@ extern "C" int pfc_segment_noalloc(unsigned mode, uint32_t nmin, uint32_t nmax, 
             w.type = PFC_TYPE_PRIMORIAL;
         } else {
             if (mode & PFC_COMPOSITORIAL) {
-                launch_cmult(cm, bits, nmin, a, b, st);
+                launch_cmult(cm, nullptr, bits, nmin, a, b, st);
                 w.base = a;
             }
             if (mode == (PFC_FACTORIAL | PFC_COMPOSITORIAL)) {

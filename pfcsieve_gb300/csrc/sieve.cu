@@ -80,16 +80,23 @@ __global__ void __launch_bounds__(256) walk_kernel(ClassBuf<typename T::W> c, Wa
     }
 }
 
-__global__ void cmult_kernel(uint32_t *out, const uint32_t *primebits, uint32_t nmin, uint32_t lo, uint32_t len,
-                             uint32_t padded) {
+// Multiplier tables of one chunk [lo, lo + len): the compositorial's (n at
+// composite n, 1 at prime n) when `out` is set and the factorial's (n) when
+// `ramp` is set; the walks load them four at a time, which costs fewer
+// instructions than forming n in every step.
+__global__ void cmult_kernel(uint32_t *out, uint32_t *ramp, const uint32_t *primebits, uint32_t nmin, uint32_t lo,
+                             uint32_t len, uint32_t padded) {
     for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < padded; k += gridDim.x * blockDim.x) {
-        uint32_t v = 1u;
-        if (k < len) {
-            const uint32_t n = lo + k, off = n - nmin;
-            const bool prime = (__ldg(primebits + (off >> 5)) >> (off & 31)) & 1u;
-            v = prime ? 1u : n;
+        if (out) {
+            uint32_t v = 1u;
+            if (k < len) {
+                const uint32_t n = lo + k, off = n - nmin;
+                const bool prime = (__ldg(primebits + (off >> 5)) >> (off & 31)) & 1u;
+                v = prime ? 1u : n;
+            }
+            out[k] = v;
         }
-        out[k] = v;
+        if (ramp) ramp[k] = lo + k;
     }
 }
 
@@ -217,13 +224,13 @@ int launch_walk64(const ClassBuf<uint64_t> &c, const WalkArgs &a, const HitBuf &
     return lazy ? launch_walk<Cls64L>(c, a, h, st, 1, variant) : launch_walk<Cls64>(c, a, h, st, 2, variant);
 }
 
-int launch_cmult(uint32_t *out, const uint32_t *primebits, uint32_t nmin, uint32_t lo, uint32_t hi,
+int launch_cmult(uint32_t *out, uint32_t *ramp, const uint32_t *primebits, uint32_t nmin, uint32_t lo, uint32_t hi,
                  cudaStream_t st) {
     const uint32_t len = hi - lo, padded = (len + 15u) & ~15u;
     unsigned blocks = (padded + 255) / 256;
     if (blocks > 4096) blocks = 4096;
     if (!padded) return 0;
-    cmult_kernel<<<blocks, 256, 0, st>>>(out, primebits, nmin, lo, len, padded);
+    cmult_kernel<<<blocks, 256, 0, st>>>(out, ramp, primebits, nmin, lo, len, padded);
     return 1;
 }
 

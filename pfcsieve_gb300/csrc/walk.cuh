@@ -298,7 +298,7 @@ __device__ __forceinline__ void walk_streams(const typename T::M (&m)[NC], typen
         K[s] = T::K(m[s], B);
     }
 
-    const uint32_t *mult0 = FUSED ? nullptr : a.mult;
+    const uint32_t *mult0 = a.mult;   // fused: the factorial's n from a table, or computed when null
     const uint32_t *mult1 = a.mult2;
     const bool vec = ((a.lo - a.base) & 3u) == 0;
     uint32_t k = a.lo;
@@ -327,7 +327,7 @@ __device__ __forceinline__ void walk_streams(const typename T::M (&m)[NC], typen
         }
         if (__any_sync(kFull, any)) {
             if (FUSED) {
-                replay_chain<T>(m[0], xs[0], nullptr, a.base, k, B, a.type, act[0], h);
+                replay_chain<T>(m[0], xs[0], mult0, a.base, k, B, a.type, act[0], h);
                 replay_chain<T>(m[0], xs[NS - 1], mult1, a.base, k, B, a.type2, act[0], h);
             } else {
 #pragma unroll
@@ -370,7 +370,7 @@ __device__ __forceinline__ void walk_streams(const typename T::M (&m)[NC], typen
         }
         if (__any_sync(kFull, any)) {
             if (FUSED) {
-                replay_chain<T>(m[0], xs[0], nullptr, a.base, k, r, a.type, act[0], h);
+                replay_chain<T>(m[0], xs[0], mult0, a.base, k, r, a.type, act[0], h);
                 replay_chain<T>(m[0], xs[NS - 1], mult1, a.base, k, r, a.type2, act[0], h);
             } else {
 #pragma unroll
