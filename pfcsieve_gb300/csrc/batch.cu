@@ -116,14 +116,16 @@ __device__ __forceinline__ void run_setup(const typename T::M (&m)[NC], typename
             using SW = typename T::SW;
             const SW *wp = static_cast<const SW *>(J.words) + g.z + off;
             uint32_t k = 0;
-            for (; k + 4 <= cnt; k += 4) {
-                const SW w0 = ldg(wp + k), w1 = ldg(wp + k + 1), w2 = ldg(wp + k + 2), w3 = ldg(wp + k + 3);
+            // wide words are unrolled by two, narrow ones by four (registers)
+            constexpr uint32_t U = sizeof(SW) > 8 ? 2 : 4;
+            for (; k + U <= cnt; k += U) {
+                SW wv[U];
+#pragma unroll
+                for (uint32_t u = 0; u < U; ++u) wv[u] = ldg(wp + k + u);
 #pragma unroll
                 for (int c = 0; c < NC; ++c) {
-                    acc[c] = T::word(m[c], acc[c], w0);
-                    acc[c] = T::word(m[c], acc[c], w1);
-                    acc[c] = T::word(m[c], acc[c], w2);
-                    acc[c] = T::word(m[c], acc[c], w3);
+#pragma unroll
+                    for (uint32_t u = 0; u < U; ++u) acc[c] = T::word(m[c], acc[c], wv[u]);
                 }
             }
             for (; k < cnt; ++k) {
@@ -280,7 +282,7 @@ __device__ void run_task(const JobDev<typename T::W> &J, const Task &t, const Hi
 // path's throughput on a single large search, against 100% with hardware
 // dispatch.)  Thread 0 finds its window by binary search over first_cta.
 template <class T, int KIND>
-__global__ void __launch_bounds__(256, (sizeof(typename T::W) == 4 || (KIND != kAnyTask && T::B > 8)) ? 3 : 2)
+__global__ void __launch_bounds__(256, KIND == kSetupTask ? 4 : ((sizeof(typename T::W) == 4 || (KIND != kAnyTask && T::B > 8)) ? 3 : 2))
     batch_kernel(const Window *wins, uint32_t nwins, const JobDev<typename T::W> *jobs, HitBuf h) {
     // the task and its search record live in shared memory: every thread
     // reads the same fields, and registers stay free for the residues
@@ -342,6 +344,7 @@ struct BatchJob {
     DevClass<uint64_t> c64;
     uint32_t n32 = 0, n64 = 0;      // candidates per class
     uint32_t pos32 = 0, pos64 = 0;  // timeline position of all blocks of a class
+    uint32_t next32 = 0, next64 = 0;  // end of the window in flight
     uint32_t tot32 = 0, tot64 = 0;  // timeline lengths (setup positions + walk steps)
     uint32_t win = 0;               // this iteration's window (0: the common window L)
     bool wait = false;              // latency policy: no window this iteration
@@ -803,11 +806,18 @@ uint32_t build_tasks(pfc_batch *b) {
 
     std::vector<std::pair<double, Window>> lists[pfc_batch::kLists][pfc_batch::kKinds];
     for (BatchJob *j : b->running) {
+        j->next32 = j->pos32;
+        j->next64 = j->pos64;
         for (int cls = 0; cls < 2; ++cls) {
             const uint32_t pos = cls ? j->pos64 : j->pos32, tot = cls ? j->tot64 : j->tot32;
             const uint32_t ns = cls ? j->nsetup64 : j->nsetup32, n = cls ? j->n64 : j->n32;
             if (pos >= tot || n == 0 || j->wait) continue;
-            const uint32_t hi = (uint32_t)std::min<uint64_t>((uint64_t)pos + (j->win ? j->win : L), tot);
+            uint32_t hi = (uint32_t)std::min<uint64_t>((uint64_t)pos + (j->win ? j->win : L), tot);
+            // a window that reaches the end of the setup stops there: the walk
+            // starts in the next iteration, in the walk kernel, and the general
+            // kernel (lower occupancy) only ends timelines without walk steps
+            if (pos < ns && hi > ns) hi = ns;
+            (cls ? j->next64 : j->next32) = hi;
             const PosCost c = pos_cost(j, cls != 0);
             const uint32_t per = per_cta(j, cls != 0);
             const double setup = pos < ns ? (double)(std::min(hi, ns) - pos) : 0.0;
@@ -936,10 +946,9 @@ int finish_iteration(pfc_batch *b, uint32_t L) {
         fprintf(stderr, "batch iter %llu: running %zu prio %u L %u tasks %zu/%zu hits %llu gpu %.2f ms\n",
                 (unsigned long long)b->iterations, b->running.size(), b->prio, L, b->t32_n, b->t64_n, nh, ms);
     }
-    for (BatchJob *j : b->running) {
-        const uint64_t w = j->wait ? 0 : (j->win ? j->win : L);
-        j->pos32 = (uint32_t)std::min<uint64_t>((uint64_t)j->pos32 + w, j->tot32);
-        j->pos64 = (uint32_t)std::min<uint64_t>((uint64_t)j->pos64 + w, j->tot64);
+    for (BatchJob *j : b->running) {  // the windows' ends (build_tasks)
+        j->pos32 = j->next32;
+        j->pos64 = j->next64;
     }
     return PFC_OK;
 }
