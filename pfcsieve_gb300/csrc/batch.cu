@@ -282,7 +282,7 @@ __device__ void run_task(const JobDev<typename T::W> &J, const Task &t, const Hi
 // path's throughput on a single large search, against 100% with hardware
 // dispatch.)  Thread 0 finds its window by binary search over first_cta.
 template <class T, int KIND>
-__global__ void __launch_bounds__(256, KIND == kSetupTask ? 4 : ((sizeof(typename T::W) == 4 || (KIND != kAnyTask && T::B > 8)) ? 3 : 2))
+__global__ void __launch_bounds__(256, KIND == kSetupTask ? 4 : (((sizeof(typename T::W) == 4 && KIND != kWalkTask) || (sizeof(typename T::W) == 8 && KIND != kAnyTask && T::B > 8)) ? 3 : 2))
     batch_kernel(const Window *wins, uint32_t nwins, const JobDev<typename T::W> *jobs, HitBuf h) {
     // the task and its search record live in shared memory: every thread
     // reads the same fields, and registers stay free for the residues
