@@ -5,7 +5,7 @@
 //   class-32 candidates: p, s0, s1 (u32) and nnext (u32)   16 B / candidate
 //   class-64 candidates: p, s0, s1 (u64) and nnext (u32)   28 B / candidate
 //   hit list pfc_factor[hitcap] + 64-bit counter
-//   setup programs (u32 words for class 32; 256-bit words below 2^64/3 and
+//   setup programs (u32 words for class 32; 896-bit words below 2^64/3 and
 //   u64 words above for class 64), prime flags of [nmin, nmax) (1 bit per n)
 //   or the prime list of [nmin, nmax) for the primorial walk
 //   per-segment accumulators: counts[2], termsum, flags
@@ -39,7 +39,7 @@ struct pfc_job {
 
     DevProg<uint32_t> a32, b32;
     DevProg<uint64_t> a64, b64;   // class 64 at or above 2^64/3 (64-bit words)
-    DevProg<WideWord> aw, bw;     // class 64 below 2^64/3 (256-bit words)
+    DevProg<WideWord> aw, bw;     // class 64 below 2^64/3 (896-bit words)
     uint64_t setup_mulmods32 = 0, setup_mulmods64 = 0;
     DArr<uint32_t> primebits;
     DArr<uint32_t> qlist;

@@ -6,8 +6,9 @@
 //             walk residues are signed, in (-p, p) (redc31s).
 //   class 64: p >= 2^31, Montgomery with R = 2^64; below 2^64/3 the walk
 //             takes lazy one-word steps with R = 2^32 and residues in
-//             [0, 2p) (redc64l), and the setup multiplies by 256-bit table
-//             words in eight lazy rounds (mul_wide_word).
+//             [0, 2p) (redc64l), and the setup folds each 896-bit table
+//             word into 96 bits and multiplies it in with three lazy
+//             rounds (mul_wide_word).
 //
 // The reference keeps every residue in Montgomery form with R = 2^64
 // (kernels/iterate.cl:44-50: m_mul(a,b) = a*b/2^64 mod p in [0,p)).  Values
@@ -204,8 +205,7 @@ __device__ __forceinline__ uint64_t cios_round(uint64_t c, uint64_t s, uint32_t 
 // s*W*2^(-32L) (mod p) for an L-limb word W (32-bit limbs, little-endian),
 // s in [0, 2p), p < 2^64/3: one plain lazy round (c = 0) and L-1
 // accumulating rounds, then one conditional subtraction: result in [0, 2p).
-// The multiply-pipe cost per factor bit is about half that of multiplying by
-// 64-bit words with the 64x64 Montgomery product.
+// The setup uses it with L = 3 on a table word already folded to 96 bits.
 template <int L>
 __device__ __forceinline__ uint64_t mul_wide_word(uint64_t s, const uint32_t (&w)[L], uint64_t p, uint32_t q) {
     uint64_t c = redc64l(s, w[0], p, q);

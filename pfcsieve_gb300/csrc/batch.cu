@@ -95,6 +95,9 @@ __device__ __forceinline__ void run_setup(const typename T::M (&m)[NC], typename
                                           typename T::W (&fork)[NC], const JobDev<typename T::W> &J, uint32_t lo,
                                           uint32_t hi) {
     using W = typename T::W;
+    typename T::SC sc[NC];
+#pragma unroll
+    for (int c = 0; c < NC; ++c) sc[c] = T::sctx(m[c]);
     uint32_t a = 0, b = J.nsegs;  // segs[a].start <= lo
     while (b - a > 1) {
         const uint32_t mid = (a + b) >> 1;
@@ -116,22 +119,29 @@ __device__ __forceinline__ void run_setup(const typename T::M (&m)[NC], typename
             using SW = typename T::SW;
             const SW *wp = static_cast<const SW *>(J.words) + g.z + off;
             uint32_t k = 0;
-            // wide words are unrolled by two, narrow ones by four (registers)
-            constexpr uint32_t U = sizeof(SW) > 8 ? 2 : 4;
-            for (; k + U <= cnt; k += U) {
-                SW wv[U];
+            if constexpr (std::is_same<SW, WideWord>::value) {
+                // wide words are read inside T::word
+                for (; k < cnt; ++k) {
 #pragma unroll
-                for (uint32_t u = 0; u < U; ++u) wv[u] = ldg(wp + k + u);
-#pragma unroll
-                for (int c = 0; c < NC; ++c) {
-#pragma unroll
-                    for (uint32_t u = 0; u < U; ++u) acc[c] = T::word(m[c], acc[c], wv[u]);
+                    for (int c = 0; c < NC; ++c) acc[c] = T::word(m[c], sc[c], acc[c], wp + k);
                 }
-            }
-            for (; k < cnt; ++k) {
-                const SW w = ldg(wp + k);
+            } else {
+                constexpr uint32_t U = 4;
+                for (; k + U <= cnt; k += U) {
+                    SW wv[U];
 #pragma unroll
-                for (int c = 0; c < NC; ++c) acc[c] = T::word(m[c], acc[c], w);
+                    for (uint32_t u = 0; u < U; ++u) wv[u] = ldg(wp + k + u);
+#pragma unroll
+                    for (int c = 0; c < NC; ++c) {
+#pragma unroll
+                        for (uint32_t u = 0; u < U; ++u) acc[c] = T::word(m[c], sc[c], acc[c], wv[u]);
+                    }
+                }
+                for (; k < cnt; ++k) {
+                    const SW w = ldg(wp + k);
+#pragma unroll
+                    for (int c = 0; c < NC; ++c) acc[c] = T::word(m[c], sc[c], acc[c], w);
+                }
             }
         } else {
 #pragma unroll
@@ -281,8 +291,19 @@ __device__ void run_task(const JobDev<typename T::W> &J, const Task &t, const Hi
 // the last tasks of an iteration crowd onto a few SMs: 78% of the per-job
 // path's throughput on a single large search, against 100% with hardware
 // dispatch.)  Thread 0 finds its window by binary search over first_cta.
+//
+// CTAs per SM by kind (register budgets at 256 threads: 4 -> 64, 3 -> 85,
+// 2 -> 128): setup with narrow words at four; setup with 896-bit words
+// holds 32 position residues per thread; walks as measured per class.
 template <class T, int KIND>
-__global__ void __launch_bounds__(256, KIND == kSetupTask ? 4 : (((sizeof(typename T::W) == 4 && KIND != kWalkTask) || (sizeof(typename T::W) == 8 && KIND != kAnyTask && T::B > 8)) ? 3 : 2))
+constexpr int batch_min_ctas() {
+    if (KIND == kSetupTask) return std::is_same<typename T::SW, WideWord>::value ? 2 : 4;
+    if (sizeof(typename T::W) == 4) return KIND != kWalkTask ? 3 : 2;
+    return (KIND != kAnyTask && T::B > 8) ? 3 : 2;
+}
+
+template <class T, int KIND>
+__global__ void __launch_bounds__(256, batch_min_ctas<T, KIND>())
     batch_kernel(const Window *wins, uint32_t nwins, const JobDev<typename T::W> *jobs, HitBuf h) {
     // the task and its search record live in shared memory: every thread
     // reads the same fields, and registers stay free for the residues
@@ -410,7 +431,7 @@ static void prepare_job(BatchJob *j, const std::vector<uint32_t> &cache) {
     const std::vector<uint32_t> below(primes.begin(), std::upper_bound(primes.begin(), primes.end(), startN));
     const unsigned mode = j->mode;
     const bool fc = mode == (PFC_FACTORIAL | PFC_COMPOSITORIAL);
-    const bool wide = j->pmax <= kLazyEnd;  // class 64 with 256-bit words
+    const bool wide = j->pmax <= kLazyEnd;  // class 64 with 896-bit words
     HostProg<uint32_t> a32, b32;
     HostProg<uint64_t> a64, b64;
     HostProg<WideWord> aw, bw;
@@ -713,14 +734,15 @@ int admit_prepared(pfc_batch *b) {
 // Returns the window length used.
 // Cost of timeline positions in IMAD-equivalent multiplies per candidate
 // (measured multiply-pipe rates: class-32 step 6; class-64 lazy step 10.5
-// plus its share of the block restore; a 256-bit setup word eight lazy rounds)
+// plus its share of the block restore; an 896-bit setup word 64 wide
+// multiply-adds and three lazy rounds)
 struct PosCost {
     double setup, walk;
 };
 static PosCost pos_cost(const BatchJob *j, bool cls64) {
     const double chains = j->mode == (PFC_FACTORIAL | PFC_COMPOSITORIAL) ? 2.0 : 1.0;
     if (!cls64) return {6.0, 6.0 * chains};
-    if (j->pmax <= kLazyEnd) return {85.0, 12.0 * chains};
+    if (j->pmax <= kLazyEnd) return {175.0, 12.0 * chains};
     return {60.0, 30.0 * chains};
 }
 

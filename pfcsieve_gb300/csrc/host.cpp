@@ -86,9 +86,6 @@ template <class W>
 static inline u128 word_max() { return (u128)(W)~(W)0; }
 template <class W>
 static inline W to_word(u128 v) { return (W)v; }
-// R = 2^64 powers a word removes (R = 2^32 for the class-32 words)
-template <class W>
-static constexpr int word_drift() { return sizeof(W) == sizeof(WideWord) ? kWideLimbs / 2 : 1; }
 
 // greedy: consecutive factors multiplied while the product fits a word
 template <class W>
@@ -102,27 +99,50 @@ static void pack_words(const std::vector<uint32_t> &f, std::vector<W> &words) {
     }
 }
 
-// 256-bit words: the product kept as eight 32-bit limbs, a factor joining
-// while the product still fits
+// 896-bit words: the product is built in 64-bit limbs over the limbs in use,
+// two factors (< 2^62) per multiplication while both fit, then one, and the
+// finished word is cut into 28-bit limbs
 template <>
 void pack_words<WideWord>(const std::vector<uint32_t> &f, std::vector<WideWord> &words) {
+    constexpr int L64 = kWideLimbs * kWideRadixBits / 64;
+    static_assert(L64 * 64 == kWideLimbs * kWideRadixBits, "whole 64-bit limbs");
+    constexpr uint64_t mask = (1ull << kWideRadixBits) - 1u;
     size_t i = 0;
     while (i < f.size()) {
-        WideWord acc{};
-        acc.limb[0] = f[i++];
+        uint64_t a[L64] = {};
+        int used = 1;
+        a[0] = f[i++];
         while (i < f.size()) {
-            WideWord next{};
-            uint64_t carry = 0;
-            for (int k = 0; k < kWideLimbs; ++k) {
-                const uint64_t t = (uint64_t)acc.limb[k] * f[i] + carry;
-                next.limb[k] = (uint32_t)t;
-                carry = t >> 32;
+            bool joined = false;
+            for (int take = i + 1 < f.size() ? 2 : 1; take >= 1 && !joined; --take) {
+                const uint64_t m = take == 2 ? (uint64_t)f[i] * f[i + 1] : (uint64_t)f[i];
+                uint64_t b[L64];
+                u128 carry = 0;
+                for (int k = 0; k < used; ++k) {
+                    const u128 t = (u128)a[k] * m + carry;
+                    b[k] = (uint64_t)t;
+                    carry = t >> 64;
+                }
+                int nu = used;
+                if (carry) {
+                    if (used == L64) continue;  // would not fit in 896 bits
+                    b[nu++] = (uint64_t)carry;
+                }
+                std::copy(b, b + nu, a);
+                used = nu;
+                i += (size_t)take;
+                joined = true;
             }
-            if (carry) break;  // would not fit in 256 bits
-            acc = next;
-            ++i;
+            if (!joined) break;
         }
-        words.push_back(acc);
+        WideWord w{};
+        for (int k = 0; k < kWideLimbs; ++k) {
+            const int bit = k * kWideRadixBits, x = bit / 64, sh = bit % 64;
+            uint64_t v = a[x] >> sh;
+            if (sh + kWideRadixBits > 64 && x + 1 < L64) v |= a[x + 1] << (64 - sh);
+            w.limb[k] = (uint32_t)(v & mask);
+        }
+        words.push_back(w);
     }
 }
 
@@ -139,7 +159,7 @@ static bool finish_prog(HostProg<W> &p) {
             d = 2 * d - 1;
             if (-d > lim) return false;
         }
-        d -= (__int128)word_drift<W>() * (p.groups[g + 1] - p.groups[g]);
+        d -= (__int128)(p.groups[g + 1] - p.groups[g]);
     }
     for (uint32_t k = 0; k < p.final_sq; ++k) {
         d = 2 * d - 1;

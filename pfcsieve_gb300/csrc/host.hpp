@@ -6,9 +6,12 @@
 
 namespace pfc {
 
-// 256-bit setup table word (class 64 below 2^64/3): eight little-endian
-// 32-bit limbs, read on the device with two 16-byte loads
-constexpr int kWideLimbs = 8;
+// 896-bit setup table word (class 64 below 2^64/3): a product of primes as
+// 32 little-endian limbs of 28 bits (each limb in the low bits of a u32),
+// read on the device with eight 16-byte loads.  The 28-bit radix lets the
+// device sum limb x residue products in 64-bit accumulators without carries.
+constexpr int kWideLimbs = 32;
+constexpr int kWideRadixBits = 28;
 struct alignas(16) WideWord {
     uint32_t limb[kWideLimbs];
 };
@@ -20,8 +23,7 @@ std::vector<uint32_t> primes_between(uint32_t lo, uint32_t hi);
 
 // Setup program on the host: words, groups {begin, end, squarings}, final
 // squarings and the drift correction exponent (see kernels.cuh Prog).  Each
-// 32- or 64-bit word lowers the power of R of the device value by one, each
-// 256-bit word by four.
+// word, of any width, lowers the power of R of the device value by one.
 template <class W>
 struct HostProg {
     std::vector<W> words;

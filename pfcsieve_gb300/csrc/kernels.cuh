@@ -77,7 +77,7 @@ struct WalkArgs {
 // size classes: class 32 holds p < 2^31, class 64 the rest
 constexpr uint64_t kClassSplit = 1ull << 31;
 // class-64 segments whose candidates are all below kLazyEnd (3p < 2^64) set
-// up with 256-bit table words and walk with lazy one-word steps
+// up with 896-bit table words and walk with lazy one-word steps
 constexpr uint64_t kLazyEnd = 0x5555555555555556ull;
 constexpr uint64_t kLazyWalkEnd = kLazyEnd;
 
@@ -104,7 +104,7 @@ struct GenArgs {
 int launch_gen(const GenArgs &a, int sms, cudaStream_t st);
 int launch_setup32(const ClassBuf<uint32_t> &c, const SetupArgs<uint32_t> &a, cudaStream_t st);
 int launch_setup64(const ClassBuf<uint64_t> &c, const SetupArgs<uint64_t> &a, cudaStream_t st);
-// class 64 below 2^64/3 with 256-bit table words
+// class 64 below 2^64/3 with 896-bit table words
 int launch_setup64w(const ClassBuf<uint64_t> &c, const SetupArgs<WideWord> &a, cudaStream_t st);
 // walk launches: `variant` indexes the walk variants of the size class
 // (0 = default; see walk_variant_shape)

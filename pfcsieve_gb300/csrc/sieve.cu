@@ -19,12 +19,13 @@ __global__ void __launch_bounds__(256) setup_kernel(ClassBuf<typename T::W> c, S
     if (i >= cnt) return;
     typename T::M m;
     m.init(c.p[i]);
+    const typename T::SC sc = T::sctx(m);
     W s0, s1 = 0;
     if (a.mode == (PFC_FACTORIAL | PFC_COMPOSITORIAL)) {
-        s1 = run_prog<T>(m, a.a, m.one);      // (n-1)!/(n-1)#
-        s0 = run_prog<T>(m, a.b, s1);         // (n-1)! = that * (n-1)#
+        s1 = run_prog<T>(m, sc, a.a, m.one);      // (n-1)!/(n-1)#
+        s0 = run_prog<T>(m, sc, a.b, s1);         // (n-1)! = that * (n-1)#
     } else {
-        s0 = run_prog<T>(m, a.a, m.one);
+        s0 = run_prog<T>(m, sc, a.a, m.one);
     }
     c.s0[i] = s0;
     c.s1[i] = s1;

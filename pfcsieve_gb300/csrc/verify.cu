@@ -5,7 +5,7 @@
 // comparing (kernels/verifyslow.cl, kernels/verify.cl, cl_sieve.cpp:917-970,
 // 1100-1140, 1270-1310); a mismatch ends the run.  Here the fast side is the
 // job's own setup program run by the production setup kernel on a test prime
-// its arithmetic accepts (2^31 - 1 for class-32 words, 2^62 - 57 for 256-bit
+// its arithmetic accepts (2^31 - 1 for class-32 words, 2^62 - 57 for 896-bit
 // words, 2^64 - 59 for 64-bit words), and the slow side is a grid-stride
 // product over k in [2, n0 - 1] split into primes and composites by a
 // deterministic Miller-Rabin test (bases 2, 7, 61, exact below 4.76e9), which

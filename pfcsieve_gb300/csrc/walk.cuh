@@ -83,7 +83,9 @@ struct Cls32 {
     __device__ static __forceinline__ W step(const M &m, W s, uint32_t n) { return redc32(s, n, m.p, m.pinv); }
     // setup: table words of the class (SW) and squarings
     using SW = uint32_t;
-    __device__ static __forceinline__ W word(const M &m, W s, SW w) { return redc32(s, w, m.p, m.pinv); }
+    struct SC {};
+    __device__ static __forceinline__ SC sctx(const M &) { return {}; }
+    __device__ static __forceinline__ W word(const M &m, const SC &, W s, SW w) { return redc32(s, w, m.p, m.pinv); }
     __device__ static __forceinline__ W sq(const M &m, W s) { return m.mul(s, s); }
     // checksum form: residue * 2^64 mod p from its class-32 Montgomery form
     __device__ static __forceinline__ uint64_t term(const M &m, W s) { return m.mul(s, m.r2); }
@@ -115,7 +117,9 @@ struct Cls64 {
     __device__ static __forceinline__ W canon(const M &, W x) { return x; }
     __device__ static __forceinline__ W step(const M &m, W s, uint32_t n) { return redc64_u32(s, n, m.p, m.pinv); }
     using SW = uint64_t;
-    __device__ static __forceinline__ W word(const M &m, W s, SW w) { return redc64(s, w, m.p, m.pinv); }
+    struct SC {};
+    __device__ static __forceinline__ SC sctx(const M &) { return {}; }
+    __device__ static __forceinline__ W word(const M &m, const SC &, W s, SW w) { return redc64(s, w, m.p, m.pinv); }
     __device__ static __forceinline__ W sq(const M &m, W s) { return m.mul(s, s); }
     __device__ static __forceinline__ uint64_t term(const M &, W s) { return s; }
     __device__ static __forceinline__ uint64_t mont64_of(const M &m, uint32_t v) { return m.to_mont(v); }
@@ -164,11 +168,53 @@ struct Cls64L {
         return c >= 2 * m.p ? c - m.p : c;
     }
     __device__ static __forceinline__ W step(const M &m, W s, uint32_t n) { return canon(m, redc64l(s, n, m.p, m.q32)); }
-    // setup (p < 2^64/3): 256-bit table words, each lowering the power of
-    // R = 2^64 by four; values stay in [0, 2p), canonical before a squaring
+    // setup (p < 2^64/3): 896-bit table words Z = sum z_i 2^(28 i) (limbs
+    // z_i < 2^28).  Per candidate the residues w_i = 2^(28 i + 32) mod p
+    // (canonical) are kept in registers; a word is folded into 96 bits as
+    // T = sum z_i w_i = Z 2^32 (mod p) with one wide multiply-add per limb and
+    // 32-bit half (z_i lo(w_i) < 2^60: sixteen terms per 64-bit accumulator;
+    // z_i hi(w_i) < 2^58.5: all 32 in one), then s <- s T 2^-96 = s Z R^-1 by
+    // three lazy rounds.  Each word lowers the power of R = 2^64 by one;
+    // values stay in [0, 2p), canonical before a squaring.
     using SW = WideWord;
-    __device__ static __forceinline__ W word(const M &m, W s, const SW &w) {
-        return mul_wide_word<kWideLimbs>(s, w.limb, m.p, m.q32);
+    struct SC {
+        uint64_t w[kWideLimbs];
+    };
+    // from the top: w_31 = 2^900 = Mont(2^(64*14)) 2^-32 2^-28, then
+    // w_i = w_(i+1) 2^-28 = redc(w_(i+1) * 16), one lazy round each
+    static_assert(kWideRadixBits == 28 && kWideLimbs % 16 == 0, "2^(28(L-1)+92) must be a power of R");
+    __device__ static __forceinline__ SC sctx(const M &m) {
+        SC c;
+        constexpr uint64_t kTop = (28ull * (kWideLimbs - 1) + 92) / 64 - 1;
+        uint64_t x = redc64l(m.mont_R_pow(kTop), 1u, m.p, m.q32);
+#pragma unroll
+        for (int i = kWideLimbs - 1; i >= 0; --i) {
+            x = canon(m, redc64l(x, 16u, m.p, m.q32));
+            c.w[i] = x;
+        }
+        return c;
+    }
+    __device__ static __forceinline__ W word(const M &m, const SC &c, W s, const SW *wp) {
+        const uint4 *v = reinterpret_cast<const uint4 *>(wp);
+        uint64_t u0 = 0, u1 = 0, hv = 0;
+#pragma unroll
+        for (int k = 0; k < kWideLimbs / 4; ++k) {
+            const uint4 z4 = __ldg(v + k);
+            const uint32_t z[4] = {z4.x, z4.y, z4.z, z4.w};
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const int i = 4 * k + j;
+                const uint64_t lo = (uint64_t)z[j] * (uint32_t)c.w[i];
+                if (i < kWideLimbs / 2) u0 += lo;
+                else u1 += lo;
+                hv += (uint64_t)z[j] * (uint32_t)(c.w[i] >> 32);
+            }
+        }
+        // T = u0 + u1 + hv 2^32 < 2^96 as three 32-bit limbs
+        const uint64_t u = u0 + u1;
+        const uint64_t mid = (u >> 32) + ((uint64_t)(u < u0) << 32) + hv;
+        const uint32_t t[3] = {(uint32_t)u, (uint32_t)mid, (uint32_t)(mid >> 32)};
+        return mul_wide_word<3>(s, t, m.p, m.q32);
     }
     __device__ static __forceinline__ W sq(const M &m, W s) {
         s = canon(m, s);
@@ -180,27 +226,28 @@ struct Cls64L {
 
 template <class W>
 __device__ __forceinline__ W ldg(const W *p) { return __ldg(p); }
-__device__ __forceinline__ WideWord ldg(const WideWord *p) {
-    const uint4 *v = reinterpret_cast<const uint4 *>(p);
-    const uint4 a = __ldg(v), b = __ldg(v + 1);
-    return WideWord{{a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w}};
-}
 
 // Evaluate a setup program from Montgomery-form `acc` (see kernels.cuh Prog).
+// Wide words are read inside T::word; narrow ones are loaded four at a time.
 template <class T>
-__device__ typename T::W run_prog(const typename T::M &m, const Prog<typename T::SW> &pg, typename T::W acc) {
+__device__ typename T::W run_prog(const typename T::M &m, const typename T::SC &sc, const Prog<typename T::SW> &pg,
+                                  typename T::W acc) {
     for (uint32_t g = 0; g < pg.ngroups; ++g) {
         const uint32_t b = __ldg(pg.groups + 3 * g), e = __ldg(pg.groups + 3 * g + 1);
         const uint32_t sq = __ldg(pg.groups + 3 * g + 2);
         for (uint32_t k = 0; k < sq; ++k) acc = T::sq(m, acc);
         uint32_t i = b;
-        for (; i + 4 <= e; i += 4) {
-            acc = T::word(m, acc, ldg(pg.words + i));
-            acc = T::word(m, acc, ldg(pg.words + i + 1));
-            acc = T::word(m, acc, ldg(pg.words + i + 2));
-            acc = T::word(m, acc, ldg(pg.words + i + 3));
+        if constexpr (std::is_same<typename T::SW, WideWord>::value) {
+            for (; i < e; ++i) acc = T::word(m, sc, acc, pg.words + i);
+        } else {
+            for (; i + 4 <= e; i += 4) {
+                acc = T::word(m, sc, acc, ldg(pg.words + i));
+                acc = T::word(m, sc, acc, ldg(pg.words + i + 1));
+                acc = T::word(m, sc, acc, ldg(pg.words + i + 2));
+                acc = T::word(m, sc, acc, ldg(pg.words + i + 3));
+            }
+            for (; i < e; ++i) acc = T::word(m, sc, acc, ldg(pg.words + i));
         }
-        for (; i < e; ++i) acc = T::word(m, acc, ldg(pg.words + i));
     }
     for (uint32_t k = 0; k < pg.final_sq; ++k) acc = T::sq(m, acc);
     return m.mul(acc, m.mont_R_pow(pg.corr));
