@@ -229,7 +229,8 @@ int pfc_format_factor(const pfc_factor *f, char *buf, size_t cap);
  * Limits (PFC_ERR_ARG beyond them): at most 2^18 expected candidates per size
  * class (p < 2^31 and p >= 2^31; roughly (p_hi - p_lo) / ln p_lo <= 2^18 / 1.25),
  * nmax - nmin <= 2^22, at most 2^18 primes in [nmin, nmax) for n#, and setup
- * tables of at most 2^17 32-bit and 2^16 64-bit words (nmin up to a few 10^5).
+ * tables of at most 2^12 896-bit words (p < 2^31) and 2^16 64-bit words
+ * (p >= 2^31): nmin up to a few 10^5.
  *
  * The first call on each device resolves the device address of the array and
  * stores the sieve patterns in it; make that first call before any stream

@@ -37,7 +37,7 @@ struct pfc_job {
     uint32_t nmin = 0, nmax = 0;
     uint64_t pmin = 0, pmax = 0;
 
-    DevProg<uint32_t> a32, b32;
+    DevProg<WideWord> a32, b32;   // class 32 (896-bit words)
     DevProg<uint64_t> a64, b64;   // class 64 at or above 2^64/3 (64-bit words)
     DevProg<WideWord> aw, bw;     // class 64 below 2^64/3 (896-bit words)
     uint64_t setup_mulmods32 = 0, setup_mulmods64 = 0;
@@ -227,7 +227,7 @@ extern "C" int pfc_job_create(pfc_ctx *c, unsigned mode, uint32_t nmin, uint32_t
     const uint32_t plim = (mode & PFC_COMPOSITORIAL) ? nmax : std::max(startN, nmax - 1);
     const std::vector<uint32_t> primes = primes_between(2, plim);
     const std::vector<uint32_t> below(primes.begin(), std::upper_bound(primes.begin(), primes.end(), startN));
-    HostProg<uint32_t> a32, b32;
+    HostProg<WideWord> a32, b32;
     HostProg<uint64_t> a64, b64;
     HostProg<WideWord> aw, bw;
     const bool need32 = pmin < kClassSplit;
@@ -342,7 +342,7 @@ extern "C" int pfc_gen_candidates(pfc_job *j, uint64_t p_lo, uint64_t p_hi) {
 
 static int enqueue_setup(pfc_job *j) {
     pfc_ctx *c = j->ctx;
-    SetupArgs<uint32_t> s32;
+    SetupArgs<WideWord> s32;
     s32.mode = j->mode;
     s32.a = j->a32.view;
     s32.b = j->b32.view;
@@ -839,8 +839,8 @@ extern "C" int pfc_job_verify_tables(pfc_job *j, uint64_t *table_bytes) {
         const uint64_t p = kVerifyPrime[f.t];
         uint64_t s0 = 0, s1 = 0;
         if (f.form == 0) {
-            rc = setup_on_prime<uint32_t, uint32_t>(j, j->a32, j->b32, p, s0, s1);
-            bytes += (j->a32.words.n + j->b32.words.n) * 4;
+            rc = setup_on_prime<uint32_t, WideWord>(j, j->a32, j->b32, p, s0, s1);
+            bytes += (j->a32.words.n + j->b32.words.n) * sizeof(WideWord);
         } else if (f.form == 1) {
             rc = setup_on_prime<uint64_t, WideWord>(j, j->aw, j->bw, p, s0, s1);
             bytes += (j->aw.words.n + j->bw.words.n) * sizeof(WideWord);

@@ -293,17 +293,29 @@ __device__ void run_task(const JobDev<typename T::W> &J, const Task &t, const Hi
 // dispatch.)  Thread 0 finds its window by binary search over first_cta.
 //
 // CTAs per SM by kind (register budgets at 256 threads: 4 -> 64, 3 -> 85,
-// 2 -> 128): setup with narrow words at four; setup with 896-bit words
-// holds 32 position residues per thread; walks as measured per class.
+// 2 -> 128): setup with 64-bit words at four; setup with 896-bit words holds
+// 32 position residues per candidate (two candidates per thread in class 32)
+// and the general kind both setup and walk state; walks as measured per class.
 template <class T, int KIND>
 constexpr int batch_min_ctas() {
     if (KIND == kSetupTask) return std::is_same<typename T::SW, WideWord>::value ? 2 : 4;
-    if (sizeof(typename T::W) == 4) return KIND != kWalkTask ? 3 : 2;
-    return (KIND != kAnyTask && T::B > 8) ? 3 : 2;
+    if (KIND == kAnyTask || sizeof(typename T::W) == 4) return 2;
+    return T::B > 8 ? 3 : 2;
 }
 
+// Class-32 setup windows run one candidate per thread in CTAs of 512 (the
+// shape of setup_kernel: 64 registers, 32 warps per SM); the two-candidate
+// form at 256 threads ran a setup-bound search at half that speed.  Every
+// other kind: 256 threads, T::NC candidates per thread (one in the fused walk).
 template <class T, int KIND>
-__global__ void __launch_bounds__(256, batch_min_ctas<T, KIND>())
+__host__ __device__ constexpr bool setup32_shape() { return KIND == kSetupTask && sizeof(typename T::W) == 4; }
+template <class T, int KIND>
+__host__ __device__ constexpr int task_threads() { return setup32_shape<T, KIND>() ? 512 : 256; }
+template <class T, int KIND>
+__host__ __device__ constexpr int task_nc() { return setup32_shape<T, KIND>() ? 1 : T::NC; }
+
+template <class T, int KIND>
+__global__ void __launch_bounds__(task_threads<T, KIND>(), setup32_shape<T, KIND>() ? 2 : batch_min_ctas<T, KIND>())
     batch_kernel(const Window *wins, uint32_t nwins, const JobDev<typename T::W> *jobs, HitBuf h) {
     // the task and its search record live in shared memory: every thread
     // reads the same fields, and registers stay free for the residues
@@ -318,7 +330,7 @@ __global__ void __launch_bounds__(256, batch_min_ctas<T, KIND>())
         }
         const Window w = wins[a];
         sj = jobs[w.slot];
-        const uint32_t per = (sj.mode == (PFC_FACTORIAL | PFC_COMPOSITORIAL) ? 1u : (uint32_t)T::NC) * blockDim.x;
+        const uint32_t per = (sj.mode == (PFC_FACTORIAL | PFC_COMPOSITORIAL) ? 1u : (uint32_t)task_nc<T, KIND>()) * blockDim.x;
         st.slot = w.slot;
         st.first = (blockIdx.x - w.first_cta) * per;
         st.count = min(per, w.ncand - st.first);
@@ -329,7 +341,7 @@ __global__ void __launch_bounds__(256, batch_min_ctas<T, KIND>())
     HitBuf hh = h;
     hh.tagval = st.slot;
     if (sj.mode == (PFC_FACTORIAL | PFC_COMPOSITORIAL)) run_task<T, 1, true, KIND>(sj, st, hh);
-    else run_task<T, T::NC, false, KIND>(sj, st, hh);
+    else run_task<T, task_nc<T, KIND>(), false, KIND>(sj, st, hh);
 }
 
 // ------------------------------------------------------------------ host side
@@ -347,7 +359,8 @@ struct BatchJob {
     uint32_t slot = 0;
     // host tables, built by prepare_job
     int prep_rc = PFC_OK;
-    std::vector<uint32_t> words32, cmult, qlist;
+    std::vector<WideWord> words32;     // class 32
+    std::vector<uint32_t> cmult, qlist;
     std::vector<uint64_t> words64;   // class 64 at or above 2^64/3
     std::vector<WideWord> wordsw;      // class 64 below 2^64/3
     std::vector<SetupSeg> segs32, segs64;
@@ -357,7 +370,8 @@ struct BatchJob {
     bool use32 = false, use64 = false;
     uint32_t cap32 = 0, cap64 = 0;
     // device
-    DArr<uint32_t> d_words32, d_cmult, d_qlist;
+    DArr<WideWord> d_words32;
+    DArr<uint32_t> d_cmult, d_qlist;
     DArr<uint64_t> d_words64;
     DArr<WideWord> d_wordsw;
     DArr<SetupSeg> d_segs32, d_segs64;
@@ -432,7 +446,7 @@ static void prepare_job(BatchJob *j, const std::vector<uint32_t> &cache) {
     const unsigned mode = j->mode;
     const bool fc = mode == (PFC_FACTORIAL | PFC_COMPOSITORIAL);
     const bool wide = j->pmax <= kLazyEnd;  // class 64 with 896-bit words
-    HostProg<uint32_t> a32, b32;
+    HostProg<WideWord> a32, b32;
     HostProg<uint64_t> a64, b64;
     HostProg<WideWord> aw, bw;
     const bool ok = build_progs(mode, startN, primes, below, a32, b32) &&
@@ -734,14 +748,15 @@ int admit_prepared(pfc_batch *b) {
 // Returns the window length used.
 // Cost of timeline positions in IMAD-equivalent multiplies per candidate
 // (measured multiply-pipe rates: class-32 step 6; class-64 lazy step 10.5
-// plus its share of the block restore; an 896-bit setup word 64 wide
-// multiply-adds and three lazy rounds)
+// plus its share of the block restore; an 896-bit setup word 32 wide
+// multiply-adds and two rounds in class 32, 64 and three lazy rounds in
+// class 64)
 struct PosCost {
     double setup, walk;
 };
 static PosCost pos_cost(const BatchJob *j, bool cls64) {
     const double chains = j->mode == (PFC_FACTORIAL | PFC_COMPOSITORIAL) ? 2.0 : 1.0;
-    if (!cls64) return {6.0, 6.0 * chains};
+    if (!cls64) return {85.0, 6.0 * chains};
     if (j->pmax <= kLazyEnd) return {175.0, 12.0 * chains};
     return {60.0, 30.0 * chains};
 }
@@ -754,9 +769,10 @@ static double class_cost(uint32_t n, uint32_t pos, uint32_t ns, uint32_t tot, Po
     return (double)n * (setup * c.setup + walk * c.walk);
 }
 
-// candidates per CTA of a class
-static uint32_t per_cta(const BatchJob *j, bool cls64) {
+// candidates per CTA of a class and task kind (as batch_kernel computes them)
+static uint32_t per_cta(const BatchJob *j, bool cls64, int kind) {
     if (cls64) return 256u * Cls64L::NC;
+    if (kind == kSetupTask) return 512u;
     return j->mode == (PFC_FACTORIAL | PFC_COMPOSITORIAL) ? 256u : 256u * Cls32::NC;
 }
 
@@ -795,11 +811,12 @@ uint32_t build_tasks(pfc_batch *b) {
         double jrate = 0, worst = 0;
         if (j->pos32 < j->tot32) {
             jrate += j->n32 * (j->pos32 < j->nsetup32 ? c32.setup : c32.walk);
-            worst = std::max(worst, per_cta(j, false) * std::max(c32.setup, c32.walk));
+            worst = std::max(worst, std::max(per_cta(j, false, kSetupTask) * c32.setup,
+                                             per_cta(j, false, kWalkTask) * c32.walk));
         }
         if (j->pos64 < j->tot64) {
             jrate += j->n64 * (j->pos64 < j->nsetup64 ? c64.setup : c64.walk);
-            worst = std::max(worst, per_cta(j, true) * std::max(c64.setup, c64.walk));
+            worst = std::max(worst, per_cta(j, true, kSetupTask) * std::max(c64.setup, c64.walk));
         }
         j->win = 0;
         j->wait = false;
@@ -841,7 +858,8 @@ uint32_t build_tasks(pfc_batch *b) {
             if (pos < ns && hi > ns) hi = ns;
             (cls ? j->next64 : j->next32) = hi;
             const PosCost c = pos_cost(j, cls != 0);
-            const uint32_t per = per_cta(j, cls != 0);
+            const int kind = (hi <= ns && hi < tot) ? kSetupTask : (pos >= ns ? kWalkTask : kAnyTask);
+            const uint32_t per = per_cta(j, cls != 0, kind);
             const double setup = pos < ns ? (double)(std::min(hi, ns) - pos) : 0.0;
             const double walk = hi > ns ? (double)(hi - std::max(pos, ns)) : 0.0;
             const double cost = (double)std::min(per, n) * (setup * c.setup + walk * c.walk);
@@ -852,7 +870,6 @@ uint32_t build_tasks(pfc_batch *b) {
             w.lo = pos;
             w.hi = hi;
             const int l = cls == 0 ? 0 : (j->pmax <= kLazyEnd ? 1 : 2);
-            const int kind = (hi <= ns && hi < tot) ? kSetupTask : (pos >= ns ? kWalkTask : kAnyTask);
             lists[l][kind].push_back({cost, w});
         }
     }
@@ -877,8 +894,8 @@ static void launch_list(pfc_batch *b, int l, const JobDev<typename T::W> *jobs, 
     const uint64_t n = b->ctas[l][KIND];
     if (!n) return;
     const int si = (l == 0 ? 0 : 3) + KIND;
-    batch_kernel<T, KIND><<<(unsigned)n, 256, 0, b->st[si]>>>(b->wins[l][KIND].p, (uint32_t)b->w[l][KIND].size(),
-                                                              jobs, h);
+    batch_kernel<T, KIND><<<(unsigned)n, task_threads<T, KIND>(), 0, b->st[si]>>>(
+        b->wins[l][KIND].p, (uint32_t)b->w[l][KIND].size(), jobs, h);
     b->used[si] = true;
     b->ctx->launches++;
 }

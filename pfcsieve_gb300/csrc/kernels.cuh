@@ -102,7 +102,7 @@ struct GenArgs {
 
 // Launch wrappers (enqueue on `st`); return the number of kernels launched.
 int launch_gen(const GenArgs &a, int sms, cudaStream_t st);
-int launch_setup32(const ClassBuf<uint32_t> &c, const SetupArgs<uint32_t> &a, cudaStream_t st);
+int launch_setup32(const ClassBuf<uint32_t> &c, const SetupArgs<WideWord> &a, cudaStream_t st);
 int launch_setup64(const ClassBuf<uint64_t> &c, const SetupArgs<uint64_t> &a, cudaStream_t st);
 // class 64 below 2^64/3 with 896-bit table words
 int launch_setup64w(const ClassBuf<uint64_t> &c, const SetupArgs<WideWord> &a, cudaStream_t st);

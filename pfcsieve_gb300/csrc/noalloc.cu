@@ -31,7 +31,7 @@ namespace {
 
 // ----- limits of one call (the scratch layout below is sized for them)
 constexpr uint32_t kCands = 1u << 18;        // candidates per size class
-constexpr uint32_t kWords32 = 1u << 17;      // setup program words, class 32
+constexpr uint32_t kWords32 = 1u << 12;      // setup program words, class 32 (896-bit)
 constexpr uint32_t kWords64 = 1u << 16;      // setup program words, class 64
 constexpr uint32_t kGroups = 256;            // setup program groups (x3 u32) in all
 constexpr uint32_t kNRange = 1u << 22;       // nmax - nmin
@@ -46,7 +46,7 @@ constexpr size_t kOffPat = align256(kOffStats + 64);                      // sie
 constexpr size_t kOffC32 = align256(kOffPat + kPatEntries * 8);           // p,s0,s1,nnext u32
 constexpr size_t kOffC64 = align256(kOffC32 + (size_t)kCands * 16);       // p,s0,s1 u64 + nnext
 constexpr size_t kOffW32 = align256(kOffC64 + (size_t)kCands * 28);
-constexpr size_t kOffW64 = align256(kOffW32 + (size_t)kWords32 * 4);
+constexpr size_t kOffW64 = align256(kOffW32 + (size_t)kWords32 * sizeof(WideWord));
 constexpr size_t kOffGrp = align256(kOffW64 + (size_t)kWords64 * 8);
 constexpr size_t kOffBits = align256(kOffGrp + (size_t)kGroups * 12);
 constexpr size_t kOffQ = align256(kOffBits + ((size_t)kNRange / 32 + 2) * 4);
@@ -132,7 +132,7 @@ extern "C" int pfc_segment_noalloc(unsigned mode, uint32_t nmin, uint32_t nmax, 
     const uint32_t plim = (mode & PFC_COMPOSITORIAL) ? nmax : std::max(startN, nmax ? nmax - 1 : 0);
     const std::vector<uint32_t> primes = primes_between(2, plim);
     const std::vector<uint32_t> below(primes.begin(), std::upper_bound(primes.begin(), primes.end(), startN));
-    HostProg<uint32_t> a32, b32;
+    HostProg<WideWord> a32, b32;
     HostProg<uint64_t> a64, b64;
     bool ok = true;
     if (mode == PFC_FACTORIAL) ok = build_power_prog(startN, 0, primes, a32) && build_power_prog(startN, 0, primes, a64);
@@ -166,7 +166,7 @@ extern "C" int pfc_segment_noalloc(unsigned mode, uint32_t nmin, uint32_t nmax, 
 
     Stats *stats = reinterpret_cast<Stats *>(base + kOffStats);
     uint32_t *counts = &stats->counts[0];
-    uint32_t *w32 = reinterpret_cast<uint32_t *>(base + kOffW32);
+    WideWord *w32 = reinterpret_cast<WideWord *>(base + kOffW32);
     uint64_t *w64 = reinterpret_cast<uint64_t *>(base + kOffW64);
     uint32_t *grp = reinterpret_cast<uint32_t *>(base + kOffGrp);
     uint32_t *bits = reinterpret_cast<uint32_t *>(base + kOffBits);
@@ -197,7 +197,7 @@ extern "C" int pfc_segment_noalloc(unsigned mode, uint32_t nmin, uint32_t nmax, 
         return p;
     };
     size_t wo32 = 0, wo64 = 0, go = 0;
-    SetupArgs<uint32_t> s32;
+    SetupArgs<WideWord> s32;
     SetupArgs<uint64_t> s64;
     s32.mode = s64.mode = mode;
     s32.nnext0 = s64.nnext0 = 0;

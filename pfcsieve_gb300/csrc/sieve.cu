@@ -132,7 +132,7 @@ __global__ void __launch_bounds__(256) check_kernel(ClassBuf<typename T::W> c, C
 
 static inline unsigned grid_for(uint32_t cap) { return (cap + 255) / 256; }
 
-int launch_setup32(const ClassBuf<uint32_t> &c, const SetupArgs<uint32_t> &a, cudaStream_t st) {
+int launch_setup32(const ClassBuf<uint32_t> &c, const SetupArgs<WideWord> &a, cudaStream_t st) {
     if (!c.cap) return 0;
     setup_kernel<Cls32><<<grid_for(c.cap), 256, 0, st>>>(c, a);
     return 1;

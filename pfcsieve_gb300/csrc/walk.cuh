@@ -81,11 +81,48 @@ struct Cls32 {
     __device__ static __forceinline__ W restore(const M &m, W x, W K) { return fstep(m, x, K); }
     __device__ static __forceinline__ W canon(const M &m, W x) { return (int32_t)x < 0 ? x + m.p : x; }
     __device__ static __forceinline__ W step(const M &m, W s, uint32_t n) { return redc32(s, n, m.p, m.pinv); }
-    // setup: table words of the class (SW) and squarings
-    using SW = uint32_t;
-    struct SC {};
-    __device__ static __forceinline__ SC sctx(const M &) { return {}; }
-    __device__ static __forceinline__ W word(const M &m, const SC &, W s, SW w) { return redc32(s, w, m.p, m.pinv); }
+    // setup: 896-bit table words Z = sum z_i 2^(28 i) (limbs z_i < 2^28) and
+    // squarings, canonical residues.  Per candidate the residues
+    // w_i = 2^(28 i + 32) mod p < 2^31 are kept in registers; a word is folded
+    // as T = sum z_i w_i = Z 2^32 (mod p), one wide multiply-add per limb
+    // (each term < 2^59: all 32 in one 64-bit accumulator), then
+    // s <- s T 2^-64 = s Z R^-1 by two Montgomery rounds on the 32-bit halves
+    // of T.  Each word lowers the power of R = 2^32 by one.
+    using SW = WideWord;
+    struct SC {
+        uint32_t w[kWideLimbs];
+    };
+    __device__ static __forceinline__ SC sctx(const M &m) {
+        SC c;
+        const uint32_t k60 = m.mul(m.r2, 1u << kWideRadixBits);   // 2^60 mod p
+        uint32_t x = m.one;                                         // 2^32 mod p
+#pragma unroll
+        for (int i = 0; i < kWideLimbs; ++i) {
+            c.w[i] = x;
+            x = m.mul(x, k60);                                      // x 2^28
+        }
+        return c;
+    }
+    // s < p: both rounds stay below 2^64 (s t < 2^63, m p < 2^63) and the
+    // result is below 2p before the conditional subtraction
+    __device__ static __forceinline__ W word(const M &m, const SC &c, W s, const SW *wp) {
+        const uint4 *v = reinterpret_cast<const uint4 *>(wp);
+        uint64_t t = 0;
+#pragma unroll
+        for (int k = 0; k < kWideLimbs / 4; ++k) {
+            const uint4 z = __ldg(v + k);
+            t += (uint64_t)z.x * c.w[4 * k];
+            t += (uint64_t)z.y * c.w[4 * k + 1];
+            t += (uint64_t)z.z * c.w[4 * k + 2];
+            t += (uint64_t)z.w * c.w[4 * k + 3];
+        }
+        const uint32_t q = 0u - m.pinv;
+        const uint64_t a = (uint64_t)s * (uint32_t)t;
+        const uint64_t b = (a + (uint64_t)((uint32_t)a * q) * m.p) >> 32;
+        const uint64_t d = b + (uint64_t)s * (uint32_t)(t >> 32);
+        const uint32_t r = (uint32_t)((d + (uint64_t)((uint32_t)d * q) * m.p) >> 32);
+        return r >= m.p ? r - m.p : r;
+    }
     __device__ static __forceinline__ W sq(const M &m, W s) { return m.mul(s, s); }
     // checksum form: residue * 2^64 mod p from its class-32 Montgomery form
     __device__ static __forceinline__ uint64_t term(const M &m, W s) { return m.mul(s, m.r2); }
