@@ -97,3 +97,20 @@ def test_finalize_rejects_false_hit(pfc):
     with pytest.raises(pfc.PFCError) as e:
         pfc.finalize(1, 2000, bad, verify=True)
     assert e.value.code == -6
+
+
+@pytest.mark.parametrize("mode", [1, 2, 4])
+def test_finalize_rejects_flipped_sign(pfc, mode):
+    """A true hit with its sign flipped (p divides n!+1, reported as n!-1) fails
+    the CPU verification in every walk type, at the largest n of the hits
+    (the longest verification product)."""
+    nmin, nmax, pmin, pmax = 101, 30000, 101, 20000
+    hits, _, _ = o.sieve(mode, nmin, nmax, o.candidates(pmin, pmax), os.cpu_count() or 1)
+    assert len(hits)
+    kept, _ = pfc.finalize(mode, nmax, hits.copy(), threads=4, verify=True)
+    bad = hits.copy()
+    i = int(np.argmax(np.abs(bad["nc"])))
+    bad["nc"][i] = -bad["nc"][i]
+    with pytest.raises(pfc.PFCError) as e:
+        pfc.finalize(mode, nmax, bad, threads=4, verify=True)
+    assert e.value.code == -6
