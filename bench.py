@@ -344,10 +344,11 @@ def run_mixed(ctx, njobs, warmup, steps=1):
     same = all((out_b[i].term_checksum, out_b[i].primecount) == (out_p[i].term_checksum, out_p[i].primecount)
                and np.array_equal(hit_order(out_b[i].hits), hit_order(out_p[i].hits))
                for i in range(len(jobs)))
-    # the user's result of every search: verified factors and checksum
+    # the user's result of every search: verified factors and checksum (hits
+    # re-verified on the GPU, sorted and filtered on the CPU)
     t = time.perf_counter()
     for i, s in enumerate(jobs):
-        pfc.finalize(s.mode, s.nmax, out_b[i].hits, threads=os.cpu_count() or 1)
+        pfc.finalize(s.mode, s.nmax, out_b[i].hits, threads=os.cpu_count() or 1, verify="device", ctx=ctx)
     t_fin = time.perf_counter() - t
     pairs = sum(out_b[i].primecount * (s.nmax - s.nmin) for i, s in enumerate(jobs))
     arrivals = sv.poisson_arrivals(len(jobs), 200.0, seed=1)
@@ -363,6 +364,7 @@ def run_mixed(ctx, njobs, warmup, steps=1):
         "plain_pairs_per_s": pairs / t_p,
         "batched_over_plain": t_p / t_b,
         "batched_s": t_b, "plain_s": t_p, "plain_table_build_s": create, "finalize_s": t_fin,
+        "finalize_verify": "device",
         "iterations": int(timing["iterations"]), "tasks": int(timing["tasks"]),
         "identical_results": bool(same and same_s),
         "serving": {"arrivals_per_s": 200.0, "makespan_s": makespan,

@@ -197,6 +197,21 @@ int pfc_job_verify_tables(pfc_job *job, uint64_t *table_bytes);
 int pfc_finalize_factors(unsigned mode, uint32_t nmax, pfc_factor *f, size_t n,
                          int threads, int verify, size_t *kept, uint64_t *checksum);
 
+/* The re-verification of pfc_finalize_factors for n hits at once on the GPU
+ * of `ctx` (no counterpart in the reference, whose check runs on the CPU,
+ * cl_sieve.cpp:509-540): each hit's product of verifyprime.cpp:199-268 -- the
+ * start value of its type (34!, 101#, 44!/44#) times every k in [35, n] for a
+ * factorial hit, or the list of the search's mode (primes in [103, nmax] for
+ * n#, composites in [45, nmax) for n!/n#) up to n -- is formed modulo p as a
+ * plain product split over one warp per hit, and must be 1 for a -1 hit and
+ * p - 1 for a +1 hit.  *failed receives the number of hits that fail; bad
+ * (n bytes, may be NULL) receives 1 for each failing hit and 0 otherwise.
+ * Returns PFC_ERR_VERIFY when any hit fails.  The records are not reordered
+ * or changed: pass them to pfc_finalize_factors with verify = 0 for the sort,
+ * the 2-PRP filter and the checksum.  Synchronises. */
+int pfc_verify_factors_device(pfc_ctx *ctx, unsigned mode, uint32_t nmax, const pfc_factor *f, size_t n,
+                              uint8_t *bad, size_t *failed);
+
 /* Deterministic primality for 64-bit p (verifyprime.cpp:157-195). */
 int pfc_is_prime(uint64_t p);
 

@@ -100,6 +100,7 @@ def lib():
             "pfc_job_verify_tables": (ctypes.c_int, [vp, P(u64)]),
             "pfc_finalize_factors": (ctypes.c_int, [ctypes.c_uint, u32, vp, sz, ctypes.c_int,
                                                     ctypes.c_int, P(sz), P(u64)]),
+            "pfc_verify_factors_device": (ctypes.c_int, [vp, ctypes.c_uint, u32, vp, sz, vp, P(sz)]),
             "pfc_is_prime": (ctypes.c_int, [u64]),
             "pfc_format_factor": (ctypes.c_int, [vp, ctypes.c_char_p, sz]),
             "pfc_status_string": (ctypes.c_char_p, [ctypes.c_int]),
@@ -400,11 +401,35 @@ class Batch:
                 return
 
 
-def finalize(mode, nmax, hits, threads=2, verify=True):
+def verify_factors(ctx, mode, nmax, hits):
+    """Re-verify hits on the GPU of `ctx` (pfc_verify_factors_device).
+
+    Returns a bool array, True for each hit whose verification product is not
+    the +-1 its sign claims; raises nothing for failing hits."""
+    f = np.ascontiguousarray(hits, dtype=FACTOR_DTYPE)
+    bad = np.zeros(len(f), dtype=np.uint8)
+    failed = ctypes.c_size_t(0)
+    rc = lib().pfc_verify_factors_device(ctx.h, mode, nmax, f.ctypes.data if len(f) else None, len(f),
+                                         bad.ctypes.data if len(f) else None, ctypes.byref(failed))
+    if rc not in (0, -6):
+        raise PFCError(rc, "pfc_verify_factors_device")
+    return bad.astype(bool)
+
+
+def finalize(mode, nmax, hits, threads=2, verify=True, ctx=None):
     """Sort, re-verify, drop 2-PRP p and fold n+-1 (cl_sieve.cpp:496-589).
 
+    verify: True re-verifies on the CPU (the reference's check), "device"
+    on the GPU of `ctx` (pfc_verify_factors_device), False not at all; a
+    failing hit raises PFCError(-6) either way.
     Returns (kept factors sorted by (p, |n|, type), checksum addend)."""
     f = np.ascontiguousarray(hits, dtype=FACTOR_DTYPE).copy()
+    if verify == "device":
+        if ctx is None:
+            raise ValueError("verify='device' needs ctx")
+        if verify_factors(ctx, mode, nmax, f).any():
+            raise PFCError(-6, "pfc_verify_factors_device")
+        verify = False
     kept = ctypes.c_size_t(0)
     add = ctypes.c_uint64(0)
     _ck(lib().pfc_finalize_factors(mode, nmax, f.ctypes.data if len(f) else None, len(f), threads,
@@ -458,7 +483,9 @@ def sieve(mode, nmin, nmax, pmin, pmax, device=0, threads=2, verify=True, ctx=No
     the end, where a worker thread and extra segments would cost more than the
     overlap gains.  Segments are disjoint p ranges in increasing order, so the
     concatenated kept factors are sorted and the checksum addends add up: the
-    result equals one verification of all hits."""
+    result equals one verification of all hits.  verify="device" checks the
+    hits on the GPU (pfc_verify_factors_device) after the last segment instead
+    of on the CPU."""
     import concurrent.futures as cf
     import math
 
@@ -467,12 +494,16 @@ def sieve(mode, nmin, nmax, pmin, pmax, device=0, threads=2, verify=True, ctx=No
     try:
         pairs_est = (pmax - pmin) / math.log(max(pmin, 3)) * max(nmax - nmin, 1)
         parts_wanted = max(segments, 1) if pairs_est >= 1e11 else 1
+        on_device = verify == "device"
+        cpu_verify = bool(verify) and not on_device
+        raw = []   # hits for the device check, which runs on this thread (one thread per context)
         with Job(ctx, mode, nmin, nmax, pmin, pmax) as job:
             if parts_wanted == 1:
                 hits = job.run()
                 termsum, primecount = job.totals()
                 pairs = job.pairs
-                parts = [finalize(mode, nmax, hits, threads=threads, verify=verify)]
+                raw.append(hits)
+                parts = [finalize(mode, nmax, hits, threads=threads, verify=cpu_verify)]
                 nhits = len(hits)
             else:
                 span = max((pmax - pmin + parts_wanted - 1) // parts_wanted, 1)
@@ -483,11 +514,14 @@ def sieve(mode, nmin, nmax, pmin, pmax, device=0, threads=2, verify=True, ctx=No
                         job.segment(lo, hi)
                         h = job.drain_hits()
                         nhits += len(h)
-                        futs.append(pool.submit(finalize, mode, nmax, h, threads, verify))
+                        raw.append(h)
+                        futs.append(pool.submit(finalize, mode, nmax, h, threads, cpu_verify))
                         lo = hi
                     termsum, primecount = job.totals()
                     pairs = job.pairs
                     parts = [f.result() for f in futs]
+        if on_device and nhits and verify_factors(ctx, mode, nmax, np.concatenate(raw)).any():
+            raise PFCError(-6, "pfc_verify_factors_device")
         kept = np.concatenate([k for k, _ in parts]) if parts else np.zeros(0, dtype=FACTOR_DTYPE)
         add = sum(a for _, a in parts)
         return SieveResult(factorcount=len(kept), primecount=primecount,

@@ -354,6 +354,8 @@ static bool verify_group(const pfc_factor *h, size_t cnt, const uint32_t *list, 
     return true;
 }
 
+uint64_t verify_start(int type, uint64_t p) { return (uint64_t)(kStart[type] % p); }
+
 bool verify_factor(uint64_t p, uint32_t n, int32_t c, int32_t type, const uint32_t *list, size_t listsize) {
     pfc_factor f;
     f.p = p;

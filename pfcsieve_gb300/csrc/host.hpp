@@ -52,4 +52,8 @@ bool is_prime_u64(uint64_t p);
 // CPU re-verification of one factor by naive products (verifyprime.cpp:199-268)
 bool verify_factor(uint64_t p, uint32_t n, int32_t c, int32_t type, const uint32_t *list, size_t listsize);
 
+// start value of the verification product of a hit of `type` (34!, 101#,
+// 44!/44#; verifyprime.cpp:205,222,241) reduced modulo p
+uint64_t verify_start(int type, uint64_t p);
+
 }  // namespace pfc

@@ -14,6 +14,8 @@
 // same way (product and count).
 #include <cuda_runtime.h>
 
+#include <algorithm>
+#include <climits>
 #include <vector>
 
 #include "devmem.hpp"
@@ -136,3 +138,137 @@ int slow_products(pfc_ctx *c, uint64_t lo, uint64_t hi, SlowProducts &out) {
 }
 
 }  // namespace pfc
+
+// ------------------------------------------------------- hit re-verification
+//
+// The CPU check of every hit (cl_sieve.cpp:509-540, verifyprime.cpp:199-268)
+// on the device, all hits at once: the hit's verification product -- the
+// type's start value (34!, 101#, 44!/44#) times every k in [35, n] (type 0),
+// times the primes in [103, n] or the composites in [45, n] (the list of the
+// search's mode, as the CPU check builds it) -- must be +1 or -1 modulo p with
+// the hit's sign.  One warp per hit: each lane multiplies a contiguous
+// sub-range of k as plain multipliers (one reduction each, the power of R
+// fixed once at the end), and the lanes' products are combined by shuffles.
+// Nothing here uses the sieve's tables or its walk, so the check is
+// independent of the arithmetic it checks.
+
+namespace pfc {
+
+struct VerifyRec {
+    uint64_t p, start;
+    uint32_t lo, hi;     // k in [lo, hi]
+    uint32_t what;       // 0 every k, 1 primes, 2 composites, 3 none
+    int32_t sign;
+};
+
+__global__ void __launch_bounds__(256) verify_hits_kernel(const VerifyRec *r, uint32_t cnt, const uint32_t *primebits,
+                                                          uint8_t *bad) {
+    const uint32_t w = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+    if (w >= cnt) return;   // whole warps
+    const VerifyRec h = r[w];
+    Mont64 m;
+    m.init(h.p);
+    uint64_t a0 = m.one, a1 = m.one;
+    uint32_t taken = 0;
+    if (h.what != 3 && h.hi >= h.lo) {
+        const uint32_t per = ((h.hi - h.lo) >> 5) + 1;
+        const uint32_t a = h.lo + lane * per;
+        const uint32_t e = min(a + per, h.hi + 1);
+        uint32_t k = a;
+        if (h.what == 0) {
+            for (; k + 1 < e; k += 2) {
+                a0 = redc64(a0, k, m.p, m.pinv);
+                a1 = redc64(a1, k + 1, m.p, m.pinv);
+            }
+            if (k < e) a0 = redc64(a0, k, m.p, m.pinv);
+            taken = e > a ? e - a : 0;
+        } else {
+            const uint32_t want = h.what == 1 ? 1u : 0u;
+            for (; k < e; ++k)
+                if (((__ldg(primebits + (k >> 5)) >> (k & 31)) & 1u) == want) {
+                    a0 = redc64(a0, k, m.p, m.pinv);
+                    ++taken;
+                }
+        }
+    }
+    // each reduction by a plain k lowered the power of R by one
+    uint64_t acc = m.mul(m.mul(a0, a1), m.mont_R_pow(taken));
+#pragma unroll
+    for (int o = 16; o; o >>= 1) acc = m.mul(acc, __shfl_down_sync(0xffffffffu, acc, o));
+    if (lane == 0) {
+        const uint64_t v = m.mul(acc, m.to_mont(h.start));
+        bad[w] = h.sign < 0 ? v != m.one : v != m.p - m.one;
+    }
+}
+
+}  // namespace pfc
+
+extern "C" int pfc_verify_factors_device(pfc_ctx *c, unsigned mode, uint32_t nmax, const pfc_factor *f, size_t n,
+                                         uint8_t *bad, size_t *failed) {
+    using namespace pfc;
+    if (!c || (!f && n) || !failed) return PFC_ERR_ARG;
+    *failed = 0;
+    if (n == 0) return PFC_OK;
+    if (n > (1u << 26)) return PFC_ERR_ARG;
+    CK(cudaSetDevice(c->device));
+    std::vector<VerifyRec> rec(n);
+    uint32_t top = 0;
+    bool lists = false;
+    for (size_t i = 0; i < n; ++i) {
+        const pfc_factor &x = f[i];
+        if (x.p < 3 || !(x.p & 1) || x.type < 0 || x.type > 2 || x.nc == 0 || x.nc == INT32_MIN) return PFC_ERR_ARG;
+        const uint32_t an = (uint32_t)(x.nc < 0 ? -x.nc : x.nc);
+        VerifyRec &v = rec[i];
+        v.p = x.p;
+        v.start = verify_start(x.type, x.p);
+        v.sign = x.nc < 0 ? -1 : 1;
+        if (x.type == 0) {
+            v.what = 0;
+            v.lo = 35;
+            v.hi = an;
+        } else if (mode & PFC_PRIMORIAL) {   // primes in [103, nmax] (cl_sieve.cpp:1468-1476)
+            v.what = 1;
+            v.lo = 103;
+            v.hi = std::min(an, nmax);
+        } else if (mode & PFC_COMPOSITORIAL) {   // composites in [45, nmax) (cl_sieve.cpp:1478-1492)
+            v.what = 2;
+            v.lo = 45;
+            v.hi = std::min(an, nmax ? nmax - 1 : 0u);
+        } else {
+            v.what = 3;
+            v.lo = 1;
+            v.hi = 0;
+        }
+        if (v.what == 1 || v.what == 2) {
+            lists = true;
+            top = std::max(top, v.hi);
+        }
+    }
+    std::vector<uint32_t> bits(lists ? top / 32 + 1 : 1, 0u);
+    if (lists)
+        for (uint32_t q : primes_between(2, top)) bits[q >> 5] |= 1u << (q & 31);
+    DArr<VerifyRec> d_rec;
+    DArr<uint32_t> d_bits;
+    DArr<uint8_t> d_bad;
+    std::vector<uint8_t> hb(n);
+    cudaError_t e = d_rec.upload(c, rec);
+    if (e == cudaSuccess) e = d_bits.upload(c, bits);
+    if (e == cudaSuccess) e = d_bad.alloc(c, n);
+    if (e == cudaSuccess) {
+        verify_hits_kernel<<<(unsigned)((n + 7) / 8), 256, 0, c->st>>>(d_rec.p, (uint32_t)n, d_bits.p, d_bad.p);
+        c->launches++;
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(hb.data(), d_bad.p, n, cudaMemcpyDeviceToHost, c->st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->st);
+    c->d2h += n;
+    d_rec.release(c);
+    d_bits.release(c);
+    d_bad.release(c);
+    CK(e);
+    size_t nb = 0;
+    for (size_t i = 0; i < n; ++i) nb += hb[i] != 0;
+    if (bad) std::copy(hb.begin(), hb.end(), bad);
+    *failed = nb;
+    return nb ? PFC_ERR_VERIFY : PFC_OK;
+}
