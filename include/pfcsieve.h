@@ -203,12 +203,12 @@ int pfc_finalize_factors(unsigned mode, uint32_t nmax, pfc_factor *f, size_t n,
  * start value of its type (34!, 101#, 44!/44#) times every k in [35, n] for a
  * factorial hit, or the list of the search's mode (primes in [103, nmax] for
  * n#, composites in [45, nmax) for n!/n#) up to n -- is formed modulo p as a
- * plain product split over one warp per hit, and must be 1 for a -1 hit and
- * p - 1 for a +1 hit.  *failed receives the number of hits that fail; bad
- * (n bytes, may be NULL) receives 1 for each failing hit and 0 otherwise.
- * Returns PFC_ERR_VERIFY when any hit fails.  The records are not reordered
- * or changed: pass them to pfc_finalize_factors with verify = 0 for the sort,
- * the 2-PRP filter and the checksum.  Synchronises. */
+ * plain product split over the 256 threads of one CTA per hit, and must be 1
+ * for a -1 hit and p - 1 for a +1 hit.  *failed receives the number of hits
+ * that fail; bad (n bytes, may be NULL) receives 1 for each failing hit and 0
+ * otherwise.  Returns PFC_ERR_VERIFY when any hit fails.  The records are not
+ * reordered or changed: pass them to pfc_finalize_factors with verify = 0 for
+ * the sort, the 2-PRP filter and the checksum.  Synchronises. */
 int pfc_verify_factors_device(pfc_ctx *ctx, unsigned mode, uint32_t nmax, const pfc_factor *f, size_t n,
                               uint8_t *bad, size_t *failed);
 

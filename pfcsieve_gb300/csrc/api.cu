@@ -142,6 +142,7 @@ extern "C" int pfc_ctx_destroy(pfc_ctx *c) {
     cudaSetDevice(c->device);
     if (c->st) cudaStreamSynchronize(c->st);
     if (c->d_pat) cudaFree(c->d_pat);
+    if (c->vbits) cudaFree(c->vbits);
     if (c->st) cudaStreamDestroy(c->st);
     delete c;
     return PFC_OK;

@@ -22,6 +22,11 @@ struct pfc_ctx {
     uint64_t *d_pat = nullptr;
     int walk_var[3][2] = {{0, 0}, {0, 0}, {0, 0}};   // walk variant per size class and kind (fused)
     bool graphs = true;   // pfc_segment replays each job's segment body as a CUDA graph
+    // prime flags of [0, vbits_top] kept for pfc_verify_factors_device (one
+    // bit per integer), rebuilt only when a call needs a larger range
+    uint32_t *vbits = nullptr;
+    uint32_t vbits_top = 0;
+    size_t vbits_bytes = 0;
 };
 
 namespace pfc {

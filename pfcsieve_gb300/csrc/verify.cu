@@ -146,9 +146,10 @@ int slow_products(pfc_ctx *c, uint64_t lo, uint64_t hi, SlowProducts &out) {
 // type's start value (34!, 101#, 44!/44#) times every k in [35, n] (type 0),
 // times the primes in [103, n] or the composites in [45, n] (the list of the
 // search's mode, as the CPU check builds it) -- must be +1 or -1 modulo p with
-// the hit's sign.  One warp per hit: each lane multiplies a contiguous
-// sub-range of k as plain multipliers (one reduction each, the power of R
-// fixed once at the end), and the lanes' products are combined by shuffles.
+// the hit's sign.  One CTA of 256 threads per hit: each thread multiplies a
+// contiguous sub-range of k as plain multipliers in four chains (one
+// reduction each, the power of R fixed once at the end), and the threads'
+// products are combined by shuffles and through shared memory.
 // Nothing here uses the sieve's tables or its walk, so the check is
 // independent of the arithmetic it checks.
 
@@ -163,41 +164,48 @@ struct VerifyRec {
 
 __global__ void __launch_bounds__(256) verify_hits_kernel(const VerifyRec *r, uint32_t cnt, const uint32_t *primebits,
                                                           uint8_t *bad) {
-    const uint32_t w = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5), lane = threadIdx.x & 31;
-    if (w >= cnt) return;   // whole warps
-    const VerifyRec h = r[w];
+    __shared__ uint64_t part[8];
+    if (blockIdx.x >= cnt) return;   // whole blocks
+    const VerifyRec h = r[blockIdx.x];
+    const uint32_t t = threadIdx.x;
     Mont64 m;
     m.init(h.p);
-    uint64_t a0 = m.one, a1 = m.one;
+    uint64_t a0 = m.one, a1 = m.one, a2 = m.one, a3 = m.one;
     uint32_t taken = 0;
     if (h.what != 3 && h.hi >= h.lo) {
-        const uint32_t per = ((h.hi - h.lo) >> 5) + 1;
-        const uint32_t a = h.lo + lane * per;
-        const uint32_t e = min(a + per, h.hi + 1);
-        uint32_t k = a;
+        const uint32_t per = (h.hi - h.lo) / blockDim.x + 1;
+        const uint32_t s = h.lo + t * per;   // <= hi + blockDim.x: no wrap below 2^31 + 256
+        const uint32_t e = s <= h.hi ? min(s + per, h.hi + 1) : s;
+        uint32_t k = s;
         if (h.what == 0) {
-            for (; k + 1 < e; k += 2) {
+            for (; k + 3 < e; k += 4) {
                 a0 = redc64(a0, k, m.p, m.pinv);
                 a1 = redc64(a1, k + 1, m.p, m.pinv);
+                a2 = redc64(a2, k + 2, m.p, m.pinv);
+                a3 = redc64(a3, k + 3, m.p, m.pinv);
             }
-            if (k < e) a0 = redc64(a0, k, m.p, m.pinv);
-            taken = e > a ? e - a : 0;
+            for (; k < e; ++k) a0 = redc64(a0, k, m.p, m.pinv);
+            taken = e - s;
         } else {
             const uint32_t want = h.what == 1 ? 1u : 0u;
             for (; k < e; ++k)
                 if (((__ldg(primebits + (k >> 5)) >> (k & 31)) & 1u) == want) {
-                    a0 = redc64(a0, k, m.p, m.pinv);
+                    if (taken & 1) a1 = redc64(a1, k, m.p, m.pinv);
+                    else a0 = redc64(a0, k, m.p, m.pinv);
                     ++taken;
                 }
         }
     }
     // each reduction by a plain k lowered the power of R by one
-    uint64_t acc = m.mul(m.mul(a0, a1), m.mont_R_pow(taken));
+    uint64_t acc = m.mul(m.mul(m.mul(a0, a1), m.mul(a2, a3)), m.mont_R_pow(taken));
 #pragma unroll
     for (int o = 16; o; o >>= 1) acc = m.mul(acc, __shfl_down_sync(0xffffffffu, acc, o));
-    if (lane == 0) {
+    if ((t & 31) == 0) part[t >> 5] = acc;
+    __syncthreads();
+    if (t == 0) {
+        for (uint32_t i = 1; i < (blockDim.x >> 5); ++i) acc = m.mul(acc, part[i]);
         const uint64_t v = m.mul(acc, m.to_mont(h.start));
-        bad[w] = h.sign < 0 ? v != m.one : v != m.p - m.one;
+        bad[blockIdx.x] = h.sign < 0 ? v != m.one : v != m.p - m.one;
     }
 }
 
@@ -244,18 +252,40 @@ extern "C" int pfc_verify_factors_device(pfc_ctx *c, unsigned mode, uint32_t nma
             top = std::max(top, v.hi);
         }
     }
-    std::vector<uint32_t> bits(lists ? top / 32 + 1 : 1, 0u);
-    if (lists)
-        for (uint32_t q : primes_between(2, top)) bits[q >> 5] |= 1u << (q & 31);
+    if (lists && (!c->vbits || top > c->vbits_top)) {
+        // prime flags up to at least twice the range asked for, kept in the
+        // context for later calls
+        const uint32_t want = (uint32_t)std::min<uint64_t>(std::max<uint64_t>(2ull * top, 1u << 20), 0x7FFFFFFFull);
+        std::vector<uint32_t> bits(want / 32 + 1, 0u);
+        for (uint32_t q : primes_between(2, want)) bits[q >> 5] |= 1u << (q & 31);
+        if (c->vbits) {
+            CK(cudaStreamSynchronize(c->st));
+            cudaFree(c->vbits);
+            c->used -= c->vbits_bytes;
+            c->vbits = nullptr;
+            c->vbits_top = 0;
+            c->vbits_bytes = 0;
+        }
+        void *vb = nullptr;
+        CK(dalloc_bytes(c, &vb, bits.size() * 4));
+        cudaError_t e = cudaMemcpy(vb, bits.data(), bits.size() * 4, cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) {
+            cudaFree(vb);
+            c->used -= bits.size() * 4;
+            CK(e);
+        }
+        c->h2d += bits.size() * 4;
+        c->vbits = static_cast<uint32_t *>(vb);
+        c->vbits_top = want;
+        c->vbits_bytes = bits.size() * 4;
+    }
     DArr<VerifyRec> d_rec;
-    DArr<uint32_t> d_bits;
     DArr<uint8_t> d_bad;
     std::vector<uint8_t> hb(n);
     cudaError_t e = d_rec.upload(c, rec);
-    if (e == cudaSuccess) e = d_bits.upload(c, bits);
     if (e == cudaSuccess) e = d_bad.alloc(c, n);
     if (e == cudaSuccess) {
-        verify_hits_kernel<<<(unsigned)((n + 7) / 8), 256, 0, c->st>>>(d_rec.p, (uint32_t)n, d_bits.p, d_bad.p);
+        verify_hits_kernel<<<(unsigned)n, 256, 0, c->st>>>(d_rec.p, (uint32_t)n, c->vbits, d_bad.p);
         c->launches++;
         e = cudaGetLastError();
     }
@@ -263,7 +293,6 @@ extern "C" int pfc_verify_factors_device(pfc_ctx *c, unsigned mode, uint32_t nma
     if (e == cudaSuccess) e = cudaStreamSynchronize(c->st);
     c->d2h += n;
     d_rec.release(c);
-    d_bits.release(c);
     d_bad.release(c);
     CK(e);
     size_t nb = 0;
