@@ -197,7 +197,21 @@ class ClockSampler:
                 if r[3 + k].lower().startswith("active"):
                     reasons.add(name)
         if not sm:
-            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+            # a timed region shorter than the first sample: one reading taken
+            # right after it, marked as such
+            out = {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0,
+                   "note": "timed region shorter than the 200 ms sampling interval"}
+            try:
+                r = subprocess.run(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.Q,
+                                    "--format=csv,noheader,nounits"], capture_output=True, text=True,
+                                   timeout=10).stdout.strip().split(",")
+                f = [x.strip() for x in r]
+                out["after_region"] = {"sm_mhz": float(f[0]), "sm_max_mhz": float(f[1]),
+                                       "reasons": [n for k, n in enumerate(names)
+                                                   if f[3 + k].lower().startswith("active")]}
+            except Exception:
+                pass
+            return out
         return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx),
                 "reasons": sorted(reasons), "samples": len(sm)}
 
