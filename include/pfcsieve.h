@@ -208,7 +208,10 @@ int pfc_finalize_factors(unsigned mode, uint32_t nmax, pfc_factor *f, size_t n,
  * that fail; bad (n bytes, may be NULL) receives 1 for each failing hit and 0
  * otherwise.  Returns PFC_ERR_VERIFY when any hit fails.  The records are not
  * reordered or changed: pass them to pfc_finalize_factors with verify = 0 for
- * the sort, the 2-PRP filter and the checksum.  Synchronises. */
+ * the sort, the 2-PRP filter and the checksum.  At most 2^26 hits per call;
+ * PFC_ERR_ARG for more, for a record with an even p or p < 3, n = 0 or a type
+ * other than 0, 1, 2.  The prime flags of the verification lists stay in the
+ * context for later calls.  Synchronises. */
 int pfc_verify_factors_device(pfc_ctx *ctx, unsigned mode, uint32_t nmax, const pfc_factor *f, size_t n,
                               uint8_t *bad, size_t *failed);
 
