@@ -91,6 +91,8 @@ def parse():
                     help="candidates in the CPU baseline sample (0 = auto)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-mixed", action="store_true", help="skip the batched-vs-plain comparison")
+    ap.add_argument("--iteration-work", type=float, default=None,
+                    help="batch iteration length in candidate-steps (default: the library's for the policy)")
     ap.add_argument("--mixed-jobs", type=int, default=32,
                     help="searches of the mixed workload sample (the full set is 512)")
     return ap.parse_args()
@@ -342,7 +344,7 @@ def hit_order(f):
     return f[np.lexsort((f["nc"], f["type"], np.abs(f["nc"].astype(np.int64)), f["p"]))]
 
 
-def run_mixed(ctx, njobs, warmup, steps=1):
+def run_mixed(ctx, njobs, warmup, steps=1, iteration_work=None):
     """Mixed-workload sample: one batch vs one search at a time, results
     compared search by search, then the request loop under Poisson arrivals."""
     import pfcsieve_gb300 as pfc
@@ -352,7 +354,7 @@ def run_mixed(ctx, njobs, warmup, steps=1):
     sv.run_batched(ctx, jobs[:4], keep_hits=False)       # warm-up: kernels loaded, pools grown
     runs = []
     for _ in range(max(1, steps)):
-        runs.append(sv.run_batched(ctx, jobs))
+        runs.append(sv.run_batched(ctx, jobs, iteration_work=iteration_work))
     out_b, t_b, timing = min(runs, key=lambda r: r[1])
     out_p, t_p, service, create = sv.run_plain(ctx, jobs)
     same = all((out_b[i].term_checksum, out_b[i].primecount) == (out_p[i].term_checksum, out_p[i].primecount)
@@ -380,6 +382,7 @@ def run_mixed(ctx, njobs, warmup, steps=1):
         "batched_s": t_b, "plain_s": t_p, "plain_table_build_s": create, "finalize_s": t_fin,
         "finalize_verify": "device",
         "iterations": int(timing["iterations"]), "tasks": int(timing["tasks"]),
+        "iteration_work": iteration_work if iteration_work else "default (1.6e12 candidate-steps, throughput policy)",
         "identical_results": bool(same and same_s),
         "serving": {"arrivals_per_s": 200.0, "makespan_s": makespan,
                     "p50_s": float(np.percentile(lat, 50)), "p99_s": float(np.percentile(lat, 99)),
@@ -400,7 +403,7 @@ def run_mixed_line(args, local):
     h2d0, d2h0 = ctx.transfer_bytes()
     clk = ClockSampler(local)
     clk.start()
-    r = run_mixed(ctx, args.mixed_jobs, args.warmup, steps=args.steps)
+    r = run_mixed(ctx, args.mixed_jobs, args.warmup, steps=args.steps, iteration_work=args.iteration_work)
     clocks = clk.stop()
     h2d1, d2h1 = ctx.transfer_bytes()
     launches = ctx.launches - launches0
@@ -538,7 +541,7 @@ def run_ours(args, wl, world, rank, local, dist):
 
     batched = None
     if rank == 0 and not args.no_mixed:
-        batched = run_mixed(ctx, args.mixed_jobs, args.warmup)
+        batched = run_mixed(ctx, args.mixed_jobs, args.warmup, iteration_work=args.iteration_work)
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:

@@ -303,23 +303,27 @@ int pfc_batch_take_hits(pfc_batch *b, uint64_t id, pfc_factor *buf, size_t cap, 
 int pfc_batch_release(pfc_batch *b, uint64_t id);
 /* Iterations run so far. */
 uint64_t pfc_batch_iterations(pfc_batch *b);
-/* Work of one iteration in candidate-steps (default 1e11, about 0.1 s of
- * GPU time; a class-64 candidate step counts 3): smaller values give new
- * searches and finished results a shorter wait, larger ones less host
- * overhead per step. */
+/* Work of one iteration in candidate-steps (a class-64 candidate step counts
+ * 3).  Default by policy: 1.6e12 for THROUGHPUT (about 0.6 s of GPU time:
+ * every iteration ends with a tail, so long ones waste least), 5e10 for
+ * LATENCY (arrivals join and finished searches leave at iteration ends).
+ * Smaller values give new searches and finished results a shorter wait,
+ * larger ones less tail and host overhead per step. */
 int pfc_batch_set_iteration_work(pfc_batch *b, double candidate_steps);
 
-/* Scheduling policy.  THROUGHPUT (default): every search advances the same
- * number of positions per iteration; a batch submitted at once ends soonest.
- * LATENCY: half of each iteration goes to the searches with the least work
- * left (shortest remaining work first), for request streams where the
- * median wait matters. */
 /* Capacity of the batch's shared hit list per iteration (default 2^20
  * records), settable while no search is on the device.  When the hits of an
  * iteration exceed it, every search of that iteration is redone alone with
  * pfc_job_run after it finishes, so results never depend on this size. */
 int pfc_batch_set_hit_capacity(pfc_batch *b, uint32_t records);
 
+/* Scheduling policy.  THROUGHPUT (default): every search advances the same
+ * number of positions per iteration; a batch submitted at once ends soonest.
+ * LATENCY: searches are taken in order of least work left (shortest
+ * remaining work first), each with a window that the iteration's budget still
+ * pays for; the others wait, except that one that has waited 32 iterations
+ * gets a minimal window and the smallest always advances.  For request
+ * streams where the median wait matters. */
 #define PFC_BATCH_THROUGHPUT 0
 #define PFC_BATCH_LATENCY    1
 int pfc_batch_set_policy(pfc_batch *b, int policy);

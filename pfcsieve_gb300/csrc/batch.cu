@@ -505,6 +505,10 @@ static void free_vec(std::vector<W> &v) {
 
 using namespace pfc;
 
+// default work of one iteration in candidate-steps, per policy
+constexpr double kThroughputIterWork = 1.6e12;
+constexpr double kLatencyIterWork = 5e10;
+
 struct pfc_batch {
     pfc_ctx *ctx = nullptr;
     static constexpr uint32_t kSlots = 4096;
@@ -533,7 +537,7 @@ struct pfc_batch {
     std::vector<Window> w[kLists][kKinds];   // this iteration's windows per launch
     uint64_t ctas[kLists][kKinds] = {};
     uint64_t next_id = 1;
-    double work_per_iter = 1e11;         // candidate-steps per iteration (class 64 weighs 3)
+    double work_per_iter = 0;            // candidate-steps per iteration (class 64 weighs 3); 0: the policy's
     int policy = PFC_BATCH_THROUGHPUT;
     uint64_t iterations = 0;
     // timing: kernel spans (CUDA events) and host phases (wall clock)
@@ -793,7 +797,14 @@ uint32_t build_tasks(pfc_batch *b) {
         b->running.push_back(j);
     }
     b->ready.clear();
-    const double budget = b->work_per_iter * 6.0;   // candidate-steps -> multiplies
+    // iteration length unless set: long for the throughput policy (every
+    // iteration ends with a tail; on the 512-search mix 585 iterations of 1e11
+    // candidate-steps took 41.3 s, 61 of 1.6e12 38.8 s), short for the
+    // latency policy (arrivals join and results leave at iteration ends)
+    const double per_iter = b->work_per_iter > 0
+                                ? b->work_per_iter
+                                : (b->policy == PFC_BATCH_LATENCY ? kLatencyIterWork : kThroughputIterWork);
+    const double budget = per_iter * 6.0;   // candidate-steps -> multiplies
     const double cta_share = budget / (3.0 * b->ctx->sms);
     std::vector<std::pair<double, BatchJob *>> order;
     order.reserve(b->running.size());
