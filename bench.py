@@ -344,7 +344,56 @@ def hit_order(f):
     return f[np.lexsort((f["nc"], f["type"], np.abs(f["nc"].astype(np.int64)), f["p"]))]
 
 
-def run_mixed(ctx, njobs, warmup, steps=1, iteration_work=None):
+def mixed_roofline(jobs, outcomes, gpu_s, peaks):
+    """Multiply-pipe roofline of a batched run: the algorithmic multiplies of
+    every search (per candidate: its setup program's table words and squarings
+    -- pfc_setup_program_size -- and its walk steps: n for !, composite n for
+    the compositorial, prime n for #, both for -! -c), weighted by the measured
+    issue rates (IMAD 1, IMAD.WIDE and IMAD.HI by their rates relative to
+    IMAD), over the batch's GPU time.  Per unit (see arith.cuh, walk.cuh):
+    896-bit word 36 IMAD.WIDE + 2 IMAD (class 32), 76 + 3 (class 64 below
+    2^64/3); 64-bit word and class-64 squaring 8 IMAD.WIDE + 2 IMAD; class-32
+    squaring IMAD.WIDE + IMAD + IMAD.HI; walk steps as step_recipe.  Restores,
+    corrections and replays are overhead, as in the single-search roofline.
+    A search whose p range crosses 2^31 or 2^64/3 is counted in the class of
+    its upper end."""
+    import pfcsieve_gb300 as pfc
+    w = peaks["imad"] / peaks["imad_wide"]
+    h = peaks["imad"] / peaks["mul_hi"]
+    lazy_end = 0x5555555555555556
+    unit = {32: (36 * w + 2, w + 1 + h), 64: (76 * w + 3, 8 * w + 2), 65: (8 * w + 2, 8 * w + 2)}
+    top = max(s.nmax for s in jobs) + 1
+    isp = np.ones(top, dtype=bool)
+    isp[:2] = False
+    for i in range(2, int(top ** 0.5) + 1):
+        if isp[i]:
+            isp[i * i::i] = False
+    pc = np.concatenate([[0], np.cumsum(isp)])   # pc[n] = primes below n
+    total, crossing, sizes = 0.0, 0, {}
+    for i, s in enumerate(jobs):
+        cls = 32 if s.pmax <= 2**31 else (64 if s.pmax <= lazy_end else 65)
+        crossing += int(s.pmin < 2**31 < s.pmax or s.pmin < lazy_end < s.pmax)
+        key = (s.mode, s.nmin, cls != 65)
+        if key not in sizes:
+            sizes[key] = pfc.setup_program_size(*key)
+        words, sq = sizes[key]
+        n = s.nmax - s.nmin
+        primes = int(pc[s.nmax] - pc[s.nmin])
+        steps = {1: n, 2: primes, 4: n - primes, 5: 2 * n - primes}[s.mode]
+        recipe = step_recipe(cls == 32, cls == 64)
+        step = sum(k * peaks["imad"] / peaks[name] for name, k in recipe.items())
+        cw, cs = unit[cls]
+        total += outcomes[i].primecount * (words * cw + sq * cs + steps * step)
+    achieved = total / gpu_s
+    return {"bound": "int (multiply pipe)", "achieved": achieved / 1e12, "peak": peaks["imad"] / 1e12,
+            "unit": "Tops/s IMAD-equivalent (IMAD.WIDE, IMAD.HI weighted by measured rates)",
+            "frac": achieved / peaks["imad"], "traffic": None,
+            "kernel": "batch_kernel (every class and kind of the batch, over its GPU time)",
+            "alg_ops": total, "gpu_s": gpu_s, "searches_crossing_a_class_boundary": crossing,
+            "peak_source": "measured in this run (pfc_bench_int_peak, 32-bit IMAD chains)"}
+
+
+def run_mixed(ctx, njobs, warmup, steps=1, iteration_work=None, peaks=None):
     """Mixed-workload sample: one batch vs one search at a time, results
     compared search by search, then the request loop under Poisson arrivals."""
     import pfcsieve_gb300 as pfc
@@ -372,6 +421,7 @@ def run_mixed(ctx, njobs, warmup, steps=1, iteration_work=None):
     same_s = all((out_s[i].term_checksum, out_s[i].primecount) == (out_p[i].term_checksum, out_p[i].primecount)
                  for i in range(len(jobs)))
     lat_p = sv.fcfs_latencies(arrivals, service)
+    roof = mixed_roofline(jobs, out_b, timing["gpu_s"], peaks) if peaks else None
     return {
         "workload": "first %d of the 512 mixed searches (seed 0)" % len(jobs),
         "pairs": int(pairs),
@@ -384,6 +434,7 @@ def run_mixed(ctx, njobs, warmup, steps=1, iteration_work=None):
         "iterations": int(timing["iterations"]), "tasks": int(timing["tasks"]),
         "iteration_work": iteration_work if iteration_work else "default (1.6e12 candidate-steps, throughput policy)",
         "identical_results": bool(same and same_s),
+        "roofline": roof,
         "serving": {"arrivals_per_s": 200.0, "makespan_s": makespan,
                     "p50_s": float(np.percentile(lat, 50)), "p99_s": float(np.percentile(lat, 99)),
                     "plain_fcfs_p50_s": float(np.percentile(lat_p, 50)),
@@ -403,7 +454,10 @@ def run_mixed_line(args, local):
     h2d0, d2h0 = ctx.transfer_bytes()
     clk = ClockSampler(local)
     clk.start()
-    r = run_mixed(ctx, args.mixed_jobs, args.warmup, steps=args.steps, iteration_work=args.iteration_work)
+    peaks = {k: pfc.int_peak(local, v) for k, v in
+             (("imad", 0), ("mul_hi", 1), ("imad_wide", 2), ("iadd_xor", 3))}
+    r = run_mixed(ctx, args.mixed_jobs, args.warmup, steps=args.steps, iteration_work=args.iteration_work,
+                  peaks=peaks)
     clocks = clk.stop()
     h2d1, d2h1 = ctx.transfer_bytes()
     launches = ctx.launches - launches0
@@ -420,7 +474,7 @@ def run_mixed_line(args, local):
         "e2e": {"value": r["pairs"] / (r["batched_s"] + r["finalize_s"]), "unit": UNIT,
                 "h2d_bytes_per_step": (h2d1 - h2d0) // steps, "d2h_bytes_per_step": (d2h1 - d2h0) // steps},
         "gpu_launches": int(launches), "clocks": clocks, "batched": r,
-        "roofline": None, "cpu_baseline": None,
+        "roofline": r["roofline"], "cpu_baseline": None,
     }
     print(json.dumps(line), flush=True)
 
@@ -541,7 +595,7 @@ def run_ours(args, wl, world, rank, local, dist):
 
     batched = None
     if rank == 0 and not args.no_mixed:
-        batched = run_mixed(ctx, args.mixed_jobs, args.warmup, iteration_work=args.iteration_work)
+        batched = run_mixed(ctx, args.mixed_jobs, args.warmup, iteration_work=args.iteration_work, peaks=peaks)
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:

@@ -215,6 +215,13 @@ int pfc_finalize_factors(unsigned mode, uint32_t nmax, pfc_factor *f, size_t n,
 int pfc_verify_factors_device(pfc_ctx *ctx, unsigned mode, uint32_t nmax, const pfc_factor *f, size_t n,
                               uint8_t *bad, size_t *failed);
 
+/* Size of a search's setup programs, as pfc_job_create builds them (host
+ * only, no GPU): *words table words and *squarings squarings per candidate,
+ * with 896-bit words (wide = 1: class 32 and class 64 below 2^64/3) or 64-bit
+ * words (wide = 0: class 64 above).  For counting the algorithmic work of a
+ * run; no counterpart in the reference. */
+int pfc_setup_program_size(unsigned mode, uint32_t nmin, int wide, uint64_t *words, uint64_t *squarings);
+
 /* Deterministic primality for 64-bit p (verifyprime.cpp:157-195). */
 int pfc_is_prime(uint64_t p);
 

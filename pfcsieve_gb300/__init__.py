@@ -101,6 +101,7 @@ def lib():
             "pfc_finalize_factors": (ctypes.c_int, [ctypes.c_uint, u32, vp, sz, ctypes.c_int,
                                                     ctypes.c_int, P(sz), P(u64)]),
             "pfc_verify_factors_device": (ctypes.c_int, [vp, ctypes.c_uint, u32, vp, sz, vp, P(sz)]),
+            "pfc_setup_program_size": (ctypes.c_int, [ctypes.c_uint, u32, ctypes.c_int, P(u64), P(u64)]),
             "pfc_is_prime": (ctypes.c_int, [u64]),
             "pfc_format_factor": (ctypes.c_int, [vp, ctypes.c_char_p, sz]),
             "pfc_status_string": (ctypes.c_char_p, [ctypes.c_int]),
@@ -443,6 +444,14 @@ def int_peak(device=0, variant=0):
     v = ctypes.c_double(0)
     _ck(lib().pfc_bench_int_peak(device, variant, ctypes.byref(v)), "pfc_bench_int_peak")
     return v.value
+
+
+def setup_program_size(mode, nmin, wide=True):
+    """(table words, squarings) per candidate of a search's setup programs."""
+    w, q = ctypes.c_uint64(0), ctypes.c_uint64(0)
+    _ck(lib().pfc_setup_program_size(mode, nmin, int(bool(wide)), ctypes.byref(w), ctypes.byref(q)),
+        "pfc_setup_program_size")
+    return w.value, q.value
 
 
 def is_prime(p):

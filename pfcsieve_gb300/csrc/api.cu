@@ -204,6 +204,33 @@ static bool build_progs(unsigned mode, uint32_t startN, const std::vector<uint32
     return build_power_prog(startN, 1, primes, a) && build_product_prog(below, b);
 }
 
+extern "C" int pfc_setup_program_size(unsigned mode, uint32_t nmin, int wide, uint64_t *words,
+                                      uint64_t *squarings) {
+    if (!words || !squarings) return PFC_ERR_ARG;
+    const bool valid_mode = mode == PFC_FACTORIAL || mode == PFC_PRIMORIAL || mode == PFC_COMPOSITORIAL ||
+                            mode == (PFC_FACTORIAL | PFC_COMPOSITORIAL);
+    if (!valid_mode || nmin < 101 || nmin > 0x7FFFFFFFu) return PFC_ERR_ARG;
+    const uint32_t startN = nmin - 1;
+    const std::vector<uint32_t> primes = primes_between(2, startN);
+    bool ok;
+    uint64_t w = 0, m = 0;
+    if (wide) {
+        HostProg<WideWord> a, b;
+        ok = build_progs(mode, startN, primes, primes, a, b);
+        w = a.words.size() + b.words.size();
+        m = a.mulmods() + b.mulmods();
+    } else {
+        HostProg<uint64_t> a, b;
+        ok = build_progs(mode, startN, primes, primes, a, b);
+        w = a.words.size() + b.words.size();
+        m = a.mulmods() + b.mulmods();
+    }
+    if (!ok) return PFC_ERR_ARG;
+    *words = w;
+    *squarings = m - w;
+    return PFC_OK;
+}
+
 extern "C" int pfc_job_create(pfc_ctx *c, unsigned mode, uint32_t nmin, uint32_t nmax, uint64_t pmin,
                               uint64_t pmax, pfc_job **out) {
     if (!c || !out) return PFC_ERR_ARG;

@@ -114,3 +114,61 @@ def test_finalize_rejects_flipped_sign(pfc, mode):
     with pytest.raises(pfc.PFCError) as e:
         pfc.finalize(mode, nmax, bad, threads=4, verify=True)
     assert e.value.code == -6
+
+
+def _program_model(mode, nmin):
+    """Setup program size from the definition: (nmin-1)! (mode 1), its
+    composite part (mode 4) or the primorial (mode 2) as prime products
+    grouped by the bits of the Legendre exponents (Horner form: one squaring
+    between consecutive bit levels), each group packed greedily into 896-bit
+    words two primes at a time, then one; mode 5 = mode 4 + the primorial."""
+    n0 = nmin - 1
+    primes = [q for q in range(2, n0 + 1) if all(q % d for d in range(2, int(q ** 0.5) + 1))]
+
+    def pack(fs):
+        words, i = 0, 0
+        while i < len(fs):
+            acc = fs[i]
+            i += 1
+            while i < len(fs):
+                for take in ((2, 1) if i + 1 < len(fs) else (1,)):
+                    m = fs[i] * fs[i + 1] if take == 2 else fs[i]
+                    if (acc * m).bit_length() <= 896:
+                        acc *= m
+                        i += take
+                        break
+                else:
+                    break
+            words += 1
+        return words
+
+    def power(sub):
+        bits = {}
+        for q in primes:
+            e, qk = 0, q
+            while qk <= n0:
+                e += n0 // qk
+                qk *= q
+            e -= sub
+            j = 0
+            while e:
+                if e & 1:
+                    bits.setdefault(j, []).append(q)
+                e >>= 1
+                j += 1
+        if not bits:
+            return 0, 0
+        top = max(bits)
+        return sum(pack(bits[j]) for j in bits), top
+
+    if mode == 1:
+        return power(0)
+    if mode == 2:
+        return pack(primes), 0
+    w, s = power(1)
+    return (w + pack(primes), s) if mode == 5 else (w, s)
+
+
+@pytest.mark.parametrize("mode,nmin", [(1, 101), (1, 5000), (2, 5000), (4, 5000), (5, 20011), (1, 65537)])
+def test_setup_program_size_matches_the_definition(pfc, mode, nmin):
+    assert pfc.setup_program_size(mode, nmin) == _program_model(mode, nmin)

@@ -67,3 +67,28 @@ def test_fcfs_latencies_match_an_event_simulation():
         assert abs(lat[i] - (clock - arr[i])) < 1e-9
     # an idle server: latency is the service time
     assert np.allclose(serving.fcfs_latencies([0.0, 10.0], [1.0, 2.0]), [1.0, 2.0])
+
+
+def test_batched_roofline_counts():
+    """bench.mixed_roofline: per search, candidates x (setup words x word cost
+    + squarings x squaring cost + algorithmic walk steps x step cost)."""
+    import types
+    pfc = pytest.importorskip("pfcsieve_gb300")
+    import bench
+    peaks = {"imad": 20e12, "mul_hi": 8e12, "imad_wide": 10e12, "iadd_xor": 40e12}
+    w, h = 2.0, 2.5
+    S = serving.Search
+    jobs = [S(1, 5000, 6000, 10**9, 10**9 + 10**6),          # class 32, n! : 1000 steps
+            S(4, 5000, 6000, 2**40, 2**40 + 10**6),          # class 64 below 2^64/3, composite n only
+            S(2, 5000, 6000, 2**63 + 10**6, 2**63 + 2 * 10**6)]  # class 64 above 2^64/3, prime n only
+    out = {i: types.SimpleNamespace(primecount=100 + i) for i in range(3)}
+    r = bench.mixed_roofline(jobs, out, 2.0, peaks)
+    primes = sum(1 for q in range(5000, 6000) if all(q % d for d in range(2, int(q ** 0.5) + 1)))
+    w1, s1 = pfc.setup_program_size(1, 5000)
+    w4, s4 = pfc.setup_program_size(4, 5000)
+    w2, s2 = pfc.setup_program_size(2, 5000, wide=False)
+    want = (100 * (w1 * (36 * w + 2) + s1 * (w + 1 + h) + 1000 * (2 * w + 1))
+            + 101 * (w4 * (76 * w + 3) + s4 * (8 * w + 2) + (1000 - primes) * (4 * w + 1))
+            + 102 * (w2 * (8 * w + 2) + s2 * (8 * w + 2) + primes * (7 * w + 2)))
+    assert abs(r["alg_ops"] - want) < 1e-6 * want
+    assert abs(r["frac"] - want / 2.0 / 20e12) < 1e-9
