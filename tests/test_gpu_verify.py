@@ -1,6 +1,6 @@
 """Device re-verification of hits (pfc_verify_factors_device) against the CPU
 check that the reference runs (pfc_finalize_factors with verify, the check of
-verifyprime.cpp:199-268), which stays the judge.
+verifyprime.cpp:199-268), which remains the check of record.
 
 Bar: the device's verdict equals the CPU check's verdict hit by hit, on true
 hits of every walk type and on records with one field wrong (sign, n, p), and
