@@ -4,14 +4,17 @@
 // The reference runs one search per process and one kernel per stage
 // (cl_sieve.cpp:1563-1726); a small search there leaves most of a large GPU
 // idle.  Here every admitted job contributes blocks of candidates (256, or 512
-// for two-candidate class-32 walks).  Each block has a timeline: its setup
+// for two-candidate class-32 walks and for class-32 setup windows, which run
+// one candidate per thread in CTAs of 512).  Each block has a timeline: its setup
 // programs as a table of runs ([0, S): squarings, table words, the fork of
 // the combined search), then its walk ([S, S+N): n steps, or prime steps for
 // n#).  All blocks of a job share one position.  One iteration gives every
 // running job (or, under the latency policy, every job the budget pays for)
 // a window of its timeline; the iteration's windows, sorted by task cost, are
-// one launch per size class with one CTA per block, dispatched by the
-// hardware block scheduler, so jobs of every size and mode share the SMs.
+// one launch per class group (class 32, class 64 below 2^64/3, other class 64)
+// and task kind (setup, walk, general) with one CTA per block, on six
+// streams, dispatched by the hardware block scheduler, so jobs of every size
+// and mode share the SMs.
 // Between iterations the host admits new jobs as memory and slots allow,
 // drains the hits (tagged with the job slot) and retires finished jobs:
 // requests that arrive while others run join at the next iteration.

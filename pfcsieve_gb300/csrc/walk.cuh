@@ -13,9 +13,11 @@
 // ORs its comparisons into one predicate; if any lane of the warp saw a hit
 // the warp replays that block from its saved start with per-step recording.
 //
-// Each launch walks one residue chain.  The combined search (-! -c) walks the
-// factorial chain over n and then the compositorial chain over a multiplier
-// table holding n at composite n and 1 at prime n (the reference skips prime
+// Single-chain searches walk NC candidates per thread.  The combined search
+// (-! -c) walks the factorial and the compositorial chain of one candidate
+// together (fused: shared targets, counter and loop); both take their
+// multipliers from a per-chunk table, n for the factorial and, for the
+// compositorial, n at composite n and 1 at prime n (the reference skips prime
 // n, iterate.cl:137-140, 181-184): multiplying by 1 keeps the drift at one
 // power of R per step, and the replay skips the test where the multiplier is
 // 1.  The fast path tests every step: at a prime n the compositorial value is
