@@ -5,8 +5,8 @@
 //   class-32 candidates: p, s0, s1 (u32) and nnext (u32)   16 B / candidate
 //   class-64 candidates: p, s0, s1 (u64) and nnext (u32)   28 B / candidate
 //   hit list pfc_factor[hitcap] + 64-bit counter
-//   setup programs (u32 words for class 32; 896-bit words below 2^64/3 and
-//   u64 words above for class 64), prime flags of [nmin, nmax) (1 bit per n)
+//   setup programs (896-bit words for class 32 and for class 64 below 2^64/3,
+//   u64 words above), prime flags of [nmin, nmax) (1 bit per n)
 //   or the prime list of [nmin, nmax) for the primorial walk
 //   per-segment accumulators: counts[2], termsum, flags
 //
