@@ -123,10 +123,27 @@ __device__ __forceinline__ void run_setup(const typename T::M (&m)[NC], typename
             const SW *wp = static_cast<const SW *>(J.words) + g.z + off;
             uint32_t k = 0;
             if constexpr (std::is_same<SW, WideWord>::value) {
-                // wide words are read inside T::word
-                for (; k < cnt; ++k) {
+                // Every thread of the CTA walks the same words: the CTA copies
+                // kStageWords of them at a time into shared memory with one
+                // coalesced load, and the threads read the limbs from there
+                // (a table word read from global memory by every warp waited
+                // on its loads: the pointer comes from the job record, so the
+                // address is not known to be warp-uniform).  Trip counts are
+                // uniform across the CTA, so every thread reaches the barriers.
+                constexpr uint32_t kStageWords = 16, kVec = sizeof(WideWord) / 16;
+                __shared__ uint4 stage[kStageWords * kVec];
+                const uint4 *src = reinterpret_cast<const uint4 *>(wp);
+                for (; k < cnt; k += kStageWords) {
+                    const uint32_t nw = min(kStageWords, cnt - k);
+                    __syncthreads();   // the previous chunk is consumed
+                    for (uint32_t i = threadIdx.x; i < nw * kVec; i += blockDim.x)
+                        stage[i] = __ldg(src + (size_t)k * kVec + i);
+                    __syncthreads();
+                    for (uint32_t u = 0; u < nw; ++u) {
+                        const SW *sp = reinterpret_cast<const SW *>(stage + u * kVec);
 #pragma unroll
-                    for (int c = 0; c < NC; ++c) acc[c] = T::word(m[c], sc[c], acc[c], wp + k);
+                        for (int c = 0; c < NC; ++c) acc[c] = T::template word<true>(m[c], sc[c], acc[c], sp);
+                    }
                 }
             } else {
                 constexpr uint32_t U = 4;

@@ -107,12 +107,15 @@ struct Cls32 {
     }
     // s < p: both rounds stay below 2^64 (s t < 2^63, m p < 2^63) and the
     // result is below 2p before the conditional subtraction
+    // SMEM: the word is read from shared memory (a staged copy) instead of
+    // through the read-only global path
+    template <bool SMEM = false>
     __device__ static __forceinline__ W word(const M &m, const SC &c, W s, const SW *wp) {
         const uint4 *v = reinterpret_cast<const uint4 *>(wp);
         uint64_t t = 0;
 #pragma unroll
         for (int k = 0; k < kWideLimbs / 4; ++k) {
-            const uint4 z = __ldg(v + k);
+            const uint4 z = SMEM ? v[k] : __ldg(v + k);
             t += (uint64_t)z.x * c.w[4 * k];
             t += (uint64_t)z.y * c.w[4 * k + 1];
             t += (uint64_t)z.z * c.w[4 * k + 2];
@@ -233,12 +236,13 @@ struct Cls64L {
         }
         return c;
     }
+    template <bool SMEM = false>
     __device__ static __forceinline__ W word(const M &m, const SC &c, W s, const SW *wp) {
         const uint4 *v = reinterpret_cast<const uint4 *>(wp);
         uint64_t u0 = 0, u1 = 0, hv = 0;
 #pragma unroll
         for (int k = 0; k < kWideLimbs / 4; ++k) {
-            const uint4 z4 = __ldg(v + k);
+            const uint4 z4 = SMEM ? v[k] : __ldg(v + k);
             const uint32_t z[4] = {z4.x, z4.y, z4.z, z4.w};
 #pragma unroll
             for (int j = 0; j < 4; ++j) {
