@@ -16,9 +16,10 @@ __global__ void __launch_bounds__(256) setup_kernel(ClassBuf<typename T::W> c, S
     using W = typename T::W;
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     const uint32_t cnt = min(*c.count, c.cap);
-    if (i >= cnt) return;
+    if (blockIdx.x * blockDim.x >= cnt) return;   // whole CTAs only: run_prog stages words per CTA
+    const bool act = i < cnt;
     typename T::M m;
-    m.init(c.p[i]);
+    m.init(act ? c.p[i] : (W)3);
     const typename T::SC sc = T::sctx(m);
     W s0, s1 = 0;
     if (a.mode == (PFC_FACTORIAL | PFC_COMPOSITORIAL)) {
@@ -27,9 +28,11 @@ __global__ void __launch_bounds__(256) setup_kernel(ClassBuf<typename T::W> c, S
     } else {
         s0 = run_prog<T>(m, sc, a.a, m.one);
     }
-    c.s0[i] = s0;
-    c.s1[i] = s1;
-    c.nnext[i] = a.nnext0;
+    if (act) {
+        c.s0[i] = s0;
+        c.s1[i] = s1;
+        c.nnext[i] = a.nnext0;
+    }
 }
 
 // ------------------------------------------------------------------- walk

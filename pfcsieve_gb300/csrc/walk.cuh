@@ -271,7 +271,9 @@ template <class W>
 __device__ __forceinline__ W ldg(const W *p) { return __ldg(p); }
 
 // Evaluate a setup program from Montgomery-form `acc` (see kernels.cuh Prog).
-// Wide words are read inside T::word; narrow ones are loaded four at a time.
+// Wide words are staged through shared memory by the whole CTA (every thread
+// of the CTA must call this with the same program); narrow ones are loaded
+// four at a time.
 template <class T>
 __device__ typename T::W run_prog(const typename T::M &m, const typename T::SC &sc, const Prog<typename T::SW> &pg,
                                   typename T::W acc) {
@@ -281,7 +283,22 @@ __device__ typename T::W run_prog(const typename T::M &m, const typename T::SC &
         for (uint32_t k = 0; k < sq; ++k) acc = T::sq(m, acc);
         uint32_t i = b;
         if constexpr (std::is_same<typename T::SW, WideWord>::value) {
-            for (; i < e; ++i) acc = T::word(m, sc, acc, pg.words + i);
+            // every thread of the CTA runs the same program: the CTA copies
+            // kStageWords words at a time into shared memory with one coalesced
+            // load and the threads read the limbs there (all threads of the
+            // CTA must call run_prog; trip counts are uniform)
+            constexpr uint32_t kStageWords = 16, kVec = sizeof(WideWord) / 16;
+            __shared__ uint4 stage[kStageWords * kVec];
+            const uint4 *src = reinterpret_cast<const uint4 *>(pg.words);
+            for (; i < e; i += kStageWords) {
+                const uint32_t nw = min(kStageWords, e - i);
+                __syncthreads();
+                for (uint32_t j = threadIdx.x; j < nw * kVec; j += blockDim.x)
+                    stage[j] = __ldg(src + (size_t)i * kVec + j);
+                __syncthreads();
+                for (uint32_t u = 0; u < nw; ++u)
+                    acc = T::template word<true>(m, sc, acc, reinterpret_cast<const WideWord *>(stage + u * kVec));
+            }
         } else {
             for (; i + 4 <= e; i += 4) {
                 acc = T::word(m, sc, acc, ldg(pg.words + i));
