@@ -64,65 +64,58 @@ static void help() {
     fail();
 }
 
-// Number with optional suffix: K M G T P (x1000^k), e<k> (x10^k),
-// k m g t p (x2^(10k)), b<k> (x2^k).  0 ok, -1 unparsable, -2 out of range.
-// Same rules as the reference's parse_uint64 (putil.c:34-116).
+// Number arguments: an integer (decimal, 0x hex or 0 octal) with at most one
+// suffix that scales it.  The accepted suffixes are the reference's
+// (putil.c:34-116): K M G T P scale by 1000^1..5, k m g t p by 1024^1..5,
+// e<d> / E<d> by 10^d and b<d> / B<d> by 2^d, where d is a number that ends
+// the text.  Each suffix is a (factor, repeat count) pair; the value is then
+// scaled by one checked multiplication per repeat.
+struct NumberSuffix {
+    char letter;
+    uint64_t factor;
+    int repeats;  // -1: the repeat count is the number written after the letter
+};
+
+static const NumberSuffix kNumberSuffixes[] = {
+    {'K', 1000, 1}, {'M', 1000, 2}, {'G', 1000, 3}, {'T', 1000, 4}, {'P', 1000, 5},
+    {'k', 1024, 1}, {'m', 1024, 2}, {'g', 1024, 3}, {'t', 1024, 4}, {'p', 1024, 5},
+    {'e', 10, -1},  {'E', 10, -1},  {'b', 2, -1},   {'B', 2, -1},
+};
+
+// 0: *out holds the value; -1: the text is not a number with an accepted
+// suffix; -2: the number, or the number scaled, lies outside [lo, hi].
 static int parse_u64(uint64_t *out, const char *s, uint64_t lo, uint64_t hi) {
     errno = 0;
-    char *tail = nullptr;
-    uint64_t v = strtoull(s, &tail, 0);
-    if (errno != 0 || v > hi) return -2;
-    unsigned e = 0;
-    switch (*tail) {
-        case 'P': e += 3; /* fall through */
-        case 'T': e += 3; /* fall through */
-        case 'G': e += 3; /* fall through */
-        case 'M': e += 3; /* fall through */
-        case 'K':
-            e += 3;
-            if (tail[1] != '\0') return -1;
-            for (; e > 0; e -= 3) {
-                if (v > hi / 1000) return -2;
-                v *= 1000;
-            }
-            break;
-        case 'e':
-        case 'E': {
-            e = (unsigned)strtoul(tail + 1, &tail, 0);
+    char *end = nullptr;
+    uint64_t value = strtoull(s, &end, 0);
+    if (errno != 0 || value > hi) return -2;
+
+    uint64_t factor = 1, repeats = 0;
+    if (*end != '\0') {
+        const NumberSuffix *suffix = nullptr;
+        for (const NumberSuffix &cand : kNumberSuffixes)
+            if (cand.letter == *end) suffix = &cand;
+        if (suffix == nullptr) return -1;
+        const char *rest = end + 1;
+        factor = suffix->factor;
+        if (suffix->repeats >= 0) {
+            repeats = (uint64_t)suffix->repeats;
+        } else {
+            char *after = nullptr;
+            errno = 0;
+            repeats = strtoull(rest, &after, 0);
             if (errno != 0) return -2;
-            if (*tail != '\0') return -1;
-            while (e-- > 0) {
-                if (v > hi / 10) return -2;
-                v *= 10;
-            }
-            break;
+            rest = after;
         }
-        case 'p': e += 10; /* fall through */
-        case 't': e += 10; /* fall through */
-        case 'g': e += 10; /* fall through */
-        case 'm': e += 10; /* fall through */
-        case 'k':
-            e += 10;
-            if (tail[1] != '\0') return -1;
-            if (v > (hi >> e)) return -2;
-            v <<= e;
-            break;
-        case 'b':
-        case 'B': {
-            e = (unsigned)strtoul(tail + 1, &tail, 0);
-            if (errno != 0) return -2;
-            if (*tail != '\0') return -1;
-            while (e-- > 0) {
-                if (v > (hi >> 1)) return -2;
-                v <<= 1;
-            }
-            break;
-        }
-        case '\0': break;
-        default: return -1;
+        if (*rest != '\0') return -1;
     }
-    if (v < lo) return -2;
-    *out = v;
+
+    for (uint64_t i = 0; i < repeats && value != 0; ++i) {
+        if (value > hi / factor) return -2;
+        value *= factor;
+    }
+    if (value < lo) return -2;
+    *out = value;
     return 0;
 }
 

@@ -60,6 +60,10 @@ def test_record_size():
     (["-!", "-n", "101", "-N", "200", "-p", "1x", "-P", "2e6"], "invalid argument -p 1x"),
     (["-!", "-n", "101", "-N", "200", "-p", "1e6", "-P", "2e6", "-v", "129"], "out of range argument -v"),
     (["-!", "-n", "101", "-N", "200", "-p", "1e6", "-P", "18447P"], "out of range argument -P 18447P"),
+    (["-!", "-n", "101", "-N", "200", "-p", "1e6", "-P", "1k1"], "invalid argument -P 1k1"),
+    (["-!", "-n", "101", "-N", "200", "-p", "1e6", "-P", "16b60"], "out of range argument -P 16b60"),
+    (["-!", "-n", "101", "-N", "200", "-p", "1e6", "-P", "2e6x"], "invalid argument -P 2e6x"),
+    (["-!", "-n", "101", "-N", "200", "-p", "1e6", "-P", "18446744073709551616"], "out of range argument -P"),
 ])
 def test_rejected(tmp_path, args, msg):
     rc, out, err = run(args, tmp_path)
@@ -70,6 +74,8 @@ def test_rejected(tmp_path, args, msg):
 @pytest.mark.parametrize("arg,val", [
     ("1K", 1000), ("2M", 2000000), ("3e6", 3000000), ("4k", 4096), ("1m", 1 << 20),
     ("1b20", 1 << 20), ("0x10000", 65536), ("7G", 7 * 10**9), ("2t", 2 << 40), ("1P", 10**15),
+    ("5E3", 5000), ("3B4", 48), ("0x10K", 16000), ("9e0", 9), ("16p", 1 << 54), ("010", 8),
+    ("18446744073709551615", 2**64 - 1), ("15b60", 15 << 60),
 ])
 def test_number_suffixes(tmp_path, arg, val):
     rc, out, err = run(["-!", "-n", "101", "-N", "200", "-p", "3", "-P", arg], tmp_path)
