@@ -106,6 +106,13 @@ int pfc_ctx_device_info(pfc_ctx *ctx, char *name, size_t name_cap, int *sm_count
  * 101 <= nmin <= nmax < 2^31 (main.cpp:58-72, cl_sieve.cpp:631-641). */
 int pfc_job_create(pfc_ctx *ctx, unsigned mode, uint32_t nmin, uint32_t nmax,
                    uint64_t pmin, uint64_t pmax, pfc_job **out);
+
+/* The same call under the name of the stage-call interface: a search of
+ * `mode` over n in [nmin, nmax) and p in [pmin, pmax) is submitted to the
+ * context that will run its stages (setupSearch, cl_sieve.cpp:596-665, and
+ * the per-run table set-up that follows it).  Identical to pfc_job_create. */
+int pfc_job_submit(pfc_ctx *ctx, unsigned mode, uint32_t nmin, uint32_t nmax,
+                   uint64_t pmin, uint64_t pmax, pfc_job **out);
 int pfc_job_destroy(pfc_job *job);
 
 /* Suggest the end of the next p-segment starting at p_lo, sized to the
@@ -254,14 +261,18 @@ int pfc_format_factor(const pfc_factor *f, char *buf, size_t cap);
  * Limits (PFC_ERR_ARG beyond them): at most 2^18 expected candidates per size
  * class (p < 2^31 and p >= 2^31; roughly (p_hi - p_lo) / ln p_lo <= 2^18 / 1.25),
  * nmax - nmin <= 2^22, at most 2^18 primes in [nmin, nmax) for n#, and setup
- * tables of at most 2^12 896-bit words (p < 2^31) and 2^16 64-bit words
- * (p >= 2^31): nmin up to a few 10^5.
+ * tables of at most 2^12 896-bit words (p < 2^64/3) and 2^16 64-bit words
+ * (p >= 2^64/3): nmin up to a few 10^5.  Requests whose nmin is far beyond
+ * that are refused before any host table is built.
  *
  * The first call on each device resolves the device address of the array and
  * stores the sieve patterns in it; make that first call before any stream
- * capture.  All calls on a device share the array and it keeps the last call's
- * contents (the call clears what must start at zero): calls that overlap on
- * the GPU race, so issue them one at a time per device. */
+ * capture.  The call copies tables from host memory that lives only for the
+ * call and waits for `stream` before it returns, so a call on a stream that is
+ * capturing returns PFC_ERR_STATE and enqueues nothing.  All calls on a device
+ * share the array and it keeps the last call's contents (the call clears what
+ * must start at zero): calls that overlap on the GPU race, so issue them one
+ * at a time per device. */
 int pfc_segment_noalloc(unsigned mode, uint32_t nmin, uint32_t nmax, uint64_t p_lo, uint64_t p_hi,
                         pfc_factor *d_hits, uint64_t hit_cap, uint64_t *d_totals, void *stream);
 

@@ -300,6 +300,11 @@ extern "C" int pfc_job_create(pfc_ctx *c, unsigned mode, uint32_t nmin, uint32_t
     return PFC_OK;
 }
 
+extern "C" int pfc_job_submit(pfc_ctx *c, unsigned mode, uint32_t nmin, uint32_t nmax, uint64_t pmin,
+                              uint64_t pmax, pfc_job **out) {
+    return pfc_job_create(c, mode, nmin, nmax, pmin, pmax, out);
+}
+
 extern "C" int pfc_job_destroy(pfc_job *j) {
     if (!j) return PFC_ERR_ARG;
     job_release(j);

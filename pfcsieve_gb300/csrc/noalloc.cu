@@ -16,6 +16,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <mutex>
 #include <type_traits>
@@ -71,10 +72,10 @@ namespace {
 
 // d_totals = {checksum terms, candidates, hits, flags}; flag bit 0: candidate
 // overflow, bit 1: n-counter validation failure
-__global__ void noalloc_finish_kernel(uint64_t *totals) {
+__global__ void noalloc_finish_kernel(uint64_t *totals, uint32_t cap) {
     const Stats *s = reinterpret_cast<const Stats *>(g_noalloc_scratch + kOffStats);
     uint64_t flags = 0;
-    if (s->counts[0] > kCands || s->counts[1] > kCands) flags |= 1;
+    if (s->counts[0] > cap || s->counts[1] > cap) flags |= 1;
     if (s->flags & 1u) flags |= 2;
     totals[0] = s->termsum;
     totals[1] = (uint64_t)s->counts[0] + s->counts[1];
@@ -107,6 +108,28 @@ int device_scratch(int dev, unsigned char **base) {
     return PFC_OK;
 }
 
+// Candidates per size class that one call holds: kCands, or less when the
+// environment sets PFCSIEVE_NOALLOC_CAND_CAP (tests use it to exercise the
+// candidate-overflow flag; values above kCands are ignored).
+uint32_t cand_capacity() {
+    const char *v = getenv("PFCSIEVE_NOALLOC_CAND_CAP");
+    if (!v || !*v) return kCands;
+    const unsigned long long c = strtoull(v, nullptr, 10);
+    return c >= 1 && c < kCands ? (uint32_t)c : kCands;
+}
+
+// Lower bound on the bits of any setup program for (nmin - 1): every program
+// multiplies at least the primes q <= (nmin - 1) / 2 (the compositorial's
+// exponents e_q - 1 are non-zero exactly there), and their product has
+// theta(x) / ln 2 bits, theta(x) > x (1 - 1 / ln x) for x >= 41 (Rosser and
+// Schoenfeld, 1962).  Lets a call whose tables cannot fit the scratch be
+// rejected before the host sieves primes up to nmax.
+double setup_bits_lower_bound(uint32_t startN) {
+    const double x = startN / 2;
+    if (x < 41) return 0;
+    return x * (1.0 - 1.0 / std::log(x)) / std::log(2.0);
+}
+
 double est_cands(uint64_t lo, uint64_t hi) {
     if (hi <= lo) return 0;
     const double a = (double)std::max<uint64_t>(lo, 114);
@@ -127,21 +150,35 @@ extern "C" int pfc_segment_noalloc(unsigned mode, uint32_t nmin, uint32_t nmax, 
     const double e32 = est_cands(p_lo, std::min(p_hi, split));
     const double e64 = est_cands(std::max(p_lo, split), p_hi);
     if (e32 > kCands || e64 > kCands) return PFC_ERR_ARG;
-
     const uint32_t startN = nmin - 1;
+    if (setup_bits_lower_bound(startN) > std::max<double>(kWords32 * 896.0, kWords64 * 64.0)) return PFC_ERR_ARG;
+
+    // The call enqueues copies from host memory that lives only for the call
+    // and waits for the stream at the end; on a stream that is being captured
+    // either would end the caller's capture with an error, so refuse first.
+    cudaStreamCaptureStatus capture = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing((cudaStream_t)stream, &capture) != cudaSuccess ||
+        capture != cudaStreamCaptureStatusNone)
+        return PFC_ERR_STATE;
+
+    // size classes present, and which setup program forms they need: 896-bit
+    // words below 2^64/3 (class 32 and the lazy class 64), 64-bit words above
+    const bool use32 = p_lo < split, use64 = p_hi > split;
+    const bool wide64 = use64 && p_hi <= kLazyEnd;
+    const bool need_wide = use32 || wide64, need_narrow = use64 && !wide64;
+
     const uint32_t plim = (mode & PFC_COMPOSITORIAL) ? nmax : std::max(startN, nmax ? nmax - 1 : 0);
     const std::vector<uint32_t> primes = primes_between(2, plim);
     const std::vector<uint32_t> below(primes.begin(), std::upper_bound(primes.begin(), primes.end(), startN));
     HostProg<WideWord> a32, b32;
     HostProg<uint64_t> a64, b64;
-    bool ok = true;
-    if (mode == PFC_FACTORIAL) ok = build_power_prog(startN, 0, primes, a32) && build_power_prog(startN, 0, primes, a64);
-    else if (mode == PFC_COMPOSITORIAL) ok = build_power_prog(startN, 1, primes, a32) && build_power_prog(startN, 1, primes, a64);
-    else if (mode == PFC_PRIMORIAL) ok = build_product_prog(below, a32) && build_product_prog(below, a64);
-    else
-        ok = build_power_prog(startN, 1, primes, a32) && build_power_prog(startN, 1, primes, a64) &&
-             build_product_prog(below, b32) && build_product_prog(below, b64);
-    if (!ok) return PFC_ERR_ARG;
+    auto build = [&](auto &a, auto &b) {
+        if (mode == PFC_FACTORIAL) return build_power_prog(startN, 0, primes, a);
+        if (mode == PFC_COMPOSITORIAL) return build_power_prog(startN, 1, primes, a);
+        if (mode == PFC_PRIMORIAL) return build_product_prog(below, a);
+        return build_power_prog(startN, 1, primes, a) && build_product_prog(below, b);
+    };
+    if ((need_wide && !build(a32, b32)) || (need_narrow && !build(a64, b64))) return PFC_ERR_ARG;
     if (a32.words.size() + b32.words.size() > kWords32 || a64.words.size() + b64.words.size() > kWords64 ||
         a32.groups.size() + b32.groups.size() + a64.groups.size() + b64.groups.size() > 3 * kGroups)
         return PFC_ERR_ARG;
@@ -213,20 +250,20 @@ extern "C" int pfc_segment_noalloc(unsigned mode, uint32_t nmin, uint32_t nmax, 
         errs.push_back(cudaMemcpyAsync(q, qlist.data(), qlist.size() * 4, cudaMemcpyHostToDevice, st));
 
     // candidate classes inside the scratch
-    const bool use32 = p_lo < split, use64 = p_hi > split;
+    const uint32_t cap = cand_capacity();
     ClassBuf<uint32_t> c32;
     c32.p = reinterpret_cast<uint32_t *>(base + kOffC32);
     c32.s0 = c32.p + kCands;
     c32.s1 = c32.s0 + kCands;
     c32.nnext = c32.s1 + kCands;
-    c32.cap = kCands;
+    c32.cap = cap;
     c32.count = counts;
     ClassBuf<uint64_t> c64;
     c64.p = reinterpret_cast<uint64_t *>(base + kOffC64);
     c64.s0 = c64.p + kCands;
     c64.s1 = c64.s0 + kCands;
     c64.nnext = reinterpret_cast<uint32_t *>(c64.s1 + kCands);
-    c64.cap = kCands;
+    c64.cap = cap;
     c64.count = counts + 1;
 
     // generate
@@ -237,8 +274,8 @@ extern "C" int pfc_segment_noalloc(unsigned mode, uint32_t nmin, uint32_t nmax, 
     g.nodd = p_hi > gbase ? (p_hi - gbase + 1) / 2 : 0;
     g.p32 = c32.p;
     g.p64 = c64.p;
-    g.cap32 = use32 ? kCands : 0;
-    g.cap64 = use64 ? kCands : 0;
+    g.cap32 = use32 ? cap : 0;
+    g.cap64 = use64 ? cap : 0;
     g.count = counts;
     g.pat = reinterpret_cast<const uint64_t *>(base + kOffPat);
     static const uint32_t sp[kSmallPrimes] = {3,  5,  7,  11, 13, 17, 19, 23, 29, 31, 37,  41,  43,  47,  53,
@@ -248,7 +285,8 @@ extern "C" int pfc_segment_noalloc(unsigned mode, uint32_t nmin, uint32_t nmax, 
 
     // setup
     if (use32) launch_setup32(c32, s32, st);
-    if (use64) launch_setup64(c64, s64, st);
+    if (wide64) launch_setup64w(c64, s32, st);
+    else if (use64) launch_setup64(c64, s64, st);
 
     // walks over [nmin, nmax) (prime indices for n#), in chunks of kChunk
     HitBuf h{};
@@ -301,7 +339,7 @@ extern "C" int pfc_segment_noalloc(unsigned mode, uint32_t nmin, uint32_t nmax, 
     ck.flags = &stats->flags;
     if (use32) launch_check32(c32, ck, st);
     if (use64) launch_check64(c64, ck, st);
-    noalloc_finish_kernel<<<1, 1, 0, st>>>(d_totals);
+    noalloc_finish_kernel<<<1, 1, 0, st>>>(d_totals, cap);
 
     errs.push_back(cudaGetLastError());
     // the host tables above must outlive their copies: wait for the stream

@@ -35,6 +35,16 @@ CASES = [
     (1, 101, 5000, 3, 50000),
 ]
 
+# one call whose p range holds both size classes (it crosses 2^31), the
+# combined search on class-64 p below 2^64/3 (lazy steps, 896-bit setup
+# words), and segments at or above 2^64/3 (canonical 64-bit steps)
+MORE_CASES = [
+    (5, 101, 5000, 2**31 - 10**6, 2**31 + 10**6),
+    (5, 1000, 8000, 2**50, 2**50 + 10**6),
+    (1, 101, 3000, 2**64 - 2 * 10**6, 2**64 - 1),
+    (4, 500, 4000, 2**64 // 3 - 5 * 10**5, 2**64 // 3 + 5 * 10**5),
+]
+
 
 def with_allocation(mode, nmin, nmax, lo, hi):
     with pfc.Context(0) as ctx, pfc.Job(ctx, mode, nmin, nmax, lo, hi) as job:
@@ -44,12 +54,19 @@ def with_allocation(mode, nmin, nmax, lo, hi):
     return termsum, count, hits
 
 
+def call(case, hits, cap, totals, stream=None):
+    """One call through the C ABI into caller-owned device buffers."""
+    mode, nmin, nmax, lo, hi = case
+    if stream is None:
+        stream = torch.cuda.current_stream().cuda_stream
+    return pfc.lib().pfc_segment_noalloc(mode, nmin, nmax, lo, hi, ctypes.c_void_p(hits.data_ptr()), cap,
+                                         ctypes.c_void_p(totals.data_ptr()), ctypes.c_void_p(stream))
+
+
 def without_allocation(mode, nmin, nmax, lo, hi, cap=1 << 16):
     hits = torch.zeros(cap * pfc.FACTOR_DTYPE.itemsize, dtype=torch.uint8, device="cuda")
     totals = torch.zeros(4, dtype=torch.int64, device="cuda")
-    stream = torch.cuda.current_stream().cuda_stream
-    rc = pfc.lib().pfc_segment_noalloc(mode, nmin, nmax, lo, hi, ctypes.c_void_p(hits.data_ptr()), cap,
-                                       ctypes.c_void_p(totals.data_ptr()), ctypes.c_void_p(stream))
+    rc = call((mode, nmin, nmax, lo, hi), hits, cap, totals)
     assert rc == 0, pfc.status_string(rc)
     t = totals.cpu().numpy().view(np.uint64)
     n = int(t[2])
@@ -86,3 +103,77 @@ def test_requests_beyond_the_limits_are_rejected():
     rc = L.pfc_segment_noalloc(1, 101, 101 + (1 << 22) + 1, 10**9, 10**9 + 1000, None, 0,
                                ctypes.c_void_p(totals.data_ptr()), None)
     assert rc == -1
+
+
+@pytest.mark.parametrize("case", MORE_CASES)
+def test_both_classes_and_the_canonical_class_64(case):
+    want = with_allocation(*case)
+    termsum, count, hits, flags = without_allocation(*case)
+    assert flags == 0
+    assert (termsum, count) == want[:2], case
+    assert np.array_equal(hits, want[2]), case
+
+
+def test_call_leaves_device_memory_unchanged():
+    """After a first call on the device (which resolves the array's address),
+    a call changes nothing in the device's free memory."""
+    case = CASES[0]
+    cap = 1 << 12
+    hits = torch.zeros(cap * pfc.FACTOR_DTYPE.itemsize, dtype=torch.uint8, device="cuda")
+    totals = torch.zeros(4, dtype=torch.int64, device="cuda")
+    assert call(case, hits, cap, totals) == 0
+    torch.cuda.synchronize()
+    free_before, _ = torch.cuda.mem_get_info()
+    assert call(case, hits, cap, totals) == 0
+    torch.cuda.synchronize()
+    free_after, _ = torch.cuda.mem_get_info()
+    assert free_after == free_before
+
+
+def test_hits_beyond_the_capacity_are_counted_not_written():
+    case = CASES[2]                      # factorial with p <= n: many hits
+    full = with_allocation(*case)[2]
+    slots = 16
+    hits = torch.full((slots * pfc.FACTOR_DTYPE.itemsize,), 0xFF, dtype=torch.uint8, device="cuda")
+    totals = torch.zeros(4, dtype=torch.int64, device="cuda")
+    assert call(case, hits, 1, totals) == 0
+    t = totals.cpu().numpy().view(np.uint64)
+    assert int(t[2]) == len(full) > 1
+    rec = hits.cpu().numpy().view(pfc.FACTOR_DTYPE)
+    assert (full == rec[0]).any()
+    assert (hits.cpu().numpy()[pfc.FACTOR_DTYPE.itemsize:] == 0xFF).all()
+
+
+def test_candidate_overflow_sets_the_flag(monkeypatch):
+    """More candidates than the call holds: flag bit 0, the true count, and no
+    write beyond the capacity (the test lowers the capacity to 1000 through
+    the library's environment setting; the p range holds about 4,800)."""
+    case = (1, 101, 2000, 10**9, 10**9 + 10**5)
+    want_count = with_allocation(*case)[1]
+    monkeypatch.setenv("PFCSIEVE_NOALLOC_CAND_CAP", "1000")
+    termsum, count, hits, flags = without_allocation(*case)
+    assert flags & 1
+    assert count == want_count > 1000
+    monkeypatch.delenv("PFCSIEVE_NOALLOC_CAND_CAP")
+    termsum, count, hits, flags = without_allocation(*case)
+    assert flags == 0 and count == want_count
+
+
+def test_call_on_a_capturing_stream_is_refused():
+    """The call waits for its stream and copies from short-lived host memory,
+    so on a stream under capture it returns PFC_ERR_STATE and enqueues
+    nothing: the caller's capture stays valid."""
+    cap = 1 << 10
+    hits = torch.zeros(cap * pfc.FACTOR_DTYPE.itemsize, dtype=torch.uint8, device="cuda")
+    totals = torch.zeros(4, dtype=torch.int64, device="cuda")
+    x = torch.zeros(1, device="cuda")
+    side = torch.cuda.Stream()
+    graph = torch.cuda.CUDAGraph()
+    torch.cuda.synchronize()
+    with torch.cuda.graph(graph, stream=side):
+        x += 1
+        rc = call(CASES[0], hits, cap, totals, stream=side.cuda_stream)
+    assert rc == -7
+    graph.replay()
+    torch.cuda.synchronize()
+    assert float(x.item()) == 1.0
