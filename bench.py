@@ -37,10 +37,15 @@ served by the request loop with Poisson arrivals (200 per second, seed 1):
 p50 and p99 latency from arrival to result, against the same arrivals served
 one at a time.  --workload mixed makes that comparison the headline line.
 
---impl reference times the reference algorithm's CPU form (the oracle port of
-the reference kernels, OpenMP over all host threads) on a bounded sample of
-the same workload.  Under torchrun each rank runs its own p range (weak
-scaling) and rank 0 prints the JSON line.
+--impl reference times the reference's CPU path on a bounded sample of the
+same workload: its own kernels/setup.cl and kernels/iterate.cl compiled for the
+CPU (oracle/_ref/libpfcref.so, OpenMP over all host threads), or the oracle's
+restatement of them where the reference sources were not staged.
+--impl reference-opencl times the reference's own OpenCL program
+(oracle/_ref/pfcsieve_ref, built from its sources) on this GPU end to end, as a
+user runs it, with as many verification threads as ours.  The default line
+carries the same measurement as `reference_opencl`.  Under torchrun each rank
+runs its own p range (weak scaling) and rank 0 prints the JSON line.
 """
 import argparse
 import json
@@ -84,7 +89,7 @@ def parse():
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
-    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference", "reference-opencl"])
     ap.add_argument("--workload", default="combined", choices=sorted(WORKLOADS))
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--cpu-sample", type=int, default=0,
@@ -93,8 +98,10 @@ def parse():
     ap.add_argument("--no-mixed", action="store_true", help="skip the batched-vs-plain comparison")
     ap.add_argument("--iteration-work", type=float, default=None,
                     help="batch iteration length in candidate-steps (default: the library's for the policy)")
-    ap.add_argument("--mixed-jobs", type=int, default=32,
-                    help="searches of the mixed workload sample (the full set is 512)")
+    ap.add_argument("--mixed-jobs", type=int, default=512,
+                    help="searches of the mixed workload (the full set is 512)")
+    ap.add_argument("--no-reference-opencl", action="store_true",
+                    help="skip timing the reference's OpenCL program")
     return ap.parse_args()
 
 
@@ -220,9 +227,21 @@ class ClockSampler:
 
 # ------------------------------------------------------- CPU baseline (oracle)
 
-def cpu_sample_run(wl, ncands, offset=0):
-    """Time the oracle (the reference algorithm on the CPU) on `ncands`
-    candidates of the workload's p range, all host threads."""
+def cpu_kind():
+    """'reference' when the reference's own kernels are built for the CPU
+    (oracle/_ref/libpfcref.so), else 'port' (the oracle's restatement)."""
+    from oracle import oracle as o
+    o.build()
+    return "reference" if o.ref_available() else "port"
+
+
+REF_HIT_CAP = 1 << 24
+
+
+def cpu_sample_run(wl, ncands, offset=0, kind="port"):
+    """Time the reference's CPU path on `ncands` candidates of the workload's
+    p range with all host threads: kind 'reference' runs the reference's own
+    setup/iterate kernels compiled for the CPU, 'port' the oracle."""
     from oracle import oracle as o
     o.build()
     # candidates of a short range at the bottom of the workload's p range
@@ -231,10 +250,78 @@ def cpu_sample_run(wl, ncands, offset=0):
     cands = o.candidates(lo, lo + span)[:ncands]
     threads = os.cpu_count() or 1
     t0 = time.perf_counter()
-    o.sieve(wl["mode"], wl["nmin"], wl["nmax"], cands, threads)
+    if kind == "reference":
+        # iterate chunks sized so that the kernels' unbounded hit appends fit
+        nstep = int(max(64, min(20000, REF_HIT_CAP // (2 * max(len(cands), 1)))))
+        o.ref_segment(wl["mode"], wl["nmin"], wl["nmax"], cands, nstep=nstep, hit_cap=REF_HIT_CAP)
+    else:
+        o.sieve(wl["mode"], wl["nmin"], wl["nmax"], cands, threads)
     dt = time.perf_counter() - t0
     pairs = len(cands) * (wl["nmax"] - wl["nmin"])
     return pairs / dt, dict(cores=threads, seconds=dt, cands=len(cands), pairs=pairs)
+
+
+CPU_KIND_TEXT = {"reference": "the reference's kernels/setup.cl + kernels/iterate.cl compiled for the CPU "
+                              "(oracle/_ref/libpfcref.so), OpenMP over candidates",
+                 "port": "the oracle's restatement of the reference kernels (oracle/liboracle.so), "
+                         "OpenMP over candidates"}
+
+
+# ------------------------------------------------- reference OpenCL program
+
+MODE_FLAGS = {1: ["-!"], 2: ["-#"], 4: ["-c"], 5: ["-!", "-c"]}
+
+
+def _ref_opencl_run(exe, wl, lo, hi, threads, timeout):
+    import re
+    import tempfile
+    cmd = [exe] + MODE_FLAGS[wl["mode"]] + ["-n", str(wl["nmin"]), "-N", str(wl["nmax"]),
+                                            "-p", str(lo), "-P", str(hi), "-v", str(threads)]
+    with tempfile.TemporaryDirectory() as d:
+        t = time.perf_counter()
+        r = subprocess.run(cmd, cwd=d, stdout=subprocess.PIPE, stderr=subprocess.PIPE, text=True,
+                           timeout=timeout)
+        wall = time.perf_counter() - t
+    m = re.search(r"factors (\d+), prime count (\d+), checksum ([0-9A-F]{16})", r.stdout)
+    if r.returncode != 0 or not m:
+        tail = (r.stdout + r.stderr).strip().splitlines()[-1:] or ["no output"]
+        raise RuntimeError("reference OpenCL program failed (rc %d): %s" % (r.returncode, tail[0]))
+    return wall, int(m.group(1)), int(m.group(2)), m.group(3)
+
+
+def reference_opencl(wl, lo, hi, runs=1):
+    """The reference's OpenCL program (built from its sources with the
+    standalone BOINC and prime-list stand-ins, oracle/Makefile `refcl`) run on
+    this GPU over the same search, timed from process start to exit: JIT
+    build of its kernels (cached by the driver after the first run), tables,
+    sieve, CPU verification of every factor, factors.txt.  A run over a
+    1,000-wide p range at the bottom of the range first warms the kernel cache
+    and measures the fixed costs; `sieve_pairs_per_s` takes them out."""
+    exe = os.path.join(ROOT, "oracle", "_ref", "pfcsieve_ref")
+    chk = os.path.join(ROOT, "oracle", "_ref", "refcl_check")
+    if not (os.path.exists(exe) and os.path.exists(chk)):
+        return {"unavailable": "reference OpenCL program not built (reference sources not staged)"}
+    r = subprocess.run([chk], stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True, timeout=300)
+    if r.returncode != 0:
+        return {"unavailable": "OpenCL dispatch check failed: %s" % (r.stdout.strip().splitlines()[-1:] or [""])[0]}
+    threads = os.cpu_count() or 1
+    try:
+        fixed, _, _, _ = _ref_opencl_run(exe, wl, lo, lo + 1000, threads, 600)
+        walls, res = [], None
+        for _ in range(max(1, runs)):
+            w, fc, pc, ck = _ref_opencl_run(exe, wl, lo, hi, threads, 3600)
+            walls.append(w)
+            res = (fc, pc, ck)
+    except Exception as e:   # noqa: BLE001
+        return {"unavailable": str(e)}
+    wall = float(np.mean(walls))
+    pairs = res[1] * (wl["nmax"] - wl["nmin"])
+    return {"program": "oracle/_ref/pfcsieve_ref (the reference's main.cpp, cl_sieve.cpp, simpleCL.c, "
+                       "kernels/*.cl; OpenCL on this GPU)",
+            "wall_s": wall, "runs": len(walls), "fixed_s": fixed, "verify_threads": threads,
+            "e2e_pairs_per_s": pairs / wall,
+            "sieve_pairs_per_s": pairs / max(wall - fixed, 1e-9),
+            "pairs": int(pairs), "factors": res[0], "primecount": res[1], "checksum": res[2]}
 
 
 def auto_sample(wl):
@@ -251,24 +338,49 @@ def auto_sample(wl):
 def run_reference(args, wl, world, rank):
     if rank != 0:
         return
+    kind = cpu_kind()
     n = args.cpu_sample or max(16, auto_sample(wl) // 4)
-    rates = []
+    pairs, secs = 0, 0.0
     info = None
     for s in range(args.warmup + args.steps):
-        rate, info = cpu_sample_run(wl, n, offset=s * 1000)
+        rate, info = cpu_sample_run(wl, n, offset=s * 1000, kind=kind)
         if s >= args.warmup:
-            rates.append(rate)
-    value = float(np.mean(rates))
+            pairs += info["pairs"]
+            secs += info["seconds"]
+    value = pairs / secs
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT,
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": info["seconds"] * 1e3, "higher_is_better": True, "scaling": "weak",
+        "ms_per_step": secs / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "u64", "data": "synthetic (deterministic search bounds)",
         "config": {"workload": wl["desc"], "sample": "%d candidates x full n range per step" % n,
                    "l2": "n/a (CPU)"},
-        "cpu_baseline": {"value": value, "unit": UNIT, "cores": info["cores"], "kind": "port",
-                         "sample": "%d candidates from the bottom of the p range x all n" % n},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": info["cores"], "kind": kind,
+                         "sample": "%d candidates from the bottom of the p range x all n; %s"
+                                   % (n, CPU_KIND_TEXT[kind])},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_reference_opencl_line(args, wl, rank):
+    """--impl reference-opencl: the reference's OpenCL program on this GPU."""
+    if rank != 0:
+        return
+    lo, hi = shard(wl, 0)
+    r = reference_opencl(wl, lo, hi, runs=args.steps)
+    if "unavailable" in r:
+        print(json.dumps({"impl": "reference-opencl", "unavailable": r["unavailable"]}), flush=True)
+        return
+    line = {
+        "impl": "reference-opencl", "metric": METRIC, "value": r["e2e_pairs_per_s"], "unit": UNIT,
+        "n_gpus": 1, "steps": r["runs"], "warmup": 1, "ms_per_step": r["wall_s"] * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64",
+        "data": "synthetic (deterministic search bounds)",
+        "config": {"workload": wl["desc"], "l2": "n/a (whole program per step)"},
+        "e2e": {"value": r["e2e_pairs_per_s"], "unit": UNIT, "h2d_bytes_per_step": None,
+                "d2h_bytes_per_step": None},
+        "reference_opencl": r,
     }
     print(json.dumps(line), flush=True)
 
@@ -281,7 +393,7 @@ def run_reference_mixed(args, rank):
         return
     from oracle import oracle as o
     from pfcsieve_gb300 import serving as sv
-    o.build()
+    kind = cpu_kind()
     jobs = sv.mixed_jobs(512, seed=0)
     threads = os.cpu_count() or 1
     pairs_t, secs_t, samples = 0, 0.0, []
@@ -294,7 +406,11 @@ def run_reference_mixed(args, rank):
         span = max(int(m * np.log(float(s.pmin)) * 1.3), 1000)
         cands = o.candidates(s.pmin, min(s.pmin + span, s.pmax))[:m]
         t = time.perf_counter()
-        o.sieve(s.mode, s.nmin, s.nmax, cands, threads)
+        if kind == "reference":
+            nstep = int(max(64, min(20000, REF_HIT_CAP // (2 * max(len(cands), 1)))))
+            o.ref_segment(s.mode, s.nmin, s.nmax, cands, nstep=nstep, hit_cap=REF_HIT_CAP)
+        else:
+            o.sieve(s.mode, s.nmin, s.nmax, cands, threads)
         dt = time.perf_counter() - t
         if step >= args.warmup:
             pairs_t += len(cands) * (s.nmax - s.nmin)
@@ -309,8 +425,9 @@ def run_reference_mixed(args, rank):
         "config": {"workload": WORKLOADS["mixed"]["desc"],
                    "sample": "per step one search of the set (in order): %s candidates x its full n range, "
                              "setup included" % samples, "l2": "n/a (CPU)"},
-        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
-                         "sample": "candidates %s of searches %d.. of the mixed set" % (samples, args.warmup)},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": kind,
+                         "sample": "candidates %s of searches %d.. of the mixed set; %s"
+                                   % (samples, args.warmup, CPU_KIND_TEXT[kind])},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -593,18 +710,33 @@ def run_ours(args, wl, world, rank, local, dist):
                "seconds_per_step": float(np.mean(walls)),
                "factors": int(res.factorcount), "checksum": res.checksum_hex()}
 
+    ctx.close()
+
     batched = None
     if rank == 0 and not args.no_mixed:
-        batched = run_mixed(ctx, args.mixed_jobs, args.warmup, iteration_work=args.iteration_work, peaks=peaks)
+        # the mixed workload's own context, under the 120 GB device budget of
+        # the serving configuration
+        mctx = pfc.Context(local, budget=120 * 10**9)
+        batched = run_mixed(mctx, args.mixed_jobs, args.warmup, iteration_work=args.iteration_work, peaks=peaks)
+        batched["budget_bytes"] = 120 * 10**9
+        mctx.close()
+
+    ref_cl = None
+    if rank == 0 and not args.no_reference_opencl:
+        ref_cl = reference_opencl(wl, lo, hi)
+        if e2e is not None and "checksum" in ref_cl:
+            ref_cl["same_checksum_and_factor_count"] = (ref_cl["checksum"] == e2e["checksum"]
+                                                        and ref_cl["factors"] == e2e["factors"])
+            ref_cl["our_e2e_over_reference_e2e"] = e2e["value"] / ref_cl["e2e_pairs_per_s"]
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
+        kind = cpu_kind()
         n = args.cpu_sample or auto_sample(wl)
-        rate, info = cpu_sample_run(wl, n)
-        cpu = {"value": rate, "unit": UNIT, "cores": info["cores"], "kind": "port",
-               "sample": "%d candidates from the bottom of the p range x all %d n (%.1f s)"
-                         % (info["cands"], wl["nmax"] - wl["nmin"], info["seconds"])}
-    ctx.close()
+        rate, info = cpu_sample_run(wl, n, kind=kind)
+        cpu = {"value": rate, "unit": UNIT, "cores": info["cores"], "kind": kind,
+               "sample": "%d candidates from the bottom of the p range x all %d n (%.1f s); %s"
+                         % (info["cands"], wl["nmax"] - wl["nmin"], info["seconds"], CPU_KIND_TEXT[kind])}
 
     if rank == 0:
         line = {
@@ -640,6 +772,8 @@ def run_ours(args, wl, world, rank, local, dist):
         }
         if batched is not None:
             line["batched"] = batched
+        if ref_cl is not None:
+            line["reference_opencl"] = ref_cl
         print(json.dumps(line), flush=True)
 
 
@@ -648,7 +782,9 @@ def main():
     wl = WORKLOADS[args.workload]
     world, rank, local = dist_env()
     dist = dist_init(world)
-    if args.impl == "reference":
+    if args.impl == "reference-opencl":
+        run_reference_opencl_line(args, wl, rank)
+    elif args.impl == "reference":
         if args.workload == "mixed":
             run_reference_mixed(args, rank)
         else:
