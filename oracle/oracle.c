@@ -10,8 +10,10 @@
  * the faster algorithms used on the GPU.
  *
  * Parity pins: the reference's self-test triples (cl_sieve.cpp:1787-2080),
- * see tests/test_oracle_golden.py, and the reference kernels themselves
- * compiled for the CPU (oracle/ref_kernels.cpp -> oracle/_ref).
+ * see tests/test_oracle.py; the reference kernels themselves compiled for the
+ * CPU (oracle/ref_kernels.cpp -> oracle/_ref); and the factors.txt files the
+ * reference's own OpenCL program wrote for two benchmark searches
+ * (tests/test_gpu_configs.py).
  */
 #include "oracle.h"
 

@@ -607,7 +607,9 @@ static int device_from_init_data() {
     fclose(f);
     buf[n] = 0;
     const char *k = strstr(buf, "<gpu_device_num>");
-    return k ? atoi(k + strlen("<gpu_device_num>")) : 0;
+    const int dev = k ? atoi(k + strlen("<gpu_device_num>")) : 0;
+    printf("init_data.xml found, using device %d.\n", dev);
+    return dev;
 }
 
 int main(int argc, char **argv) {

@@ -126,3 +126,21 @@ def test_bad_checkpoint_is_ignored(tmp_path, kind, msg):
     # fell back to a fresh start: the results file was truncated, then the GPU was needed
     assert (tmp_path / "factors.txt").read_text() == ""
     assert rc != 0 and "no usable CUDA device" in out + err
+
+
+@pytest.mark.parametrize("xml,dev", [
+    (None, 0),
+    ("<app_init_data>\n<gpu_device_num>5</gpu_device_num>\n</app_init_data>\n", 5),
+    ("<app_init_data>\n<gpu_type>NVIDIA</gpu_type>\n</app_init_data>\n", 0),
+])
+def test_init_data_selects_the_device(tmp_path, xml, dev):
+    """A BOINC client names the GPU in init_data.xml (<gpu_device_num>,
+    main.cpp:252-274); without the file, or without the tag, device 0 is
+    used.  The choice is printed before the GPU is touched."""
+    if xml is not None:
+        (tmp_path / "init_data.xml").write_text(xml)
+    rc, out, err = run(["-!", "-n", "101", "-N", "110", "-p", "1000", "-P", "1100"], tmp_path)
+    if xml is None:
+        assert "init_data.xml not found, using device 0." in out
+    else:
+        assert "init_data.xml found, using device %d." % dev in out
