@@ -238,6 +238,13 @@ def cpu_kind():
 REF_HIT_CAP = 1 << 24
 
 
+def ref_nstep(ncand):
+    """n per iterate launch of the reference kernels on the CPU: the kernels
+    append hits without a bound, so a launch may cover at most
+    REF_HIT_CAP / (2 x candidates) n (two hits per candidate and n at most)."""
+    return int(max(1, min(20000, REF_HIT_CAP // (2 * max(ncand, 1)))))
+
+
 def cpu_sample_run(wl, ncands, offset=0, kind="port"):
     """Time the reference's CPU path on `ncands` candidates of the workload's
     p range with all host threads: kind 'reference' runs the reference's own
@@ -252,8 +259,7 @@ def cpu_sample_run(wl, ncands, offset=0, kind="port"):
     t0 = time.perf_counter()
     if kind == "reference":
         # iterate chunks sized so that the kernels' unbounded hit appends fit
-        nstep = int(max(64, min(20000, REF_HIT_CAP // (2 * max(len(cands), 1)))))
-        o.ref_segment(wl["mode"], wl["nmin"], wl["nmax"], cands, nstep=nstep, hit_cap=REF_HIT_CAP)
+        o.ref_segment(wl["mode"], wl["nmin"], wl["nmax"], cands, nstep=ref_nstep(len(cands)), hit_cap=REF_HIT_CAP)
     else:
         o.sieve(wl["mode"], wl["nmin"], wl["nmax"], cands, threads)
     dt = time.perf_counter() - t0
@@ -407,8 +413,7 @@ def run_reference_mixed(args, rank):
         cands = o.candidates(s.pmin, min(s.pmin + span, s.pmax))[:m]
         t = time.perf_counter()
         if kind == "reference":
-            nstep = int(max(64, min(20000, REF_HIT_CAP // (2 * max(len(cands), 1)))))
-            o.ref_segment(s.mode, s.nmin, s.nmax, cands, nstep=nstep, hit_cap=REF_HIT_CAP)
+            o.ref_segment(s.mode, s.nmin, s.nmax, cands, nstep=ref_nstep(len(cands)), hit_cap=REF_HIT_CAP)
         else:
             o.sieve(s.mode, s.nmin, s.nmax, cands, threads)
         dt = time.perf_counter() - t

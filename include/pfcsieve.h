@@ -66,9 +66,15 @@ typedef struct pfc_job pfc_job;
 /* ----------------------------------------------------------------- context */
 
 /* Select `device`, create the context's stream and its device buffers.
- * `mem_budget` caps the device memory the context may hold (0 = 90% of free
- * memory).  Replaces the OpenCL platform/context/queue set-up of main.cpp:
- * 245-297 and the buffer creation of cl_sieve.cpp:1339-1350,1508-1519. */
+ * `mem_budget` caps the device memory the context's jobs and batches may hold
+ * at once (0 = 90% of free memory).  Buffers come from a memory pool of the
+ * context, allocated and freed in order on its stream: a freed buffer stays
+ * in the pool for the next job (no cudaMalloc, and none of the device-wide
+ * synchronisation of cudaFree, per search); the pool gives its idle memory
+ * back to the device when an allocation would not fit, and all of it when
+ * the context is destroyed.  Replaces the OpenCL platform/context/queue
+ * set-up of main.cpp:245-297 and the buffer creation of
+ * cl_sieve.cpp:1339-1350,1508-1519. */
 int pfc_ctx_create(int device, uint64_t mem_budget, pfc_ctx **out);
 
 /* Free everything the context owns (cleanup(), cl_sieve.cpp:77-103). */

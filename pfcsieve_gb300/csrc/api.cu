@@ -122,12 +122,24 @@ extern "C" int pfc_ctx_create(int device, uint64_t mem_budget, pfc_ctx **out) {
     const char *g = getenv("PFCSIEVE_CUDA_GRAPHS");
     c->graphs = !(g && g[0] == '0');
     cudaError_t e = cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking);
+    if (e == cudaSuccess) {
+        cudaMemPoolProps props = {};
+        props.allocType = cudaMemAllocationTypePinned;
+        props.location.type = cudaMemLocationTypeDevice;
+        props.location.id = device;
+        e = cudaMemPoolCreate(&c->pool, &props);
+    }
+    if (e == cudaSuccess) {
+        uint64_t keep = ~0ull;   // keep freed blocks between jobs
+        e = cudaMemPoolSetAttribute(c->pool, cudaMemPoolAttrReleaseThreshold, &keep);
+    }
     if (e == cudaSuccess) e = dalloc_bytes(c, (void **)&c->d_pat, kPatEntries * sizeof(uint64_t));
     if (e == cudaSuccess) {
         std::vector<uint64_t> pat(kPatEntries);
         uint32_t pr[kSmallPrimes];
         build_pattern_table(pat.data(), pr);
-        e = cudaMemcpy(c->d_pat, pat.data(), pat.size() * sizeof(uint64_t), cudaMemcpyHostToDevice);
+        e = cudaMemcpyAsync(c->d_pat, pat.data(), pat.size() * sizeof(uint64_t), cudaMemcpyHostToDevice, c->st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(c->st);
     }
     if (e != cudaSuccess) {
         pfc_ctx_destroy(c);
@@ -140,9 +152,13 @@ extern "C" int pfc_ctx_create(int device, uint64_t mem_budget, pfc_ctx **out) {
 extern "C" int pfc_ctx_destroy(pfc_ctx *c) {
     if (!c) return PFC_ERR_ARG;
     cudaSetDevice(c->device);
-    if (c->st) cudaStreamSynchronize(c->st);
-    if (c->d_pat) cudaFree(c->d_pat);
-    if (c->vbits) cudaFree(c->vbits);
+    if (c->st) {
+        dfree_bytes(c, c->d_pat, kPatEntries * sizeof(uint64_t));
+        dfree_bytes(c, c->vbits, c->vbits_bytes);
+        cudaStreamSynchronize(c->st);
+    }
+    if (c->pool) cudaMemPoolDestroy(c->pool);
+    for (void *h : c->pinned_stats) cudaFreeHost(h);
     if (c->st) cudaStreamDestroy(c->st);
     delete c;
     return PFC_OK;
@@ -188,7 +204,7 @@ static int job_release(pfc_job *j) {
     j->c64.release(c);
     j->hits.release(c);
     j->stats.release(c);
-    if (j->h_stats) cudaFreeHost(j->h_stats);
+    if (j->h_stats) c->pinned_stats.push_back(j->h_stats);   // kept for the next job
     j->h_stats = nullptr;
     return PFC_OK;
 }
@@ -288,7 +304,14 @@ extern "C" int pfc_job_create(pfc_ctx *c, unsigned mode, uint32_t nmin, uint32_t
     }
     if (e == cudaSuccess) e = j->stats.alloc(c, 1);
     if (e == cudaSuccess) e = cudaMemsetAsync(j->stats.p, 0, sizeof(SegStats), c->st);
-    if (e == cudaSuccess) e = cudaMallocHost((void **)&j->h_stats, sizeof(SegStats));
+    if (e == cudaSuccess) {
+        if (!c->pinned_stats.empty()) {
+            j->h_stats = static_cast<SegStats *>(c->pinned_stats.back());
+            c->pinned_stats.pop_back();
+        } else {
+            e = cudaMallocHost((void **)&j->h_stats, sizeof(SegStats));
+        }
+    }
     if (e == cudaSuccess) e = j->hits.alloc(c, 1u << 20);
     if (e == cudaSuccess) e = cudaStreamSynchronize(c->st);
     if (e != cudaSuccess) {

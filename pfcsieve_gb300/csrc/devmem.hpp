@@ -14,6 +14,13 @@
 struct pfc_ctx {
     int device = 0;
     cudaStream_t st = nullptr;
+    // the context's buffers come from its own stream-ordered pool, allocated
+    // and freed on `st`: freed blocks stay in the pool for the next job, so a
+    // search does not pay for cudaMalloc and the device-wide synchronisation
+    // of cudaFree each time (the pool is trimmed only when an allocation
+    // would not fit, and released when the context is destroyed)
+    cudaMemPool_t pool = nullptr;
+    std::vector<void *> pinned_stats;   // spare pinned blocks for the jobs' segment stats
     int sms = 0;
     char name[256] = {0};
     uint64_t budget = 0, used = 0;
@@ -31,13 +38,32 @@ struct pfc_ctx {
 
 namespace pfc {
 
+// A buffer of the context's pool, ordered on the context stream (work on
+// other streams must wait for that stream before using it; every caller
+// synchronises it first).  Counted against the memory budget while held.
 inline cudaError_t dalloc_bytes(pfc_ctx *c, void **p, size_t bytes) {
     *p = nullptr;
     if (bytes == 0) return cudaSuccess;
     if (c->used + bytes > c->budget) return cudaErrorMemoryAllocation;
-    cudaError_t e = cudaMalloc(p, bytes);
+    cudaError_t e = cudaMallocFromPoolAsync(p, bytes, c->pool, c->st);
+    if (e == cudaErrorMemoryAllocation) {
+        // give the pool's idle blocks back to the device and try once more
+        cudaGetLastError();
+        e = cudaStreamSynchronize(c->st);
+        if (e == cudaSuccess) e = cudaMemPoolTrimTo(c->pool, 0);
+        if (e == cudaSuccess) e = cudaMallocFromPoolAsync(p, bytes, c->pool, c->st);
+    }
     if (e == cudaSuccess) c->used += bytes;
     return e;
+}
+
+// Back to the pool after the work enqueued so far on the context stream.
+// Buffers that other streams use are freed only when those streams are idle
+// (the batch frees a search's buffers after its iteration has finished).
+inline void dfree_bytes(pfc_ctx *c, void *p, size_t bytes) {
+    if (!p) return;
+    cudaFreeAsync(p, c->st);
+    c->used -= bytes;
 }
 
 template <class T>
@@ -58,10 +84,7 @@ struct DArr {
         return cudaMemcpyAsync(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, c->st);
     }
     void release(pfc_ctx *c) {
-        if (p) {
-            cudaFree(p);
-            c->used -= n * sizeof(T);
-        }
+        dfree_bytes(c, p, n * sizeof(T));
         p = nullptr;
         n = 0;
     }

@@ -5,6 +5,8 @@
 // One thread owns one candidate prime p (two in class-32 single-chain walks)
 // for a launch; its residues live in registers between the loads at launch
 // start and the stores at launch end.
+#include <type_traits>
+
 #include "walk.cuh"
 
 namespace pfc {
@@ -152,30 +154,32 @@ int launch_setup64w(const ClassBuf<uint64_t> &c, const SetupArgs<WideWord> &a, c
 }
 
 // Walk variants (candidates per thread, block length) per size class and walk
-// kind; entry 0 is the default, pfc_autotune measures the others.
+// kind; entry 0 is the default, pfc_autotune measures the others.  Register
+// bounds for four CTAs of 256 per SM (64 registers) were measured and dropped:
+// the fused class-32 walk ran 1.3% slower, the two-candidate one 23% slower.
+// Blocks of 32 are the lazy class-64 default: 77.0 ms against 80.0 ms for
+// blocks of 16 on the primorial search near 2^62 (1.16e6 candidates x 78,473
+// prime n); two candidates per thread there took 81.5 ms.
 struct WalkVariant {
     int nc, b;
 };
 static const WalkVariant kVar32[] = {{2, 16}, {2, 8}, {1, 16}};
 static const WalkVariant kVar32F[] = {{1, 16}, {1, 8}};
-static const WalkVariant kVar64L[] = {{1, 16}, {1, 8}};
+static const WalkVariant kVar64L[] = {{1, 32}, {1, 16}, {1, 8}, {2, 16}};
 static const WalkVariant kVar64LF[] = {{1, 16}, {1, 8}};
 static const WalkVariant kVar64[] = {{1, 8}};
 static const WalkVariant kVar64F[] = {{1, 8}};
 
-static const WalkVariant *variants(int cls, bool fused, int *n) {
-    const WalkVariant *v;
-    if (cls == 0) {
-        v = fused ? kVar32F : kVar32;
-        *n = fused ? 2 : 3;
-    } else if (cls == 1) {
-        v = fused ? kVar64LF : kVar64L;
-        *n = 2;
-    } else {
-        v = fused ? kVar64F : kVar64;
-        *n = 1;
-    }
+template <size_t N>
+static const WalkVariant *table(const WalkVariant (&v)[N], int *n) {
+    *n = (int)N;
     return v;
+}
+
+static const WalkVariant *variants(int cls, bool fused, int *n) {
+    if (cls == 0) return fused ? table(kVar32F, n) : table(kVar32, n);
+    if (cls == 1) return fused ? table(kVar64LF, n) : table(kVar64L, n);
+    return fused ? table(kVar64F, n) : table(kVar64, n);
 }
 
 int walk_variant_count(int cls, bool fused) {
@@ -193,13 +197,45 @@ int walk_variant_shape(int cls, bool fused, int variant, int *nc, int *b) {
     return 0;
 }
 
+// SM count of the current device (cached per device)
+static int device_sms() {
+    static int cached[64] = {0};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 152;
+    if (!cached[dev]) {
+        int n = 0;
+        if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0) n = 152;
+        cached[dev] = n;
+    }
+    return cached[dev];
+}
+
+// Candidate sets too small to give every SM several CTAs of 256 threads
+// (about three are resident per SM at the walks' register counts) leave SMs
+// idle or unevenly loaded; their walks run in CTAs of 128 threads, sized from
+// the class capacity (an upper estimate of the count).  Measured on GB300 for
+// 61,945 candidates x 19,899 n, two candidates per thread: 0.745 ms in CTAs of
+// 128 (64 and 32 the same), 0.772 ms in CTAs of 256; one candidate per thread
+// was slower at every CTA size (0.82-0.87 ms): with so few chains per SM the
+// walk is latency-bound and two chains per thread hide more of it than more
+// warps do.
+constexpr uint32_t kWalkFullCtas = 3;
+
+static bool walk_small(uint32_t cap, int nc, int sms) {
+    return (uint64_t)cap < (uint64_t)sms * kWalkFullCtas * 256u * (uint32_t)nc;
+}
+
+static unsigned walk_cta_threads(uint32_t cap, int nc, int sms) { return walk_small(cap, nc, sms) ? 128 : 256; }
+
 template <class T, int NC, bool FUSED, int B>
 static int launch_one(const ClassBuf<typename T::W> &c, const WalkArgs &a, const HitBuf &h, cudaStream_t st) {
-    const uint32_t per_block = 256u * NC;
-    walk_kernel<T, NC, FUSED, B><<<(c.cap + per_block - 1) / per_block, 256, 0, st>>>(c, a, h);
+    const unsigned threads = walk_cta_threads(c.cap, NC, device_sms());
+    const uint32_t per_block = threads * NC;
+    walk_kernel<T, NC, FUSED, B><<<(c.cap + per_block - 1) / per_block, threads, 0, st>>>(c, a, h);
     return 1;
 }
 
+// the compiled shapes of each class (others fall back to the default)
 template <class T>
 static int launch_walk(const ClassBuf<typename T::W> &c, const WalkArgs &a, const HitBuf &h, cudaStream_t st,
                        int cls, int variant) {
@@ -211,12 +247,17 @@ static int launch_walk(const ClassBuf<typename T::W> &c, const WalkArgs &a, cons
         if (v.b == 8) return launch_one<T, 1, true, 8>(c, a, h, st);
         return launch_one<T, 1, true, 16>(c, a, h, st);
     }
-    if constexpr (T::NC == 2) {
-        if (v.nc == 2 && v.b == 8) return launch_one<T, 2, false, 8>(c, a, h, st);
-        if (v.nc == 1) return launch_one<T, 1, false, 16>(c, a, h, st);
-        return launch_one<T, 2, false, 16>(c, a, h, st);
+    const bool two = v.nc == 2;
+    if constexpr (std::is_same<T, Cls32>::value) {
+        if (two && v.b == 8) return launch_one<T, 2, false, 8>(c, a, h, st);
+        if (two) return launch_one<T, 2, false, 16>(c, a, h, st);
+        return launch_one<T, 1, false, 16>(c, a, h, st);
+    } else if constexpr (std::is_same<T, Cls64L>::value) {
+        if (two) return launch_one<T, 2, false, 16>(c, a, h, st);
+        if (v.b == 32) return launch_one<T, 1, false, 32>(c, a, h, st);
+        if (v.b == 8) return launch_one<T, 1, false, 8>(c, a, h, st);
+        return launch_one<T, 1, false, 16>(c, a, h, st);
     } else {
-        if (v.b == 16) return launch_one<T, 1, false, 16>(c, a, h, st);
         return launch_one<T, 1, false, 8>(c, a, h, st);
     }
 }

@@ -259,19 +259,17 @@ extern "C" int pfc_verify_factors_device(pfc_ctx *c, unsigned mode, uint32_t nma
         std::vector<uint32_t> bits(want / 32 + 1, 0u);
         for (uint32_t q : primes_between(2, want)) bits[q >> 5] |= 1u << (q & 31);
         if (c->vbits) {
-            CK(cudaStreamSynchronize(c->st));
-            cudaFree(c->vbits);
-            c->used -= c->vbits_bytes;
+            dfree_bytes(c, c->vbits, c->vbits_bytes);
             c->vbits = nullptr;
             c->vbits_top = 0;
             c->vbits_bytes = 0;
         }
         void *vb = nullptr;
         CK(dalloc_bytes(c, &vb, bits.size() * 4));
-        cudaError_t e = cudaMemcpy(vb, bits.data(), bits.size() * 4, cudaMemcpyHostToDevice);
+        cudaError_t e = cudaMemcpyAsync(vb, bits.data(), bits.size() * 4, cudaMemcpyHostToDevice, c->st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(c->st);   // `bits` is freed on return
         if (e != cudaSuccess) {
-            cudaFree(vb);
-            c->used -= bits.size() * 4;
+            dfree_bytes(c, vb, bits.size() * 4);
             CK(e);
         }
         c->h2d += bits.size() * 4;

@@ -249,11 +249,14 @@ def test_autotune_reports_and_picks_one_variant_per_kind():
     with pfc.Context(0) as c:
         rep = c.autotune()
         lines = [x for x in rep.splitlines() if x]
-        assert len(lines) == 3 + 2 + 2 + 2
+        # class 32 single (3 variants) and fused (2), lazy class 64 single (4) and fused (2)
+        assert len(lines) == 3 + 2 + 4 + 2
         for kind in ("class32 single", "class32 fused", "class64-lazy single", "class64-lazy fused"):
             assert sum(1 for x in lines if x.startswith(kind) and x.endswith("*")) == 1
         v, nc, b = c.walk_variant(0, 0)
         assert (nc, b) in ((2, 16), (2, 8), (1, 16))
+        v, nc, b = c.walk_variant(1, 0)
+        assert (nc, b) in ((1, 32), (1, 16), (1, 8), (2, 16))
 
 
 @pytest.mark.parametrize("mode", [1, 2, 4, 5])
