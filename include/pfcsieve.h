@@ -93,6 +93,20 @@ void *pfc_ctx_stream(pfc_ctx *ctx);
  * stream.  Results are identical. */
 int pfc_ctx_set_graphs(pfc_ctx *ctx, int on);
 
+/* Split walks.  A segment whose candidates are too few to fill the GPU (a
+ * walk of dependent multiplications per candidate leaves most SMs waiting on
+ * latency) and whose whole n range fits one walk launch has that range cut
+ * into up to 8 sub-ranges: the residue at each boundary b comes from a setup
+ * program for (b-1)! (or (b-1)!/(b-1)#, or the primorial below the boundary's
+ * prime), and one launch walks every (candidate, sub-range) pair.  Used only
+ * when those programs cost under a sixth of the walk (a small nmin), in
+ * pfc_segment and in a pfc_iterate call over the whole range.  No
+ * counterpart in the reference, which walks each prime's n range in order
+ * (kernels/iterate.cl:59-198).  On by default; off (`on` = 0, or
+ * PFCSIEVE_SPLIT=0 in the environment when the context is created) walks
+ * every candidate in one chain.  Results are identical. */
+int pfc_ctx_set_split(pfc_ctx *ctx, int on);
+
 /* Number of kernels this context has launched so far. */
 uint64_t pfc_ctx_launch_count(pfc_ctx *ctx);
 

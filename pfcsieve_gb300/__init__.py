@@ -120,6 +120,7 @@ def lib():
             "pfc_batch_set_hit_capacity": (ctypes.c_int, [vp, u32]),
             "pfc_autotune": (ctypes.c_int, [vp, ctypes.c_char_p, sz]),
             "pfc_ctx_set_graphs": (ctypes.c_int, [vp, ctypes.c_int]),
+            "pfc_ctx_set_split": (ctypes.c_int, [vp, ctypes.c_int]),
             "pfc_ctx_set_walk_variant": (ctypes.c_int, [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int]),
             "pfc_ctx_walk_variant": (ctypes.c_int, [vp, ctypes.c_int, ctypes.c_int, P(ctypes.c_int),
                                                     P(ctypes.c_int), P(ctypes.c_int)]),
@@ -191,6 +192,10 @@ class Context:
     def set_graphs(self, on):
         """Replay each job's segment body as a CUDA graph (default on)."""
         _ck(lib().pfc_ctx_set_graphs(self.h, int(bool(on))), "pfc_ctx_set_graphs")
+
+    def set_split(self, on):
+        """Walk small candidate sets in n sub-ranges (default on)."""
+        _ck(lib().pfc_ctx_set_split(self.h, int(bool(on))), "pfc_ctx_set_split")
 
     def set_walk_variant(self, cls, fused, variant):
         _ck(lib().pfc_ctx_set_walk_variant(self.h, cls, int(fused), variant), "pfc_ctx_set_walk_variant")

@@ -60,12 +60,26 @@ struct pfc_job {
     bool use32 = false, use64 = false;   // size classes the segment can hold
     uint64_t pairs = 0;
 
+    // split walk of the current segment (kernels.cuh SplitArgs): sub-ranges,
+    // their boundaries, the setup programs of the starts (boundaries 1..n-1;
+    // 896-bit words for class 32 and the lazy class 64, 64-bit words above
+    // 2^64/3) and the start residues per class ((n-1) blocks of s0, then
+    // (n-1) of s1, one class capacity each)
+    uint32_t split_n = 1;
+    uint32_t split_start[kMaxSplit + 1] = {0};
+    bool split_wide = false, split_narrow = false;
+    std::vector<DevProg<WideWord>> split_wa, split_wb;
+    std::vector<DevProg<uint64_t>> split_na, split_nb;
+    DArr<uint32_t> split32;
+    DArr<uint64_t> split64;
+
     // the post-generation part of a segment captured as a CUDA graph, replayed
     // while the key (buffers, launch shapes, kernel choices) is unchanged
     struct GraphKey {
-        const void *p32, *p64, *hits, *cmult, *ramp;
+        const void *p32, *p64, *hits, *cmult, *ramp, *split32, *split64;
         uint64_t cap32, cap64, hitcap;
         int lazy, use32, use64, var[3][2];
+        uint32_t split_n, split_start[kMaxSplit + 1];
     };
     cudaGraphExec_t graph = nullptr;
     GraphKey gkey{};
@@ -121,6 +135,8 @@ extern "C" int pfc_ctx_create(int device, uint64_t mem_budget, pfc_ctx **out) {
     c->budget = mem_budget ? mem_budget : (uint64_t)(0.9 * (double)fr);
     const char *g = getenv("PFCSIEVE_CUDA_GRAPHS");
     c->graphs = !(g && g[0] == '0');
+    const char *sp = getenv("PFCSIEVE_SPLIT");
+    c->split = !(sp && sp[0] == '0');
     cudaError_t e = cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking);
     if (e == cudaSuccess) {
         cudaMemPoolProps props = {};
@@ -204,6 +220,12 @@ static int job_release(pfc_job *j) {
     j->c64.release(c);
     j->hits.release(c);
     j->stats.release(c);
+    for (auto &pg : j->split_wa) pg.release(c);
+    for (auto &pg : j->split_wb) pg.release(c);
+    for (auto &pg : j->split_na) pg.release(c);
+    for (auto &pg : j->split_nb) pg.release(c);
+    j->split32.release(c);
+    j->split64.release(c);
     if (j->h_stats) c->pinned_stats.push_back(j->h_stats);   // kept for the next job
     j->h_stats = nullptr;
     return PFC_OK;
@@ -442,16 +464,30 @@ static HitBuf hitbuf(pfc_job *j) {
 // the walks of one chunk [lo, hi) (n values, or prime indices for n#):
 // factorial over n, compositorial over its multiplier table, primorial over
 // the prime list; each for both size classes
-static int enqueue_iter_range(pfc_job *j, uint32_t lo, uint32_t hi) {
+static int enqueue_iter_range(pfc_job *j, uint32_t lo, uint32_t hi, bool split = false) {
     pfc_ctx *c = j->ctx;
     const HitBuf h = hitbuf(j);
+    SplitArgs<uint32_t> sp32{};
+    SplitArgs<uint64_t> sp64{};
+    if (split) {
+        sp32.n = sp64.n = j->split_n;
+        for (uint32_t k = 0; k <= j->split_n; ++k) sp32.start[k] = sp64.start[k] = j->split_start[k];
+        sp32.pitch = j->c32.cap;
+        sp32.s0 = j->split32.p;
+        sp32.s1 = j->split32.p ? j->split32.p + (size_t)(j->split_n - 1) * j->c32.cap : nullptr;
+        sp64.pitch = j->c64.cap;
+        sp64.s0 = j->split64.p;
+        sp64.s1 = j->split64.p ? j->split64.p + (size_t)(j->split_n - 1) * j->c64.cap : nullptr;
+    }
     auto walk = [&](const WalkArgs &w) {
         const int fused = w.mult2 != nullptr;
         const bool lazy = j->seg_hi <= kLazyWalkEnd;
-        if (j->use32) c->launches += launch_walk32(j->c32.view(counts_ptr(j)), w, h, c->st, c->walk_var[0][fused]);
+        if (j->use32)
+            c->launches += launch_walk32(j->c32.view(counts_ptr(j)), w, h, c->st, c->walk_var[0][fused],
+                                         split ? &sp32 : nullptr);
         if (j->use64)
             c->launches += launch_walk64(j->c64.view(counts_ptr(j) + 1), w, h, c->st, lazy,
-                                         c->walk_var[lazy ? 1 : 2][fused]);
+                                         c->walk_var[lazy ? 1 : 2][fused], split ? &sp64 : nullptr);
     };
     WalkArgs w;
     w.lo = lo;
@@ -504,9 +540,164 @@ static uint32_t chunk_len(uint64_t count, double budget) {
     return ((uint32_t)L + 15u) & ~15u;
 }
 
+// ------------------------------------------------------------ split walks
+//
+// A segment with few candidates leaves most of the GPU idle in its walk: each
+// candidate's chain is a sequence of dependent multiplications, and a few
+// chains per SM cannot hide their latency (61,945 candidates x 19,899 n ran at
+// 10% warp occupancy, latency-bound).  When the whole walk fits one launch,
+// the n range [lo, hi) is cut into S sub-ranges; the residue at each
+// boundary b comes from a setup program for (b-1)! (or (b-1)!/(b-1)#, or the
+// primorial of the primes below the boundary's prime), evaluated by the setup
+// kernel, and one launch walks every (candidate, sub-range) pair.  S fills
+// about two waves of resident CTAs; boundaries whose programs would cost more
+// than a sixth of the walk (large nmin) disable the split.  Results are the
+// same as the plain walk's: every n is tested once, hits carry their own n,
+// the last sub-range leaves the final residue and nnext counts every step.
+
+constexpr uint32_t kMinSplitLen = 2048;   // shortest sub-range worth a setup program
+
+template <class W>
+static uint64_t prog_cost(const HostProg<W> &a, const HostProg<W> &b) {
+    // in walk steps: an 896-bit word costs about 15 class-32 steps of multiply
+    // pipe, a 64-bit word about 2; squarings about one
+    const uint64_t wc = sizeof(W) > 8 ? 15 : 2;
+    const uint64_t words = a.words.size() + b.words.size();
+    return words * wc + (a.mulmods() + b.mulmods() - words);
+}
+
+// Plan (and prepare) the split for a walk over the whole range of the current
+// segment: j->split_n = 1 when the walk stays plain.  Host tables are built
+// and uploaded here, before any graph capture.
+static int split_prepare(pfc_job *j) {
+    pfc_ctx *c = j->ctx;
+    j->split_n = 1;
+    const uint32_t lo = iter_begin(j), hi = iter_end(j), len = hi - lo;
+    const uint64_t n32 = (j->use32 && j->c32.p.p) ? j->c32.cap : 0;
+    const uint64_t n64 = (j->use64 && j->c64.p.p) ? j->c64.cap : 0;
+    const uint32_t L = std::min(chunk_len(n32 + 3 * n64, 1.5e11), kMaxChunk);
+    if (!c->split || len > L || n32 + n64 == 0) return PFC_OK;
+    const bool fused = j->mode == (PFC_FACTORIAL | PFC_COMPOSITORIAL);
+    const uint64_t chains = (n32 + n64) * (fused ? 2 : 1);
+    const uint64_t target = (uint64_t)c->sms * 3 * 256 * 2 * 2;   // two waves of CTAs, two chains a thread
+    uint32_t S = (uint32_t)std::min<uint64_t>({(uint64_t)kMaxSplit, target / chains, len / kMinSplitLen});
+    if (S < 2) return PFC_OK;
+    const bool lazy = j->seg_hi <= kLazyEnd;
+    const bool wide = n32 > 0 || (n64 > 0 && lazy), narrow = n64 > 0 && !lazy;
+    const uint64_t walk = (uint64_t)len * (fused ? 2 : 1);
+
+    // a lower bound on a boundary's program cost, before anything is built:
+    // every program multiplies at least the primes up to (b-1)/2, whose
+    // product has theta(x)/ln 2 > x (1 - 1/ln x)/ln 2 bits (x >= 41, Rosser
+    // and Schoenfeld), 896 bits a word
+    auto cost_floor = [](uint32_t b) {
+        const double x = b / 2.0;
+        return x < 41 ? 0.0 : x * (1.0 - 1.0 / std::log(x)) / std::log(2.0) / 896.0 * 15.0;
+    };
+    for (; S >= 2; --S) {
+        uint32_t start[kMaxSplit + 1];
+        const uint32_t step = ((len / S) + 15u) & ~15u;
+        for (uint32_t k = 0; k < S; ++k) start[k] = lo + k * step;
+        start[S] = hi;
+        if (start[S - 1] >= hi) continue;
+        double floor_cost = 0;
+        for (uint32_t k = 1; k < S; ++k)
+            floor_cost += cost_floor(j->mode == PFC_PRIMORIAL ? j->h_qlist[start[k]] : start[k]);
+        if (floor_cost * 6 > (double)walk) continue;
+        const bool same = j->split_wide == wide && j->split_narrow == narrow &&
+                          j->split_wa.size() + j->split_na.size() > 0 &&
+                          std::max(j->split_wa.size(), j->split_na.size()) == S - 1 &&
+                          memcmp(start, j->split_start, sizeof(uint32_t) * (S + 1)) == 0;
+        if (!same) {
+            // the value before each boundary's first multiplier
+            std::vector<uint32_t> startN(S);
+            for (uint32_t k = 1; k < S; ++k)
+                startN[k] = (j->mode == PFC_PRIMORIAL ? j->h_qlist[start[k]] : start[k]) - 1;
+            const std::vector<uint32_t> primes = primes_between(2, startN[S - 1]);
+            std::vector<HostProg<WideWord>> wa(S), wb(S);
+            std::vector<HostProg<uint64_t>> na(S), nb(S);
+            uint64_t cost = 0;
+            for (uint32_t k = 1; k < S; ++k) {
+                const std::vector<uint32_t> below(primes.begin(),
+                                                  std::upper_bound(primes.begin(), primes.end(), startN[k]));
+                if (wide && !build_progs(j->mode, startN[k], primes, below, wa[k], wb[k])) return PFC_ERR_ARG;
+                if (narrow && !build_progs(j->mode, startN[k], primes, below, na[k], nb[k])) return PFC_ERR_ARG;
+                cost += wide ? prog_cost(wa[k], wb[k]) : prog_cost(na[k], nb[k]);
+            }
+            if (cost * 6 > walk) continue;   // boundaries too dear: fewer sub-ranges or none
+            for (auto &pg : j->split_wa) pg.release(c);
+            for (auto &pg : j->split_wb) pg.release(c);
+            for (auto &pg : j->split_na) pg.release(c);
+            for (auto &pg : j->split_nb) pg.release(c);
+            j->split_wa.assign(wide ? S - 1 : 0, DevProg<WideWord>());
+            j->split_wb.assign(wide ? S - 1 : 0, DevProg<WideWord>());
+            j->split_na.assign(narrow ? S - 1 : 0, DevProg<uint64_t>());
+            j->split_nb.assign(narrow ? S - 1 : 0, DevProg<uint64_t>());
+            for (uint32_t k = 1; k < S; ++k) {
+                if (wide) {
+                    CK(j->split_wa[k - 1].upload(c, wa[k]));
+                    CK(j->split_wb[k - 1].upload(c, wb[k]));
+                }
+                if (narrow) {
+                    CK(j->split_na[k - 1].upload(c, na[k]));
+                    CK(j->split_nb[k - 1].upload(c, nb[k]));
+                }
+            }
+            j->split_wide = wide;
+            j->split_narrow = narrow;
+            memcpy(j->split_start, start, sizeof(uint32_t) * (S + 1));
+        }
+        // start residues of boundaries 1..S-1 for s0 and s1, per class
+        const size_t need32 = (size_t)2 * (S - 1) * n32, need64 = (size_t)2 * (S - 1) * n64;
+        if (n32 && j->split32.n < need32) CK(j->split32.alloc(c, need32));
+        if (n64 && j->split64.n < need64) CK(j->split64.alloc(c, need64));
+        j->split_n = S;
+        return PFC_OK;
+    }
+    return PFC_OK;
+}
+
+// one setup launch per size class for the start residues of boundaries
+// 1..split_n-1
+static int enqueue_split_setup(pfc_job *j) {
+    pfc_ctx *c = j->ctx;
+    const uint32_t S = j->split_n;
+    const bool lazy = j->seg_hi <= kLazyEnd;
+    SplitSetup<WideWord> sw{};
+    SplitSetup<uint64_t> sn{};
+    sw.mode = sn.mode = j->mode;
+    sw.n = sn.n = S;
+    for (uint32_t k = 1; k < S; ++k) {
+        if (j->split_wide) {
+            sw.a[k - 1] = j->split_wa[k - 1].view;
+            sw.b[k - 1] = j->split_wb[k - 1].view;
+        }
+        if (j->split_narrow) {
+            sn.a[k - 1] = j->split_na[k - 1].view;
+            sn.b[k - 1] = j->split_nb[k - 1].view;
+        }
+    }
+    if (j->use32 && j->c32.p.p)
+        c->launches += launch_split_setup32(j->c32.view(counts_ptr(j)), sw, j->split32.p,
+                                            j->split32.p + (size_t)(S - 1) * j->c32.cap, c->st);
+    if (j->use64 && j->c64.p.p) {
+        uint64_t *s0 = j->split64.p, *s1 = j->split64.p + (size_t)(S - 1) * j->c64.cap;
+        if (lazy) c->launches += launch_split_setup64w(j->c64.view(counts_ptr(j) + 1), sw, s0, s1, c->st);
+        else c->launches += launch_split_setup64(j->c64.view(counts_ptr(j) + 1), sn, s0, s1, c->st);
+    }
+    CK(cudaGetLastError());
+    return PFC_OK;
+}
+
 // [lo, hi) in launches of about 1.5e11 candidate-steps (class-64 steps
-// weigh 3), so no launch runs for more than a fraction of a second
+// weigh 3), so no launch runs for more than a fraction of a second; a walk
+// over the whole range of a segment that split_prepare planned runs split.
 static int enqueue_iter_chunked(pfc_job *j, uint32_t lo, uint32_t hi, uint64_t n32, uint64_t n64) {
+    if (j->split_n > 1 && lo == iter_begin(j) && hi == iter_end(j)) {
+        int rc = enqueue_split_setup(j);
+        if (rc) return rc;
+        return enqueue_iter_range(j, lo, hi, true);
+    }
     const uint32_t L = std::min(chunk_len(n32 + 3 * n64, 1.5e11), kMaxChunk);
     while (lo < hi) {
         const uint32_t e = (uint32_t)std::min<uint64_t>((uint64_t)lo + L, hi);
@@ -530,6 +721,12 @@ extern "C" int pfc_iterate(pfc_job *j, uint32_t n_lo, uint32_t n_hi) {
     }
     if (lo != j->next_it || hi > iter_end(j)) return PFC_ERR_STATE;
     if (hi == lo) return PFC_OK;
+    // one call over the whole range may walk split (split walks)
+    j->split_n = 1;
+    if (lo == iter_begin(j) && hi == iter_end(j)) {
+        const int sr = split_prepare(j);
+        if (sr) return sr;
+    }
     int rc = enqueue_iter_chunked(j, lo, hi, j->c32.cap, j->c64.cap);
     if (rc) return rc;
     j->next_it = hi;
@@ -639,6 +836,10 @@ static int segment_body_graph(pfc_job *j) {
     k.use32 = j->use32;
     k.use64 = j->use64;
     memcpy(k.var, c->walk_var, sizeof(k.var));
+    k.split32 = j->split32.p;
+    k.split64 = j->split64.p;
+    k.split_n = j->split_n;
+    if (j->split_n > 1) memcpy(k.split_start, j->split_start, sizeof(k.split_start));
     if (!j->graph || memcmp(&k, &j->gkey, sizeof(k)) != 0) {
         if (j->graph) cudaGraphExecDestroy(j->graph);
         j->graph = nullptr;
@@ -687,6 +888,8 @@ extern "C" int pfc_segment(pfc_job *j, uint64_t p_lo, uint64_t p_hi) {
         if (over32) CK(j->c32.ensure(c, (uint32_t)std::min<uint64_t>(4000000000ull, n32 + n32 / 8 + 1024)));
         if (over64) CK(j->c64.ensure(c, (uint32_t)std::min<uint64_t>(4000000000ull, n64 + n64 / 8 + 1024)));
     }
+    rc = split_prepare(j);
+    if (rc) return rc;
     const unsigned long long hit_base = j->h_stats->hits;
     for (int attempt = 0;; ++attempt) {
         // a graph pays off from the second segment of a job on: capturing and
@@ -1037,5 +1240,11 @@ extern "C" int pfc_autotune(pfc_ctx *c, char *report, size_t cap) {
 extern "C" int pfc_ctx_set_graphs(pfc_ctx *c, int on) {
     if (!c) return PFC_ERR_ARG;
     c->graphs = on != 0;
+    return PFC_OK;
+}
+
+extern "C" int pfc_ctx_set_split(pfc_ctx *c, int on) {
+    if (!c) return PFC_ERR_ARG;
+    c->split = on != 0;
     return PFC_OK;
 }

@@ -29,6 +29,7 @@ struct pfc_ctx {
     uint64_t *d_pat = nullptr;
     int walk_var[3][2] = {{0, 0}, {0, 0}, {0, 0}};   // walk variant per size class and kind (fused)
     bool graphs = true;   // pfc_segment replays each job's segment body as a CUDA graph
+    bool split = true;    // small candidate sets walk their n range in sub-ranges (split walks)
     // prime flags of [0, vbits_top] kept for pfc_verify_factors_device (one
     // bit per integer), rebuilt only when a call needs a larger range
     uint32_t *vbits = nullptr;

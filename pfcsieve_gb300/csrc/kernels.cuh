@@ -74,6 +74,32 @@ struct WalkArgs {
     int chain;          // single-chain walks: 0 -> residue s0, 1 -> residue s1
 };
 
+// A walk over n split into sub-ranges: candidate i's sub-range k covers steps
+// [start[k], start[k+1]) and begins from the residue at start[k], which the
+// setup kernel computed into s0/s1 + (k-1) * pitch for k >= 1 (sub-range 0
+// begins from the candidate's own state).  One launch walks every (candidate,
+// sub-range) pair (grid y = k); the last sub-range leaves the candidate's
+// final residue in its state and every sub-range adds its steps to nnext.
+// Candidate sets too small to fill the GPU get more chains this way.
+constexpr int kMaxSplit = 8;
+template <class W>
+struct SplitArgs {
+    uint32_t start[kMaxSplit + 1];
+    uint32_t n;        // sub-ranges (1 = no split)
+    uint32_t pitch;    // stride of the start-residue arrays (the class capacity)
+    W *s0, *s1;        // start residues of sub-ranges 1 .. n-1
+};
+
+// the setup programs of a split walk's boundaries 1..n-1 (n <= kMaxSplit),
+// evaluated in one launch (grid y = boundary - 1)
+template <class SW>
+struct SplitSetup {
+    unsigned mode;
+    uint32_t n;
+    Prog<SW> a[kMaxSplit - 1];
+    Prog<SW> b[kMaxSplit - 1];
+};
+
 // size classes: class 32 holds p < 2^31, class 64 the rest
 constexpr uint64_t kClassSplit = 1ull << 31;
 // class-64 segments whose candidates are all below kLazyEnd (3p < 2^64) set
@@ -98,6 +124,7 @@ struct GenArgs {
     uint32_t *count;   // [0] class-32 count, [1] class-64 count (may exceed caps)
     const uint64_t *pat;      // kPatEntries sieve masks (device)
     uint32_t bmod[32];        // base mod each of the 29 small primes
+    uint32_t share;           // threads per 64-bit word of odd numbers (1, 2 or 4; set by launch_gen)
 };
 
 // Launch wrappers (enqueue on `st`); return the number of kernels launched.
@@ -106,12 +133,22 @@ int launch_setup32(const ClassBuf<uint32_t> &c, const SetupArgs<WideWord> &a, cu
 int launch_setup64(const ClassBuf<uint64_t> &c, const SetupArgs<uint64_t> &a, cudaStream_t st);
 // class 64 below 2^64/3 with 896-bit table words
 int launch_setup64w(const ClassBuf<uint64_t> &c, const SetupArgs<WideWord> &a, cudaStream_t st);
+// start residues of a split walk: boundary k's into s0/s1 + (k-1) * c.cap
+int launch_split_setup32(const ClassBuf<uint32_t> &c, const SplitSetup<WideWord> &ss, uint32_t *s0, uint32_t *s1,
+                         cudaStream_t st);
+int launch_split_setup64(const ClassBuf<uint64_t> &c, const SplitSetup<uint64_t> &ss, uint64_t *s0, uint64_t *s1,
+                         cudaStream_t st);
+int launch_split_setup64w(const ClassBuf<uint64_t> &c, const SplitSetup<WideWord> &ss, uint64_t *s0, uint64_t *s1,
+                          cudaStream_t st);
 // walk launches: `variant` indexes the walk variants of the size class
 // (0 = default; see walk_variant_shape)
-int launch_walk32(const ClassBuf<uint32_t> &c, const WalkArgs &a, const HitBuf &h, cudaStream_t st, int variant);
+// (sp: a split walk, null for the plain one; split walks use each class's
+// default shape)
+int launch_walk32(const ClassBuf<uint32_t> &c, const WalkArgs &a, const HitBuf &h, cudaStream_t st, int variant,
+                  const SplitArgs<uint32_t> *sp = nullptr);
 // lazy: every candidate is below 2^64/3 (the walk then takes lazy one-word steps)
 int launch_walk64(const ClassBuf<uint64_t> &c, const WalkArgs &a, const HitBuf &h, cudaStream_t st, bool lazy,
-                  int variant);
+                  int variant, const SplitArgs<uint64_t> *sp = nullptr);
 // size class 0: p < 2^31, 1: lazy class 64 (p < 2^64/3), 2: other class 64
 int walk_variant_count(int cls, bool fused);
 int walk_variant_shape(int cls, bool fused, int variant, int *nc, int *b);

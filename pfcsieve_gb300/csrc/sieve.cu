@@ -37,17 +37,53 @@ __global__ void __launch_bounds__(256) setup_kernel(ClassBuf<typename T::W> c, S
     }
 }
 
+// The start residues of a split walk's boundaries, all in one launch: CTA
+// row blockIdx.y evaluates boundary y + 1's programs for every candidate
+// (the rows run side by side instead of one launch after another).
+template <class T>
+__global__ void __launch_bounds__(256) split_setup_kernel(ClassBuf<typename T::W> c, SplitSetup<typename T::SW> ss,
+                                                          typename T::W *out0, typename T::W *out1) {
+    using W = typename T::W;
+    const uint32_t k = blockIdx.y;
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t cnt = min(*c.count, c.cap);
+    if (blockIdx.x * blockDim.x >= cnt || k + 1 >= ss.n) return;   // whole CTAs only (staged words)
+    const bool act = i < cnt;
+    typename T::M m;
+    m.init(act ? c.p[i] : (W)3);
+    const typename T::SC sc = T::sctx(m);
+    W s0, s1 = 0;
+    if (ss.mode == (PFC_FACTORIAL | PFC_COMPOSITORIAL)) {
+        s1 = run_prog<T>(m, sc, ss.a[k], m.one);
+        s0 = run_prog<T>(m, sc, ss.b[k], s1);
+    } else {
+        s0 = run_prog<T>(m, sc, ss.a[k], m.one);
+    }
+    if (act) {
+        out0[(size_t)k * c.cap + i] = s0;
+        out1[(size_t)k * c.cap + i] = s1;
+    }
+}
+
 // ------------------------------------------------------------------- walk
 
 // One walk launch over all candidates of a class (see walk_streams): NC
 // candidates per thread (or the two chains of one, FUSED), blocks of B steps.
-template <class T, int NC, bool FUSED, int B>
-__global__ void __launch_bounds__(256) walk_kernel(ClassBuf<typename T::W> c, WalkArgs a, HitBuf h) {
+// SPLIT: sub-range blockIdx.y of a split walk (kernels.cuh SplitArgs).
+template <class T, int NC, bool FUSED, int B, bool SPLIT = false>
+__global__ void __launch_bounds__(256) walk_kernel(ClassBuf<typename T::W> c, WalkArgs a, HitBuf h,
+                                                   SplitArgs<typename T::W> sp) {
     using W = typename T::W;
     constexpr int NS = FUSED ? 2 : NC;   // streams per thread
     const uint32_t cnt = min(*c.count, c.cap);
     const uint32_t blk0 = blockIdx.x * blockDim.x * NC;
     if (blk0 >= cnt) return;  // whole block idle
+    const uint32_t sub = SPLIT ? blockIdx.y : 0;
+    const bool last = !SPLIT || sub + 1 == sp.n;
+    if (SPLIT) {
+        a.lo = sp.start[sub];
+        a.hi = sp.start[sub + 1];
+    }
 
     uint32_t idx[NC];
     bool act[NC];
@@ -59,11 +95,17 @@ __global__ void __launch_bounds__(256) walk_kernel(ClassBuf<typename T::W> c, Wa
         act[s] = idx[s] < cnt;
         m[s].init(act[s] ? c.p[idx[s]] : (W)3);
     }
+    // start residues: the candidate's state, or the sub-range's start
+    W *in0 = c.s0, *in1 = c.s1;
+    if (SPLIT && sub > 0) {
+        in0 = sp.s0 + (size_t)(sub - 1) * sp.pitch;
+        in1 = sp.s1 + (size_t)(sub - 1) * sp.pitch;
+    }
     if (FUSED) {
-        x[0] = act[0] ? c.s0[idx[0]] : 0;
-        x[NS - 1] = act[0] ? c.s1[idx[0]] : 0;
+        x[0] = act[0] ? in0[idx[0]] : 0;
+        x[NS - 1] = act[0] ? in1[idx[0]] : 0;
     } else {
-        W *st = a.chain ? c.s1 : c.s0;
+        const W *st = a.chain ? in1 : in0;
 #pragma unroll
         for (int s = 0; s < NC; ++s) x[s] = act[s] ? st[idx[s]] : 0;
     }
@@ -71,17 +113,21 @@ __global__ void __launch_bounds__(256) walk_kernel(ClassBuf<typename T::W> c, Wa
     const uint32_t walked = (a.hi - a.lo) * (FUSED ? 2u : 1u);
     if (FUSED) {
         if (act[0]) {
-            c.s0[idx[0]] = x[0];
-            c.s1[idx[0]] = x[NS - 1];
-            c.nnext[idx[0]] += walked;
+            if (last) {
+                c.s0[idx[0]] = x[0];
+                c.s1[idx[0]] = x[NS - 1];
+            }
+            if (SPLIT) atomicAdd(c.nnext + idx[0], walked);
+            else c.nnext[idx[0]] += walked;
         }
     } else {
         W *st = a.chain ? c.s1 : c.s0;
 #pragma unroll
         for (int s = 0; s < NC; ++s)
             if (act[s]) {
-                st[idx[s]] = x[s];
-                c.nnext[idx[s]] += walked;
+                if (last) st[idx[s]] = x[s];
+                if (SPLIT) atomicAdd(c.nnext + idx[s], walked);
+                else c.nnext[idx[s]] += walked;
             }
     }
 }
@@ -151,6 +197,26 @@ int launch_setup64w(const ClassBuf<uint64_t> &c, const SetupArgs<WideWord> &a, c
     if (!c.cap) return 0;
     setup_kernel<Cls64L><<<grid_for(c.cap), 256, 0, st>>>(c, a);
     return 1;
+}
+
+template <class T>
+static int launch_split_setup(const ClassBuf<typename T::W> &c, const SplitSetup<typename T::SW> &ss,
+                              typename T::W *s0, typename T::W *s1, cudaStream_t st) {
+    if (!c.cap || ss.n < 2 || ss.n > (uint32_t)kMaxSplit) return 0;
+    split_setup_kernel<T><<<dim3(grid_for(c.cap), ss.n - 1), 256, 0, st>>>(c, ss, s0, s1);
+    return 1;
+}
+int launch_split_setup32(const ClassBuf<uint32_t> &c, const SplitSetup<WideWord> &ss, uint32_t *s0, uint32_t *s1,
+                         cudaStream_t st) {
+    return launch_split_setup<Cls32>(c, ss, s0, s1, st);
+}
+int launch_split_setup64(const ClassBuf<uint64_t> &c, const SplitSetup<uint64_t> &ss, uint64_t *s0, uint64_t *s1,
+                         cudaStream_t st) {
+    return launch_split_setup<Cls64>(c, ss, s0, s1, st);
+}
+int launch_split_setup64w(const ClassBuf<uint64_t> &c, const SplitSetup<WideWord> &ss, uint64_t *s0, uint64_t *s1,
+                          cudaStream_t st) {
+    return launch_split_setup<Cls64L>(c, ss, s0, s1, st);
 }
 
 // Walk variants (candidates per thread, block length) per size class and walk
@@ -231,15 +297,43 @@ template <class T, int NC, bool FUSED, int B>
 static int launch_one(const ClassBuf<typename T::W> &c, const WalkArgs &a, const HitBuf &h, cudaStream_t st) {
     const unsigned threads = walk_cta_threads(c.cap, NC, device_sms());
     const uint32_t per_block = threads * NC;
-    walk_kernel<T, NC, FUSED, B><<<(c.cap + per_block - 1) / per_block, threads, 0, st>>>(c, a, h);
+    SplitArgs<typename T::W> none{};
+    none.n = 1;
+    walk_kernel<T, NC, FUSED, B><<<(c.cap + per_block - 1) / per_block, threads, 0, st>>>(c, a, h, none);
     return 1;
+}
+
+// a split walk: grid y runs over the sub-ranges
+template <class T, int NC, bool FUSED, int B>
+static int launch_split(const ClassBuf<typename T::W> &c, const WalkArgs &a, const HitBuf &h,
+                        const SplitArgs<typename T::W> &sp, cudaStream_t st) {
+    const unsigned threads = walk_cta_threads(c.cap * sp.n, NC, device_sms());
+    const uint32_t per_block = threads * NC;
+    const dim3 grid((c.cap + per_block - 1) / per_block, sp.n);
+    walk_kernel<T, NC, FUSED, B, true><<<grid, threads, 0, st>>>(c, a, h, sp);
+    return 1;
+}
+
+// the default shape of each class for split walks
+template <class T>
+static int launch_walk_split(const ClassBuf<typename T::W> &c, const WalkArgs &a, const HitBuf &h,
+                             const SplitArgs<typename T::W> &sp, cudaStream_t st) {
+    if (!c.cap || sp.n < 1 || sp.n > (uint32_t)kMaxSplit) return 0;
+    if (a.mult2) {
+        if constexpr (std::is_same<T, Cls64>::value) return launch_split<T, 1, true, 8>(c, a, h, sp, st);
+        else return launch_split<T, 1, true, 16>(c, a, h, sp, st);
+    }
+    if constexpr (std::is_same<T, Cls32>::value) return launch_split<T, 2, false, 16>(c, a, h, sp, st);
+    else if constexpr (std::is_same<T, Cls64L>::value) return launch_split<T, 1, false, 32>(c, a, h, sp, st);
+    else return launch_split<T, 1, false, 8>(c, a, h, sp, st);
 }
 
 // the compiled shapes of each class (others fall back to the default)
 template <class T>
 static int launch_walk(const ClassBuf<typename T::W> &c, const WalkArgs &a, const HitBuf &h, cudaStream_t st,
-                       int cls, int variant) {
+                       int cls, int variant, const SplitArgs<typename T::W> *sp) {
     if (!c.cap || a.hi <= a.lo) return 0;
+    if (sp && sp->n > 1) return launch_walk_split<T>(c, a, h, *sp, st);
     int n = 0;
     const WalkVariant *vs = variants(cls, a.mult2 != nullptr, &n);
     const WalkVariant v = vs[(variant >= 0 && variant < n) ? variant : 0];
@@ -261,12 +355,13 @@ static int launch_walk(const ClassBuf<typename T::W> &c, const WalkArgs &a, cons
         return launch_one<T, 1, false, 8>(c, a, h, st);
     }
 }
-int launch_walk32(const ClassBuf<uint32_t> &c, const WalkArgs &a, const HitBuf &h, cudaStream_t st, int variant) {
-    return launch_walk<Cls32>(c, a, h, st, 0, variant);
+int launch_walk32(const ClassBuf<uint32_t> &c, const WalkArgs &a, const HitBuf &h, cudaStream_t st, int variant,
+                  const SplitArgs<uint32_t> *sp) {
+    return launch_walk<Cls32>(c, a, h, st, 0, variant, sp);
 }
 int launch_walk64(const ClassBuf<uint64_t> &c, const WalkArgs &a, const HitBuf &h, cudaStream_t st, bool lazy,
-                  int variant) {
-    return lazy ? launch_walk<Cls64L>(c, a, h, st, 1, variant) : launch_walk<Cls64>(c, a, h, st, 2, variant);
+                  int variant, const SplitArgs<uint64_t> *sp) {
+    return lazy ? launch_walk<Cls64L>(c, a, h, st, 1, variant, sp) : launch_walk<Cls64>(c, a, h, st, 2, variant, sp);
 }
 
 int launch_cmult(uint32_t *out, uint32_t *ramp, const uint32_t *primebits, uint32_t nmin, uint32_t lo, uint32_t hi,

@@ -276,3 +276,73 @@ def test_segment_graphs_equal_stream_launches(mode):
                 out.append((job.totals(), o.sort_factors(job.drain_hits())))
     assert out[0][0] == out[1][0]
     assert np.array_equal(out[0][1], out[1][1])
+
+
+# split walks: (mode, nmin, nmax, p_lo, p_hi) with few candidates and a small
+# nmin, so that the n range is cut into sub-ranges; every size class, both
+# classes in one segment, the fused walk and the primorial's prime indices
+SPLIT_CASES = [
+    (1, 101, 20000, 10**7, 10**7 + 200000),
+    (5, 101, 30000, 10**9, 10**9 + 300000),
+    (4, 101, 30000, 10**9, 10**9 + 300000),
+    (2, 101, 200000, 2**62, 2**62 + 300000),
+    (5, 200, 30000, 2**40, 2**40 + 300000),
+    (1, 101, 20000, 2**64 - 600000, 2**64 - 1),
+    (1, 101, 20000, 2**31 - 200000, 2**31 + 200000),
+    (1, 101, 20000, 3, 60000),
+]
+
+
+def split_run(case, split, stage_calls=False):
+    mode, nmin, nmax, lo, hi = case
+    with pfc.Context(0) as c:
+        c.set_split(split)
+        with pfc.Job(c, mode, nmin, nmax, lo, hi) as job:
+            l0 = c.launches
+            if stage_calls:
+                job.gen(lo, hi)
+                job.setup()
+                job.iterate(nmin, nmax)
+                job.check()
+            else:
+                job.segment(lo, hi)
+            launches = c.launches - l0
+            p, s0, s1 = job.segment_state()
+            order = np.argsort(p)
+            return (job.totals(), o.sort_factors(job.drain_hits()), p[order], s0[order], s1[order], launches)
+
+
+@pytest.mark.parametrize("case", SPLIT_CASES)
+def test_split_walk_equals_the_plain_walk(case):
+    """The walk cut into n sub-ranges (start residues from setup programs)
+    leaves the same residues, totals and hits as one chain per candidate;
+    it did run split (its extra setup launches)."""
+    plain = split_run(case, False)
+    split = split_run(case, True)
+    assert split[5] > plain[5], "the split walk did not run"
+    assert split[0] == plain[0]
+    assert np.array_equal(split[1], plain[1])
+    for k in (2, 3, 4):
+        assert np.array_equal(split[k], plain[k])
+
+
+@pytest.mark.parametrize("case", [SPLIT_CASES[0], SPLIT_CASES[1], SPLIT_CASES[3]])
+def test_split_walk_through_the_stage_calls(case):
+    """pfc_iterate over the whole range walks split too, with the same result
+    as the plain walk through pfc_segment."""
+    plain = split_run(case, False)
+    staged = split_run(case, True, stage_calls=True)
+    assert staged[0] == plain[0]
+    assert np.array_equal(staged[1], plain[1])
+    assert np.array_equal(staged[3], plain[3]) and np.array_equal(staged[4], plain[4])
+
+
+def test_split_walk_matches_the_oracle():
+    """Hits and residues of a split walk against the oracle directly."""
+    mode, nmin, nmax, lo, hi = SPLIT_CASES[1]
+    totals, hits, p, s0, s1, _ = split_run(SPLIT_CASES[1], True)
+    cands = o.candidates(lo, hi)
+    assert np.array_equal(p, cands)
+    ohits, _, terms = o.sieve(mode, nmin, nmax, cands, want_terms=True)
+    assert np.array_equal(s0, terms[:, 0]) and np.array_equal(s1, terms[:, 2])
+    assert np.array_equal(hits, ohits)
