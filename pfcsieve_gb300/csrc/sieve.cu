@@ -69,9 +69,13 @@ __global__ void __launch_bounds__(256) split_setup_kernel(ClassBuf<typename T::W
 
 // One walk launch over all candidates of a class (see walk_streams): NC
 // candidates per thread (or the two chains of one, FUSED), blocks of B steps.
-// SPLIT: sub-range blockIdx.y of a split walk (kernels.cuh SplitArgs).
+// SPLIT: sub-range blockIdx.y of a split walk (kernels.cuh SplitArgs).  The
+// lazy class-64 walk in blocks of 32 is bounded to registers for three CTAs
+// per SM (80 instead of 92, a 20-byte spill): 75.4 ms against 76.9 ms on the
+// primorial search near 2^62.  Split walks are bounded the same way (they
+// reached 99 registers, two CTAs per SM, unbounded).
 template <class T, int NC, bool FUSED, int B, bool SPLIT = false>
-__global__ void __launch_bounds__(256) walk_kernel(ClassBuf<typename T::W> c, WalkArgs a, HitBuf h,
+__global__ void __launch_bounds__(256, ((std::is_same<T, Cls64L>::value && B == 32) || SPLIT) ? 3 : 1) walk_kernel(ClassBuf<typename T::W> c, WalkArgs a, HitBuf h,
                                                    SplitArgs<typename T::W> sp) {
     using W = typename T::W;
     constexpr int NS = FUSED ? 2 : NC;   // streams per thread
@@ -80,9 +84,13 @@ __global__ void __launch_bounds__(256) walk_kernel(ClassBuf<typename T::W> c, Wa
     if (blk0 >= cnt) return;  // whole block idle
     const uint32_t sub = SPLIT ? blockIdx.y : 0;
     const bool last = !SPLIT || sub + 1 == sp.n;
-    if (SPLIT) {
-        a.lo = sp.start[sub];
-        a.hi = sp.start[sub + 1];
+    if (SPLIT) {   // unrolled selects keep the boundary array in the parameter bank
+#pragma unroll
+        for (int k = 0; k < kMaxSplit; ++k)
+            if ((uint32_t)k == sub) {
+                a.lo = sp.start[k];
+                a.hi = sp.start[k + 1];
+            }
     }
 
     uint32_t idx[NC];
