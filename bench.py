@@ -102,6 +102,10 @@ def parse():
                     help="searches of the mixed workload (the full set is 512)")
     ap.add_argument("--no-reference-opencl", action="store_true",
                     help="skip timing the reference's OpenCL program")
+    ap.add_argument("--capture", action="store_true",
+                    help="profiling case: two rounds of the stage calls (gen, setup, iterate, check) on the "
+                         "workload with the default walk variants and nothing else, for ncu (-s 1 -c 1 on a "
+                         "kernel captures the second round's launch)")
     return ap.parse_args()
 
 
@@ -782,9 +786,26 @@ def run_ours(args, wl, world, rank, local, dist):
         print(json.dumps(line), flush=True)
 
 
+def run_capture(wl):
+    """Two rounds of the stage calls on a fresh context, for profilers."""
+    import pfcsieve_gb300 as pfc
+    with pfc.Context(0) as ctx, pfc.Job(ctx, wl["mode"], wl["nmin"], wl["nmax"], wl["pmin"], wl["pmax"]) as job:
+        for _ in range(2):
+            job.gen(wl["pmin"], wl["pmax"])
+            job.setup()
+            job.iterate(wl["nmin"], wl["nmax"])
+            job.check()
+            job.drain_hits()
+        termsum, count = job.totals()
+    print(json.dumps({"capture": wl["desc"], "candidates": count // 2, "checksum_terms": "%016X" % termsum}))
+
+
 def main():
     args = parse()
     wl = WORKLOADS[args.workload]
+    if args.capture:
+        run_capture(wl)
+        return
     world, rank, local = dist_env()
     dist = dist_init(world)
     if args.impl == "reference-opencl":
