@@ -121,6 +121,7 @@ def lib():
             "pfc_autotune": (ctypes.c_int, [vp, ctypes.c_char_p, sz]),
             "pfc_ctx_set_graphs": (ctypes.c_int, [vp, ctypes.c_int]),
             "pfc_ctx_set_split": (ctypes.c_int, [vp, ctypes.c_int]),
+            "pfc_ctx_set_setup_tc": (ctypes.c_int, [vp, ctypes.c_int]),
             "pfc_ctx_set_walk_variant": (ctypes.c_int, [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int]),
             "pfc_ctx_walk_variant": (ctypes.c_int, [vp, ctypes.c_int, ctypes.c_int, P(ctypes.c_int),
                                                     P(ctypes.c_int), P(ctypes.c_int)]),
@@ -196,6 +197,10 @@ class Context:
     def set_split(self, on):
         """Walk small candidate sets in n sub-ranges (default on)."""
         _ck(lib().pfc_ctx_set_split(self.h, int(bool(on))), "pfc_ctx_set_split")
+
+    def set_setup_tc(self, on):
+        """Fold the lazy class-64 setup's table words on the tensor cores (default on)."""
+        _ck(lib().pfc_ctx_set_setup_tc(self.h, int(bool(on))), "pfc_ctx_set_setup_tc")
 
     def set_walk_variant(self, cls, fused, variant):
         _ck(lib().pfc_ctx_set_walk_variant(self.h, cls, int(fused), variant), "pfc_ctx_set_walk_variant")

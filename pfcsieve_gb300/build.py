@@ -27,7 +27,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-fopenmp", "-I" + INC, "-I" + CSRC]
 CXX_FLAGS = ["-O3", "-std=c++17", "-fPIC", "-fopenmp", "-Wall", "-I" + INC, "-I" + CSRC]
 
-CU_SOURCES = ["gen.cu", "sieve.cu", "api.cu", "batch.cu", "verify.cu", "peak.cu", "noalloc.cu"]
+CU_SOURCES = ["gen.cu", "sieve.cu", "setup_tc.cu", "api.cu", "batch.cu", "verify.cu", "peak.cu", "noalloc.cu"]
 CXX_SOURCES = ["host.cpp"]
 
 

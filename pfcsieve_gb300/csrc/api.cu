@@ -78,7 +78,7 @@ struct pfc_job {
     struct GraphKey {
         const void *p32, *p64, *hits, *cmult, *ramp, *split32, *split64;
         uint64_t cap32, cap64, hitcap;
-        int lazy, use32, use64, var[3][2];
+        int lazy, use32, use64, var[3][2], setup_tc;
         uint32_t split_n, split_start[kMaxSplit + 1];
     };
     cudaGraphExec_t graph = nullptr;
@@ -137,6 +137,8 @@ extern "C" int pfc_ctx_create(int device, uint64_t mem_budget, pfc_ctx **out) {
     c->graphs = !(g && g[0] == '0');
     const char *sp = getenv("PFCSIEVE_SPLIT");
     c->split = !(sp && sp[0] == '0');
+    const char *tc = getenv("PFCSIEVE_SETUP_TC");
+    c->setup_tc = !(tc && tc[0] == '0');
     cudaError_t e = cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking);
     if (e == cudaSuccess) {
         cudaMemPoolProps props = {};
@@ -437,8 +439,14 @@ static int enqueue_setup(pfc_job *j) {
     sw.nnext0 = 0;
     if (j->use32) c->launches += launch_setup32(j->c32.view(counts_ptr(j)), s32, c->st);
     if (j->use64) {
-        if (j->seg_hi <= kLazyEnd) c->launches += launch_setup64w(j->c64.view(counts_ptr(j) + 1), sw, c->st);
-        else c->launches += launch_setup64(j->c64.view(counts_ptr(j) + 1), s64, c->st);
+        if (j->seg_hi <= kLazyEnd && c->setup_tc) {
+            CK(cudaMemsetAsync(&j->stats.p->tc_err, 0, sizeof(uint32_t), c->st));
+            c->launches += launch_setup64w_tc(j->c64.view(counts_ptr(j) + 1), sw, &j->stats.p->tc_err, c->st);
+        } else if (j->seg_hi <= kLazyEnd) {
+            c->launches += launch_setup64w(j->c64.view(counts_ptr(j) + 1), sw, c->st);
+        } else {
+            c->launches += launch_setup64(j->c64.view(counts_ptr(j) + 1), s64, c->st);
+        }
     }
     CK(cudaGetLastError());
     j->stage = 2;
@@ -760,6 +768,7 @@ static int commit_segment(pfc_job *j) {
     if (s.counts[0] > j->c32.cap && j->c32.p.p) return PFC_ERR_CAND_OVERFLOW;
     if (s.counts[1] > j->c64.cap && j->c64.p.p) return PFC_ERR_CAND_OVERFLOW;
     if ((!j->c32.p.p && s.counts[0]) || (!j->c64.p.p && s.counts[1])) return PFC_ERR_CAND_OVERFLOW;
+    if (s.tc_err) return PFC_ERR_CUDA;   // a tensor-core setup wait gave up
     if (s.flags & 1u) return PFC_ERR_VALIDATION;
     j->termsum += s.termsum;
     j->primecount += (uint64_t)s.counts[0] + s.counts[1];
@@ -839,6 +848,7 @@ static int segment_body_graph(pfc_job *j) {
     k.split32 = j->split32.p;
     k.split64 = j->split64.p;
     k.split_n = j->split_n;
+    k.setup_tc = c->setup_tc;
     if (j->split_n > 1) memcpy(k.split_start, j->split_start, sizeof(k.split_start));
     if (!j->graph || memcmp(&k, &j->gkey, sizeof(k)) != 0) {
         if (j->graph) cudaGraphExecDestroy(j->graph);
@@ -1246,5 +1256,11 @@ extern "C" int pfc_ctx_set_graphs(pfc_ctx *c, int on) {
 extern "C" int pfc_ctx_set_split(pfc_ctx *c, int on) {
     if (!c) return PFC_ERR_ARG;
     c->split = on != 0;
+    return PFC_OK;
+}
+
+extern "C" int pfc_ctx_set_setup_tc(pfc_ctx *c, int on) {
+    if (!c) return PFC_ERR_ARG;
+    c->setup_tc = on != 0;
     return PFC_OK;
 }

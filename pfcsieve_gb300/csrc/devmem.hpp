@@ -30,6 +30,7 @@ struct pfc_ctx {
     int walk_var[3][2] = {{0, 0}, {0, 0}, {0, 0}};   // walk variant per size class and kind (fused)
     bool graphs = true;   // pfc_segment replays each job's segment body as a CUDA graph
     bool split = true;    // small candidate sets walk their n range in sub-ranges (split walks)
+    bool setup_tc = true; // lazy class-64 setup folds its table words on the tensor cores
     // prime flags of [0, vbits_top] kept for pfc_verify_factors_device (one
     // bit per integer), rebuilt only when a call needs a larger range
     uint32_t *vbits = nullptr;
@@ -151,7 +152,7 @@ struct DevClass {
 struct SegStats {
     uint32_t counts[2];
     uint32_t flags;
-    uint32_t pad;
+    uint32_t tc_err;     // set by the tensor-core setup when a wait gave up
     unsigned long long termsum;
     unsigned long long hits;
 };

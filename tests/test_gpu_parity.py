@@ -346,3 +346,47 @@ def test_split_walk_matches_the_oracle():
     ohits, _, terms = o.sieve(mode, nmin, nmax, cands, want_terms=True)
     assert np.array_equal(s0, terms[:, 0]) and np.array_equal(s1, terms[:, 2])
     assert np.array_equal(hits, ohits)
+
+
+# tensor-core setup (class 64 below 2^64/3): programs of one tile and of many
+# (group boundaries inside tiles), both programs of the combined search, a
+# product program without squarings, p just above 2^31 and near 2^64/3
+TC_CASES = [
+    (1, 20000, 20100, 2**40, 2**40 + 20000),
+    (1, 300000, 300100, 2**50, 2**50 + 20000),
+    (5, 200000, 200050, 2**62, 2**62 + 20000),
+    (2, 100000, 100050, 2**31 + 10, 2**31 + 40000),
+    (4, 150000, 150050, 6 * 10**18, 6 * 10**18 + 40000),
+]
+
+
+def setup_run(case, tc):
+    mode, nmin, nmax, lo, hi = case
+    with pfc.Context(0) as c:
+        c.set_setup_tc(tc)
+        c.set_split(False)
+        with pfc.Job(c, mode, nmin, nmax, lo, hi) as job:
+            job.segment(lo, hi)
+            p, s0, s1 = job.segment_state()
+            order = np.argsort(p)
+            return job.totals(), o.sort_factors(job.drain_hits()), p[order], s0[order], s1[order]
+
+
+@pytest.mark.parametrize("case", TC_CASES)
+def test_tensor_core_setup_equals_the_integer_setup(case):
+    tc = setup_run(case, True)
+    ip = setup_run(case, False)
+    assert tc[0] == ip[0]
+    assert np.array_equal(tc[1], ip[1])
+    for k in (2, 3, 4):
+        assert np.array_equal(tc[k], ip[k])
+
+
+def test_tensor_core_setup_matches_the_oracle():
+    mode, nmin, nmax, lo, hi = TC_CASES[2]
+    totals, hits, p, s0, s1 = setup_run(TC_CASES[2], True)
+    cands = o.candidates(lo, hi)
+    assert np.array_equal(p, cands)
+    ohits, _, terms = o.sieve(mode, nmin, nmax, cands, want_terms=True)
+    assert np.array_equal(s0, terms[:, 0]) and np.array_equal(s1, terms[:, 2])
+    assert np.array_equal(hits, ohits)
