@@ -40,6 +40,9 @@ struct pfc_job {
     DevProg<WideWord> a32, b32;   // class 32 (896-bit words)
     DevProg<uint64_t> a64, b64;   // class 64 at or above 2^64/3 (64-bit words)
     DevProg<WideWord> aw, bw;     // class 64 below 2^64/3 (896-bit words)
+    DArr<uint8_t> tct;            // aw, bw as fp16 tiles for the tensor-core setup (packed on first use)
+    uint32_t tc_first[2] = {0, 0}, tc_end[2] = {0, 0}, tc_ntiles[2] = {0, 0};
+    bool tc_packed = false;
     uint64_t setup_mulmods32 = 0, setup_mulmods64 = 0;
     DArr<uint32_t> primebits;
     DArr<uint32_t> qlist;
@@ -214,6 +217,7 @@ static int job_release(pfc_job *j) {
     j->b64.release(c);
     j->aw.release(c);
     j->bw.release(c);
+    j->tct.release(c);
     j->primebits.release(c);
     j->qlist.release(c);
     j->cmult.release(c);
@@ -310,6 +314,16 @@ extern "C" int pfc_job_create(pfc_ctx *c, unsigned mode, uint32_t nmin, uint32_t
     }
     j->setup_mulmods32 = a32.mulmods() + b32.mulmods();
     j->setup_mulmods64 = need64 ? a64.mulmods() + b64.mulmods() : aw.mulmods() + bw.mulmods();
+
+    const HostProg<WideWord> *wide[2] = {&aw, &bw};
+    for (int k = 0; k < 2; ++k) {
+        const std::vector<uint32_t> &gr = wide[k]->groups;
+        if (gr.size() >= 3) {
+            j->tc_first[k] = gr[0];
+            j->tc_end[k] = gr[gr.size() - 2];
+            j->tc_ntiles[k] = (j->tc_end[k] - j->tc_first[k] + 127) / 128;
+        }
+    }
 
     cudaError_t e = j->a32.upload(c, a32);
     if (e == cudaSuccess) e = j->a64.upload(c, a64);
@@ -420,6 +434,22 @@ extern "C" int pfc_gen_candidates(pfc_job *j, uint64_t p_lo, uint64_t p_hi) {
     return enqueue_gen(j, p_lo, p_hi);
 }
 
+// The wide programs as fp16 tiles for the tensor-core setup, packed once per
+// job on the context stream (before any capture of a segment graph).
+static int tc_prepare(pfc_job *j) {
+    if (j->tc_packed) return PFC_OK;
+    pfc_ctx *c = j->ctx;
+    const size_t tb = tc_tile_bytes(), na = j->tc_ntiles[0], nb = j->tc_ntiles[1];
+    CK(j->tct.alloc(c, std::max<size_t>((na + nb) * tb, 16)));
+    c->launches += launch_tc_pack(j->aw.words.p, j->tc_first[0], j->tc_end[0], (uint32_t)na, j->tct.p, c->st);
+    c->launches += launch_tc_pack(j->bw.words.p, j->tc_first[1], j->tc_end[1], (uint32_t)nb, j->tct.p + na * tb, c->st);
+    CK(cudaGetLastError());
+    j->tc_packed = true;
+    return PFC_OK;
+}
+
+static bool tc_setup_applies(const pfc_job *j) { return j->use64 && j->seg_hi <= kLazyEnd && j->ctx->setup_tc; }
+
 static int enqueue_setup(pfc_job *j) {
     pfc_ctx *c = j->ctx;
     SetupArgs<WideWord> s32;
@@ -439,9 +469,13 @@ static int enqueue_setup(pfc_job *j) {
     sw.nnext0 = 0;
     if (j->use32) c->launches += launch_setup32(j->c32.view(counts_ptr(j)), s32, c->st);
     if (j->use64) {
-        if (j->seg_hi <= kLazyEnd && c->setup_tc) {
+        if (tc_setup_applies(j)) {
+            const int rc = tc_prepare(j);
+            if (rc) return rc;
+            const TcTiles ta{j->tct.p, j->tc_ntiles[0]},
+                tb{j->tct.p + (size_t)j->tc_ntiles[0] * tc_tile_bytes(), j->tc_ntiles[1]};
             CK(cudaMemsetAsync(&j->stats.p->tc_err, 0, sizeof(uint32_t), c->st));
-            c->launches += launch_setup64w_tc(j->c64.view(counts_ptr(j) + 1), sw, &j->stats.p->tc_err, c->st);
+            c->launches += launch_setup64w_tc(j->c64.view(counts_ptr(j) + 1), sw, ta, tb, &j->stats.p->tc_err, c->st);
         } else if (j->seg_hi <= kLazyEnd) {
             c->launches += launch_setup64w(j->c64.view(counts_ptr(j) + 1), sw, c->st);
         } else {
@@ -831,6 +865,10 @@ static int segment_body_graph(pfc_job *j) {
         const size_t need = (((size_t)std::min<uint64_t>(L, iter_end(j) - iter_begin(j))) + 15) & ~(size_t)15;
         if ((j->mode & PFC_COMPOSITORIAL) && j->cmult.n < need) CK(j->cmult.alloc(c, std::max<size_t>(need, 4096)));
         if ((j->mode & PFC_FACTORIAL) && j->ramp.n < need) CK(j->ramp.alloc(c, std::max<size_t>(need, 4096)));
+    }
+    if (tc_setup_applies(j)) {
+        const int rc = tc_prepare(j);
+        if (rc) return rc;
     }
     pfc_job::GraphKey k{};
     k.p32 = j->c32.p.p;

@@ -133,9 +133,19 @@ int launch_setup32(const ClassBuf<uint32_t> &c, const SetupArgs<WideWord> &a, cu
 int launch_setup64(const ClassBuf<uint64_t> &c, const SetupArgs<uint64_t> &a, cudaStream_t st);
 // class 64 below 2^64/3 with 896-bit table words
 int launch_setup64w(const ClassBuf<uint64_t> &c, const SetupArgs<WideWord> &a, cudaStream_t st);
-// the same with the table-word fold on the tensor cores (setup_tc.cu); a
-// wait that gives up sets *err (the segment then fails with PFC_ERR_CUDA)
-int launch_setup64w_tc(const ClassBuf<uint64_t> &c, const SetupArgs<WideWord> &a, uint32_t *err, cudaStream_t st);
+// the same with the table-word fold on the tensor cores (setup_tc.cu): each
+// program's words first packed once into fp16 byte tiles of 128 words
+// (tc_tile_bytes() each; tile i holds words first + 128 i ..), then the
+// setup over those tiles; a wait that gives up sets *err (the segment then
+// fails with PFC_ERR_CUDA)
+struct TcTiles {
+    const void *tiles;   // device, ntiles * tc_tile_bytes(), 16-byte aligned
+    uint32_t ntiles;
+};
+size_t tc_tile_bytes();
+int launch_tc_pack(const WideWord *words, uint32_t first, uint32_t end, uint32_t ntiles, void *out, cudaStream_t st);
+int launch_setup64w_tc(const ClassBuf<uint64_t> &c, const SetupArgs<WideWord> &a, const TcTiles &ta,
+                       const TcTiles &tb, uint32_t *err, cudaStream_t st);
 // start residues of a split walk: boundary k's into s0/s1 + (k-1) * c.cap
 int launch_split_setup32(const ClassBuf<uint32_t> &c, const SplitSetup<WideWord> &ss, uint32_t *s0, uint32_t *s1,
                          cudaStream_t st);

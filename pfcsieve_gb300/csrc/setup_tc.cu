@@ -6,29 +6,37 @@
 // on the integer pipe is the fold of each word against the candidate's
 // position residues, T = sum_b z_b w_b with w_b = 2^(8b+32) mod p: an exact
 // integer contraction (words x bytes) x (bytes x candidates).  Here it runs
-// on the tensor cores in bf16 with fp32 accumulation and stays exact:
-//   * a word is its 112 bytes z_b (0..255, exact in bf16);
+// on the tensor cores in fp16 with fp32 accumulation and stays exact:
+//   * a word is its 112 bytes z_b (0..255, exact in fp16);
 //   * a candidate's 64-bit residues w_b are split into 8 byte planes
 //     W_a[b] = byte a of w_b (0..255);
-//   * D_a[word, cand] = sum_b z_b W_a[b] < 112 * 255 * 255 < 2^23, exact in
-//     the fp32 accumulator;
-//   * T = sum_a D_a 2^(8a) < 2^79 is assembled on the CUDA cores.
-// One CTA of 256 threads owns 64 candidates: their byte planes stay in
-// shared memory (8 x 14 KB) as the MMA's B operand (N = 64, K-major), and
-// the program's words stream through in tiles of 128 (A operand, M = 128,
-// K = 112: seven MMAs of K = 16 per plane, 56 per tile, into 8 x 64 TMEM
-// columns, word = TMEM lane).  Per tile:
-//   1. the threads convert the words' limbs into 112 bf16 bytes (A tile);
-//   2. one thread issues the 56 tcgen05.mma and a commit to an mbarrier;
-//   3. each thread reads one word's 8 sums for a share of the candidates
-//      (tcgen05.ld; the warps of a lane quadrant split the candidates),
-//      assembles T and reduces it to u = T 2^-96 R (mod p, lazy), so that
-//      u = Z (mod p) and multiplying it in lowers the power of R by one, as a
-//      word on the integer pipe does;
-//   4. per candidate the words' u are multiplied into the accumulator in
-//      program order (Horner: a group's squarings come before its words):
-//      four threads per candidate, each over a quarter of the tile, when no
-//      group starts inside the tile, else one thread in order.
+//   * D_a[word, cand] = 2^23 + sum_b z_b W_a[b]: the first MMA of each plane
+//     writes 2048 * 4096 = 2^23 into every sum, and sum_b z_b W_a[b] <=
+//     112 * 255 * 255 < 2^23, so every partial sum is an integer in
+//     [2^23, 2^24), exact in fp32, and the fp32 bits of D_a are
+//     0x4B000000 + the integer sum;
+//   * T = sum_a (D_a - 2^23) 2^(8a) < 2^79 is assembled on the CUDA cores.
+// The program's words are first laid out as fp16 byte tiles of 128 words
+// (A operand, M = 128, K = 112, the shared-memory image; tc_pack_kernel,
+// once per job).  One CTA of 512 threads owns 64 candidates: their byte
+// planes stay in shared memory as the MMA's B operand, K-major, one 8-row
+// core group per candidate (row = plane), so that one MMA with N = 256 covers
+// 32 candidates x 8 planes and a candidate's 8 sums are adjacent TMEM
+// columns (512 columns, word = TMEM lane; per half of the candidates a bias
+// MMA and seven MMAs of K = 16, 16 per tile).  Per tile t:
+//   1. each thread reads one word's sums for a share of the candidates
+//      (tcgen05.ld, 8 candidates x 8 planes per load; the four warps of a
+//      lane quadrant split the candidates), assembles T and reduces it by one
+//      Montgomery round, u = (T + m p) / 2^32 with m = -T p^-1 mod 2^32, so
+//      u = T 2^-32 = Z (mod p) and u < 2^48 + p, stored in shared memory;
+//      meanwhile tile t+1 arrives by one bulk copy (cp.async.bulk);
+//   2. the products of tile t+1 are issued; they run while
+//   3. each candidate's eight threads multiply an eighth of the tile's u into
+//      their running products, two independent chains per thread (two lazy
+//      rounds per product; a product lowers the power of R by one, as a
+//      word on the integer pipe does).  At a group start that carries
+//      squarings (Horner over exponent bits) and at the end of a program the
+//      products are combined into the accumulator, which is then squared.
 // The result equals setup_kernel<Cls64L>'s: same program, exact arithmetic,
 // canonical residues at the end.  Every wait is bounded; after a timeout the
 // kernel sets bit 1 of `flags`, frees its TMEM and stores nothing.
@@ -41,60 +49,75 @@
 namespace pfc {
 namespace {
 
-constexpr int kTcThreads = 256;               // two warps per TMEM lane quadrant
-constexpr int kTcGroups = kTcThreads / 128;   // warp groups (each covers the 128 lanes)
-constexpr int kTcParts = kTcThreads / 64;     // threads per candidate
+constexpr int kTcThreads = 512;
+constexpr int kTcGroups = kTcThreads / 128;   // warp groups (each covers the 128 TMEM lanes)
+constexpr int kTcParts = kTcThreads / 64;     // threads per candidate in the products
 constexpr int kTcWords = 128;                 // words per tile: MMA M, TMEM lanes
-constexpr int kTcCands = 64;                  // candidates per CTA: MMA N
+constexpr int kTcCands = 64;                  // candidates per CTA
 constexpr int kTcBytes = 112;                 // bytes of a 896-bit word: MMA K
 constexpr int kTcPlanes = 8;                  // byte planes of a 64-bit residue
+constexpr int kTcHalf = 32;                   // candidates per MMA: N = 32 x 8 planes = 256
+constexpr int kTcChains = 4;                  // independent product chains per thread
 constexpr uint32_t kRowGroup = (kTcBytes / 8) * 128;              // 1792 B between 8-row core groups
+constexpr uint32_t kBiasRowGroup = 2 * 128;                       // bias tiles: K = 16
 constexpr uint32_t kATile = (kTcWords / 8) * kRowGroup;           // 28,672 B
-constexpr uint32_t kBPlane = (kTcCands / 8) * kRowGroup;          // 14,336 B
+constexpr uint32_t kBTile = kTcCands * kRowGroup;                 // 114,688 B: row group = candidate
+constexpr uint32_t kUStride = kTcWords + 1;   // u64 per candidate row; odd: column reads hit distinct banks
 constexpr uint32_t kOffA = 0;
-constexpr uint32_t kOffB = kOffA + kATile;                         // 8 planes
-constexpr uint32_t kOffU = kOffB + kTcPlanes * kBPlane;            // u64 [64 cands][128 words]
-constexpr uint32_t kOffPart = kOffU + kTcCands * kTcWords * 8;     // u64 [parts][64] partial products
-constexpr uint32_t kOffCand = kOffPart + kTcParts * kTcCands * 8;  // p, one (u64) and q (u32) per candidate
-constexpr uint32_t kOffMisc = kOffCand + kTcCands * 24;            // mbarrier, TMEM address, timeout flag
+constexpr uint32_t kOffB = kOffA + kATile;
+constexpr uint32_t kOffABias = kOffB + kBTile;                                // 128 x 16, column 0 = 2048
+constexpr uint32_t kOffBBias = kOffABias + (kTcWords / 8) * kBiasRowGroup;    // 256 x 16, column 0 = 4096
+constexpr uint32_t kOffU = kOffBBias + kTcHalf * kBiasRowGroup;               // u64 [64 cands][kUStride]
+constexpr uint32_t kOffPart = kOffU + kTcCands * kUStride * 8;      // u64 [parts][64] running products
+constexpr uint32_t kOffCand = kOffPart + kTcParts * kTcCands * 8;   // p (u64) and q (u32) per candidate
+constexpr uint32_t kOffMisc = kOffCand + kTcCands * 16;             // 2 mbarriers, TMEM address, timeout flag
 constexpr uint32_t kSmemBytes = kOffMisc + 64;
 static_assert(kSmemBytes <= 227 * 1024, "setup_tc shared memory");
-static_assert(kOffB % 1024 == 0 && kOffU % 16 == 0 && kOffMisc % 8 == 0, "setup_tc alignment");
-constexpr uint32_t kTmemCols = 512;           // 8 planes x 64 candidates
+static_assert(kOffB % 16 == 0 && kOffABias % 16 == 0 && kOffBBias % 16 == 0 && kOffU % 16 == 0 &&
+                  kOffMisc % 8 == 0,
+              "setup_tc alignment");
+static_assert(kATile % 16 == 0, "bulk copies move multiples of 16 bytes");
+constexpr uint32_t kTmemCols = 512;           // 64 candidates x 8 planes (column = 8 c + plane)
 constexpr long kWaitLimit = 1L << 26;         // mbarrier polls before giving up
+constexpr uint32_t kBiasBits = 0x4B000000u;   // fp32 bits of 2^23
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
 // shared-memory matrix descriptor: K-major, no swizzle; core matrices of
 // 8 rows x 16 bytes, K-adjacent cores 128 B apart (leading byte offset),
-// 8-row groups kRowGroup apart (stride byte offset), descriptor version 1
-__device__ __forceinline__ uint64_t mdesc(uint32_t addr) {
-    return (uint64_t)((addr & 0x3FFFF) >> 4) | ((uint64_t)(128u >> 4) << 16) | ((uint64_t)(kRowGroup >> 4) << 32) |
+// 8-row groups `sbo` apart (stride byte offset), descriptor version 1
+__device__ __forceinline__ uint64_t mdesc(uint32_t addr, uint32_t sbo) {
+    return (uint64_t)((addr & 0x3FFFF) >> 4) | ((uint64_t)(128u >> 4) << 16) | ((uint64_t)(sbo >> 4) << 32) |
            (1ull << 46);
 }
 
 // byte offset of the core-matrix row holding elements (r, 8 k8 .. 8 k8 + 7)
-__device__ __forceinline__ uint32_t tile_off(uint32_t r, uint32_t k8) { return (r / 8) * kRowGroup + k8 * 128 + (r % 8) * 16; }
-
-// bf16 bits of an integer 0..255 (exact): the float v, whose low 16 bits are 0
-__device__ __forceinline__ uint32_t bf16_of_byte(uint32_t v) {
-    return __float_as_uint(__uint_as_float(0x4B000000u | v) - 8388608.0f) >> 16;
+__device__ __forceinline__ uint32_t tile_off(uint32_t r, uint32_t k8, uint32_t rowgroup = kRowGroup) {
+    return (r / 8) * rowgroup + k8 * 128 + (r % 8) * 16;
 }
 
-// eight bytes -> eight bf16 (16 bytes, one core-matrix row)
-__device__ __forceinline__ uint4 bf16x8(uint64_t bytes8) {
-    uint32_t h[8];
-#pragma unroll
-    for (int i = 0; i < 8; ++i) h[i] = bf16_of_byte((uint32_t)(bytes8 >> (8 * i)) & 0xFFu);
-    return make_uint4(h[0] | (h[1] << 16), h[2] | (h[3] << 16), h[4] | (h[5] << 16), h[6] | (h[7] << 16));
+// two bytes (bits 0-7 and 8-15 of x, or 16-23 and 24-31 with hi) -> two
+// fp16 0..255: the fp16 of 1024 + v is 0x6400 | v (v < 1024), less 1024
+template <bool HI>
+__device__ __forceinline__ uint32_t f16x2_of_bytes(uint32_t x) {
+    const uint32_t y = __byte_perm(x, 0x64u, HI ? 0x4342u : 0x4140u);
+    uint32_t r;
+    asm("sub.rn.f16x2 %0, %1, %2;" : "=r"(r) : "r"(y), "r"(0x64006400u));
+    return r;
 }
 
-// bytes 8 k8 .. 8 k8 + 7 of a 896-bit word given as 32 limbs of 28 bits
-__device__ __forceinline__ uint64_t word_bytes8(const uint32_t (&limb)[kWideLimbs], int k8) {
+// eight bytes -> eight fp16 (16 bytes, one core-matrix row)
+__device__ __forceinline__ uint4 f16x8(uint64_t bytes8) {
+    const uint32_t lo = (uint32_t)bytes8, hi = (uint32_t)(bytes8 >> 32);
+    return make_uint4(f16x2_of_bytes<false>(lo), f16x2_of_bytes<true>(lo), f16x2_of_bytes<false>(hi),
+                      f16x2_of_bytes<true>(hi));
+}
+
+// bytes 8 k8 .. 8 k8 + 7 of a 896-bit word (32 limbs of 28 bits)
+__device__ __forceinline__ uint64_t word_bytes8(const uint32_t *limb, int k8) {
     const int bit = 64 * k8, i = bit / 28, o = bit % 28;
     // bits [bit, bit + 64) lie in limbs i .. i + 3 (o + 64 <= 91 < 112)
     unsigned __int128 acc = 0;
-#pragma unroll
     for (int j = 0; j < 4; ++j)
         if (i + j < kWideLimbs) acc |= (unsigned __int128)limb[i + j] << (28 * j);
     return (uint64_t)(acc >> o);
@@ -113,23 +136,32 @@ __device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity) {
     return false;
 }
 
-// the 8 plane sums of this thread's word (TMEM lane) for candidates c0..c0+7
-__device__ __forceinline__ void load_sums(uint32_t taddr, uint32_t c0, uint32_t (&v)[kTcPlanes][8]) {
-#pragma unroll
-    for (int a = 0; a < kTcPlanes; ++a) {
-        const uint32_t addr = taddr + a * kTcCands + c0;
-        asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
-                     : "=r"(v[a][0]), "=r"(v[a][1]), "=r"(v[a][2]), "=r"(v[a][3]), "=r"(v[a][4]), "=r"(v[a][5]),
-                       "=r"(v[a][6]), "=r"(v[a][7])
-                     : "r"(addr)
-                     : "memory");
-    }
+// the sums of this thread's word (TMEM lane) for candidates c0..c0+7:
+// v[8 j + a] = plane a of candidate c0 + j
+__device__ __forceinline__ void load_sums(uint32_t taddr, uint32_t c0, uint32_t (&v)[64]) {
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x64.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+        "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31,%32,%33,%34,%35,%36,%37,%38,%39,"
+        "%40,%41,%42,%43,%44,%45,%46,%47,%48,%49,%50,%51,%52,%53,%54,%55,%56,%57,%58,%59,%60,%61,%62,%63}, [%64];"
+        : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+          "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15]),
+          "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]), "=r"(v[20]), "=r"(v[21]), "=r"(v[22]), "=r"(v[23]),
+          "=r"(v[24]), "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]), "=r"(v[29]), "=r"(v[30]), "=r"(v[31]),
+          "=r"(v[32]), "=r"(v[33]), "=r"(v[34]), "=r"(v[35]), "=r"(v[36]), "=r"(v[37]), "=r"(v[38]), "=r"(v[39]),
+          "=r"(v[40]), "=r"(v[41]), "=r"(v[42]), "=r"(v[43]), "=r"(v[44]), "=r"(v[45]), "=r"(v[46]), "=r"(v[47]),
+          "=r"(v[48]), "=r"(v[49]), "=r"(v[50]), "=r"(v[51]), "=r"(v[52]), "=r"(v[53]), "=r"(v[54]), "=r"(v[55]),
+          "=r"(v[56]), "=r"(v[57]), "=r"(v[58]), "=r"(v[59]), "=r"(v[60]), "=r"(v[61]), "=r"(v[62]), "=r"(v[63])
+        : "r"(taddr + 8 * c0)
+        : "memory");
     asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 }
 
-// an exact fp32 integer 0 <= x < 2^23 (given as its bits) as uint32
-__device__ __forceinline__ uint32_t f2u23(uint32_t bits) {
-    return __float_as_uint(__uint_as_float(bits) + 8388608.0f) & 0x7FFFFFu;
+// sum_{a<4} e_a 2^(8a) from the fp32 bits kBiasBits + e_a of four planes
+// (e_a < 2^23: a pair e_0 + e_1 2^8 < 2^32, and the bias of the shifted
+// plane leaves 32 bits)
+__device__ __forceinline__ uint64_t planes4(uint32_t b0, uint32_t b1, uint32_t b2, uint32_t b3) {
+    const uint32_t lo = b0 + (b1 << 8) - kBiasBits, hi = b2 + (b3 << 8) - kBiasBits;
+    return (uint64_t)lo + ((uint64_t)hi << 16);
 }
 
 __device__ __forceinline__ void sync_tc() {
@@ -143,10 +175,31 @@ __device__ __forceinline__ uint64_t mulw2(uint64_t s, uint64_t u, uint64_t p, ui
     return mul_wide_word<2>(s, w, p, q);
 }
 
+// the program's word range [first, end)
+__device__ __forceinline__ void prog_range(const Prog<WideWord> &pg, uint32_t &first, uint32_t &end) {
+    first = end = 0;
+    if (pg.ngroups) {
+        first = __ldg(pg.groups);
+        end = __ldg(pg.groups + 3 * (pg.ngroups - 1) + 1);
+    }
+}
+
 }  // namespace
 
+// One thread per (tile, word, 8-byte group): the fp16 shared-memory image of
+// the program's words [first, end) in tiles of 128 (zeros past the end).
+__global__ void tc_pack_kernel(const WideWord *words, uint32_t first, uint32_t end, uint32_t ntiles, uint4 *out) {
+    constexpr uint32_t kPer = kTcWords * (kTcBytes / 8);
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= ntiles * kPer) return;
+    const uint32_t tile = i / kPer, word = (i % kPer) / (kTcBytes / 8), k8 = i % (kTcBytes / 8);
+    const uint32_t w = first + tile * kTcWords + word;
+    const uint64_t bytes = w < end ? word_bytes8(words[w].limb, (int)k8) : 0;
+    out[(tile * kATile + tile_off(word, k8)) / 16] = f16x8(bytes);
+}
+
 __global__ void __launch_bounds__(kTcThreads, 1) setup_tc_kernel(ClassBuf<uint64_t> c, SetupArgs<WideWord> a,
-                                                                 uint32_t *flags) {
+                                                                 TcTiles ta, TcTiles tb, uint32_t *flags) {
     extern __shared__ __align__(1024) unsigned char sm[];
     const uint32_t tid = threadIdx.x, warp = tid / 32;
     const uint32_t cnt = min(*c.count, c.cap);
@@ -156,11 +209,11 @@ __global__ void __launch_bounds__(kTcThreads, 1) setup_tc_kernel(ClassBuf<uint64
     uint64_t *U = reinterpret_cast<uint64_t *>(sm + kOffU);
     uint64_t *part = reinterpret_cast<uint64_t *>(sm + kOffPart);
     uint64_t *cand_p = reinterpret_cast<uint64_t *>(sm + kOffCand);
-    uint64_t *cand_one = cand_p + kTcCands;
-    uint32_t *cand_q = reinterpret_cast<uint32_t *>(cand_one + kTcCands);
-    uint64_t *mbar = reinterpret_cast<uint64_t *>(sm + kOffMisc);
-    uint32_t *taddr_slot = reinterpret_cast<uint32_t *>(sm + kOffMisc + 8);
-    uint32_t *timeout = reinterpret_cast<uint32_t *>(sm + kOffMisc + 12);
+    uint32_t *cand_q = reinterpret_cast<uint32_t *>(cand_p + kTcCands);
+    uint64_t *mbar_mma = reinterpret_cast<uint64_t *>(sm + kOffMisc);
+    uint64_t *mbar_load = reinterpret_cast<uint64_t *>(sm + kOffMisc + 8);
+    uint32_t *taddr_slot = reinterpret_cast<uint32_t *>(sm + kOffMisc + 16);
+    uint32_t *timeout = reinterpret_cast<uint32_t *>(sm + kOffMisc + 20);
 
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(taddr_slot)),
@@ -169,7 +222,8 @@ __global__ void __launch_bounds__(kTcThreads, 1) setup_tc_kernel(ClassBuf<uint64
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     }
     if (tid == 0) {
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(mbar)) : "memory");
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(mbar_mma)) : "memory");
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(mbar_load)) : "memory");
         *timeout = 0;
     }
 
@@ -182,19 +236,38 @@ __global__ void __launch_bounds__(kTcThreads, 1) setup_tc_kernel(ClassBuf<uint64
     m.init(act ? c.p[ci] : 0x1FFFFFFFFFFFFFFFull);   // an idle slot works on 2^61 - 1
     if (prt == 0) {
         cand_p[cl] = m.p;
-        cand_one[cl] = m.one;
         cand_q[cl] = m.q32;
     }
 
+    // bias tiles: A column 0 = 2048, B column 0 = 4096 (fp16), the rest 0
+    for (uint32_t r = tid; r < kTcWords + 8 * kTcHalf; r += kTcThreads) {
+        const bool isa = r < kTcWords;
+        const uint32_t row = isa ? r : r - kTcWords;
+        unsigned char *base = sm + (isa ? kOffABias : kOffBBias);
+        *reinterpret_cast<uint4 *>(base + tile_off(row, 0, kBiasRowGroup)) =
+            make_uint4(isa ? 0x6800u : 0x6C00u, 0, 0, 0);
+        *reinterpret_cast<uint4 *>(base + tile_off(row, 1, kBiasRowGroup)) = make_uint4(0, 0, 0, 0);
+    }
+
     // B operand: the candidate's residues w_b = 2^(8b+32) mod p as 8 byte
-    // planes (each part writes its share of the 14 groups of 8 bytes)
+    // planes, the rows of the candidate's core group (each part writes its
+    // share of the 14 groups of 8 bytes, starting from 2^32 256^b0 mod p by
+    // square-and-multiply; the plane order is rotated by the candidate so
+    // that a warp's stores spread over the banks)
     {
         constexpr uint32_t kChunk = (kTcBytes / 8 + kTcParts - 1) / kTcParts;
         const uint32_t k8a = min(prt * kChunk, (uint32_t)(kTcBytes / 8)),
                        k8b = min(k8a + kChunk, (uint32_t)(kTcBytes / 8));
         const uint64_t c256 = m.to_mont(256);
         uint64_t x = m.p > (1ull << 32) ? (1ull << 32) : (1ull << 32) - m.p;   // 2^32 mod p
-        for (uint32_t b = 0; b < 8 * k8a; ++b) x = m.mul(x, c256);
+        {
+            uint64_t pw = m.one, base = c256;
+            for (uint32_t e = 8 * k8a; e; e >>= 1) {
+                if (e & 1) pw = m.mul(pw, base);
+                base = m.mul(base, base);
+            }
+            x = m.mul(x, pw);
+        }
         for (uint32_t k8 = k8a; k8 < k8b; ++k8) {
             uint64_t w[8];
 #pragma unroll
@@ -203,151 +276,211 @@ __global__ void __launch_bounds__(kTcThreads, 1) setup_tc_kernel(ClassBuf<uint64
                 x = m.mul(x, c256);
             }
 #pragma unroll
-            for (int pl = 0; pl < kTcPlanes; ++pl) {
+            for (int r = 0; r < kTcPlanes; ++r) {
+                const int pl = (r + (int)cl) % kTcPlanes;
                 uint64_t bytes = 0;
 #pragma unroll
                 for (int j = 0; j < 8; ++j) bytes |= ((w[j] >> (8 * pl)) & 0xFFull) << (8 * j);
-                *reinterpret_cast<uint4 *>(sm + kOffB + pl * kBPlane + tile_off(cl, k8)) = bf16x8(bytes);
+                *reinterpret_cast<uint4 *>(sm + kOffB + tile_off(8 * cl + pl, k8)) = f16x8(bytes);
             }
         }
     }
+
+    const uint32_t quad = warp % 4, wgroup = warp / 4;      // TMEM lane quadrant, warp group
+    const uint32_t word = quad * 32 + (tid % 32);           // this thread's word of a tile
+    // f32 <- f16 x f16, both K-major, N = 256, M = 128
+    const uint32_t idesc = (1u << 4) | ((uint32_t)(8 * kTcHalf >> 3) << 17) | ((uint32_t)(kTcWords >> 4) << 24);
+    const int nprog = a.mode == (PFC_FACTORIAL | PFC_COMPOSITORIAL) ? 2 : 1;
+
+    // tile i of program pi into the A region (one thread), completing on mbar_load
+    auto load_tile = [&](int pi, uint32_t i) {
+        const TcTiles &tt = pi == 0 ? ta : tb;
+        const unsigned char *src = reinterpret_cast<const unsigned char *>(tt.tiles) + (size_t)i * kATile;
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(mbar_load)),
+                     "r"(kATile)
+                     : "memory");
+        asm volatile(
+            "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                smem_u32(sm + kOffA)),
+            "l"(src), "r"(kATile), "r"(smem_u32(mbar_load))
+            : "memory");
+    };
+    // the tile's products, per half of the candidates after its bias product
+    auto issue_mma = [&](uint32_t tbase) {
+        const uint32_t aaddr = smem_u32(sm + kOffA), abias = smem_u32(sm + kOffABias),
+                       bbias = smem_u32(sm + kOffBBias);
+#pragma unroll
+        for (int h = 0; h < kTcCands / kTcHalf; ++h) {
+            const uint32_t baddr = smem_u32(sm + kOffB + h * kTcHalf * kRowGroup), d = tbase + h * 8 * kTcHalf;
+            asm volatile(
+                "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, 0, 0;\n\t"
+                "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d),
+                "l"(mdesc(abias, kBiasRowGroup)), "l"(mdesc(bbias, kBiasRowGroup)), "r"(idesc)
+                : "memory");
+#pragma unroll
+            for (int s = 0; s < kTcBytes / 16; ++s)
+                asm volatile(
+                    "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, 1, 0;\n\t"
+                    "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d),
+                    "l"(mdesc(aaddr + s * 256, kRowGroup)), "l"(mdesc(baddr + s * 256, kRowGroup)), "r"(idesc)
+                    : "memory");
+        }
+        asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                         smem_u32(mbar_mma))
+                     : "memory");
+    };
+    // the tile after tile i of program pi, across programs; false at the end
+    auto next_tile = [&](int &pi, uint32_t &i, bool started) -> bool {
+        for (;;) {
+            if (pi >= nprog) return false;
+            const uint32_t t = started ? i + 1 : 0;
+            if (t < (pi == 0 ? ta : tb).ntiles) {
+                i = t;
+                return true;
+            }
+            ++pi;
+            started = false;
+        }
+    };
+
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     sync_tc();
     const uint32_t tbase = *taddr_slot;
-    const uint32_t quad = warp % 4, wgroup = warp / 4;      // TMEM lane quadrant, warp group
     const uint32_t taddr = tbase + ((quad * 32u) << 16);    // this warp's TMEM lanes
-    const uint32_t word = quad * 32 + (tid % 32);           // this thread's word of a tile
-    // f32 <- bf16 x bf16, both K-major, N = 64, M = 128
-    const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(kTcCands >> 3) << 17) |
-                           ((uint32_t)(kTcWords >> 4) << 24);
 
-    uint32_t parity = 0;
+    uint32_t par_mma = 0, par_load = 0;
     bool failed = false;
     uint64_t s0 = 0, s1 = 0;
-    const int nprog = a.mode == (PFC_FACTORIAL | PFC_COMPOSITORIAL) ? 2 : 1;
-    uint64_t acc = m.one;   // the candidate's accumulator (part 0)
-    for (int pi = 0; pi < nprog && !failed; ++pi) {
-        const Prog<WideWord> &pg = pi == 0 ? a.a : a.b;
-        uint32_t w_first = 0, w_end = 0;
-        if (pg.ngroups) {
-            w_first = __ldg(pg.groups);
-            w_end = __ldg(pg.groups + 3 * (pg.ngroups - 1) + 1);
+    uint64_t P[kTcChains];   // this part's running products (part 0, chain 0: the accumulator)
+#pragma unroll
+    for (int k = 0; k < kTcChains; ++k) P[k] = m.one;
+    uint32_t g = 0;          // first group of the current program whose squarings are still due
+    int fin = 0;             // programs finished
+
+    // the threads' products into part 0's accumulator (uniform: every thread calls it)
+    auto combine = [&]() {
+#pragma unroll
+        for (int k = 1; k < kTcChains; ++k) {
+            P[0] = mulw2(P[0], P[k], m.p, m.q32);
+            P[k] = m.one;
         }
-        uint32_t g = 0;   // first group whose squarings are still due
-        for (uint32_t t0 = w_first; t0 < w_end; t0 += kTcWords) {
-            const uint32_t t1 = min(t0 + kTcWords, w_end);
-            // 1. A tile: word t0 + word as 112 bf16 bytes (zeros past the end);
-            //    the warp groups take alternate groups of 8 bytes
-            {
-                uint32_t limb[kWideLimbs];
-                const bool have = t0 + word < t1;
-                const uint4 *src = reinterpret_cast<const uint4 *>(pg.words + (have ? t0 + word : t0));
-#pragma unroll
-                for (int k = 0; k < kWideLimbs / 4; ++k) {
-                    const uint4 z = have ? __ldg(src + k) : make_uint4(0, 0, 0, 0);
-                    limb[4 * k] = z.x;
-                    limb[4 * k + 1] = z.y;
-                    limb[4 * k + 2] = z.z;
-                    limb[4 * k + 3] = z.w;
-                }
-#pragma unroll
-                for (int k8 = 0; k8 < kTcBytes / 8; ++k8)
-                    if (k8 % kTcGroups == (int)wgroup)
-                        *reinterpret_cast<uint4 *>(sm + kOffA + tile_off(word, k8)) = bf16x8(word_bytes8(limb, k8));
-            }
-            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-            sync_tc();
-            // 2. the tile's products, plane after plane
-            if (tid == 0) {
-                const uint32_t aaddr = smem_u32(sm + kOffA);
-#pragma unroll 1
-                for (int pl = 0; pl < kTcPlanes; ++pl) {
-                    const uint32_t baddr = smem_u32(sm + kOffB + pl * kBPlane);
-#pragma unroll
-                    for (int s = 0; s < kTcBytes / 16; ++s) {
-                        const uint64_t da = mdesc(aaddr + s * 256), db = mdesc(baddr + s * 256);
-                        asm volatile(
-                            "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
-                            "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(tbase + pl * kTcCands),
-                            "l"(da), "l"(db), "r"(idesc), "r"((uint32_t)s)
-                            : "memory");
-                    }
-                }
-                asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
-                                 smem_u32(mbar))
-                             : "memory");
-            }
-            if (!mbar_wait(smem_u32(mbar), parity)) atomicOr(timeout, 1u);
-            parity ^= 1;
-            sync_tc();
-            if (*timeout) {
-                failed = true;
-                break;
-            }
-            // 3. u = T 2^-96 R for this thread's word and its warp group's candidates
-            for (uint32_t cc = wgroup * (kTcCands / kTcGroups); cc < (wgroup + 1) * (kTcCands / kTcGroups); cc += 8) {
-                uint32_t v[kTcPlanes][8];
-                load_sums(taddr, cc, v);
-#pragma unroll
-                for (int j = 0; j < 8; ++j) {
-                    uint32_t e[kTcPlanes];
-#pragma unroll
-                    for (int pl = 0; pl < kTcPlanes; ++pl) e[pl] = f2u23(v[pl][j]);
-                    const uint64_t L = (uint64_t)e[0] + ((uint64_t)e[1] << 8) + ((uint64_t)e[2] << 16) +
-                                       ((uint64_t)e[3] << 24);
-                    const uint64_t H = (uint64_t)e[4] + ((uint64_t)e[5] << 8) + ((uint64_t)e[6] << 16) +
-                                       ((uint64_t)e[7] << 24);
-                    const uint64_t M = (L >> 32) + H;
-                    const uint32_t tw[3] = {(uint32_t)L, (uint32_t)M, (uint32_t)(M >> 32)};
-                    const uint32_t cj = cc + j;
-                    U[cj * kTcWords + word] = mul_wide_word<3>(cand_one[cj], tw, cand_p[cj], cand_q[cj]);
-                }
-            }
-            // 4. the words into each candidate's accumulator, in program order
-            bool inside = false;   // a group starts strictly inside the tile
-            for (uint32_t gg = g; gg < pg.ngroups; ++gg) {
-                const uint32_t b = __ldg(pg.groups + 3 * gg);
-                if (b >= t1) break;
-                if (b > t0) {
-                    inside = true;
-                    break;
-                }
-            }
-            __syncthreads();   // U complete
-            if (prt == 0) {
-                for (; g < pg.ngroups && __ldg(pg.groups + 3 * g) <= t0; ++g)
-                    for (uint32_t k = __ldg(pg.groups + 3 * g + 2); k > 0; --k) acc = Cls64L::sq(m, acc);
-            }
-            if (!inside) {
-                constexpr uint32_t kSpan = kTcWords / kTcParts;
-                const uint32_t lo = t0 + kSpan * prt, hi = min(lo + kSpan, t1);
-                uint64_t P = m.one;
-                for (uint32_t w = lo; w < hi; ++w) P = mulw2(P, U[cl * kTcWords + (w - t0)], m.p, m.q32);
-                if (prt > 0) part[prt * kTcCands + cl] = P;
-                __syncthreads();
-                if (prt == 0) {
-                    acc = mulw2(acc, P, m.p, m.q32);
-#pragma unroll
-                    for (int h = 1; h < kTcParts; ++h) acc = mulw2(acc, part[h * kTcCands + cl], m.p, m.q32);
-                }
-            } else if (prt == 0) {
-                for (uint32_t w = t0; w < t1; ++w) {
-                    for (; g < pg.ngroups && __ldg(pg.groups + 3 * g) <= w; ++g)
-                        for (uint32_t k = __ldg(pg.groups + 3 * g + 2); k > 0; --k) acc = Cls64L::sq(m, acc);
-                    acc = mulw2(acc, U[cl * kTcWords + (w - t0)], m.p, m.q32);
-                }
-            }
-        }
-        if (failed) break;
+        if (prt > 0) part[prt * kTcCands + cl] = P[0];
+        __syncthreads();
         if (prt == 0) {
-            for (; g < pg.ngroups; ++g)   // groups after the last word: squarings only
+#pragma unroll
+            for (int h = 1; h < kTcParts; ++h) P[0] = mulw2(P[0], part[h * kTcCands + cl], m.p, m.q32);
+        } else {
+            P[0] = m.one;
+        }
+        __syncthreads();
+    };
+    // end of program pi: remaining squarings, the power-of-R correction,
+    // result; the combined search's second program (primorial words)
+    // continues from the first's result, so part 0 keeps it
+    auto finish = [&](int pi) {
+        const Prog<WideWord> &pg = pi == 0 ? a.a : a.b;
+        combine();
+        if (prt == 0) {
+            uint64_t acc = P[0];
+            for (; g < pg.ngroups; ++g)
                 for (uint32_t k = __ldg(pg.groups + 3 * g + 2); k > 0; --k) acc = Cls64L::sq(m, acc);
             for (uint32_t k = 0; k < pg.final_sq; ++k) acc = Cls64L::sq(m, acc);
             acc = m.mul(acc, m.mont_R_pow(pg.corr));
             if (nprog == 2 && pi == 0) s1 = acc;
             else s0 = acc;
+            P[0] = acc;
         }
+        g = 0;
+    };
+
+    int cpi = 0;
+    uint32_t ci_t = 0;
+    bool have = next_tile(cpi, ci_t, false);
+    if (have && tid == 0) {
+        load_tile(cpi, ci_t);
+        if (!mbar_wait(smem_u32(mbar_load), par_load)) *timeout = 1;
+        else issue_mma(tbase);
     }
+    par_load ^= 1;
+    while (have) {
+        if (!mbar_wait(smem_u32(mbar_mma), par_mma)) atomicOr(timeout, 1u);
+        par_mma ^= 1;
+        sync_tc();
+        if (*timeout) {
+            failed = true;
+            break;
+        }
+        int npi = cpi;
+        uint32_t ni_t = ci_t;
+        const bool nhave = next_tile(npi, ni_t, true);
+        if (nhave && tid == 0) load_tile(npi, ni_t);   // the A region is free: the products are done
+        // 1. u = T 2^-32 (mod p) for this thread's word and its warp group's candidates
+        for (uint32_t cc = wgroup * (kTcCands / kTcGroups); cc < (wgroup + 1) * (kTcCands / kTcGroups); cc += 8) {
+            uint32_t v[64];
+            load_sums(taddr, cc, v);
+#pragma unroll
+            for (int j = 0; j < 8; ++j) {
+                const uint64_t L = planes4(v[8 * j], v[8 * j + 1], v[8 * j + 2], v[8 * j + 3]);
+                const uint64_t H = planes4(v[8 * j + 4], v[8 * j + 5], v[8 * j + 6], v[8 * j + 7]);
+                // T = L + 2^32 H = tw0 + 2^32 M
+                const uint32_t tw0 = (uint32_t)L;
+                const uint64_t M = (L >> 32) + H;
+                const uint32_t cj = cc + j;
+                const uint64_t pj = cand_p[cj];
+                const uint32_t mm = tw0 * cand_q[cj];
+                // tw0 + lo(mm p0) = 2^32 [tw0 != 0]
+                const uint64_t lo = (uint64_t)mm * (uint32_t)pj;
+                U[cj * kUStride + word] =
+                    M + (uint64_t)mm * (uint32_t)(pj >> 32) + (lo >> 32) + (tw0 != 0 ? 1u : 0u);
+            }
+        }
+        // 2. the next tile's products (TMEM is free once every thread's loads
+        //    above are complete; the bulk copy has had step 1 to land)
+        sync_tc();
+        if (nhave && tid == 0) {
+            if (!mbar_wait(smem_u32(mbar_load), par_load)) *timeout = 1;   // seen after the next wait
+            else issue_mma(tbase);
+        }
+        if (nhave) par_load ^= 1;
+        while (fin < cpi) finish(fin++);   // programs without words
+        // 3. the tile's u into the running products, in segments between the
+        //    group starts inside the tile
+        {
+            const Prog<WideWord> &pg = cpi == 0 ? a.a : a.b;
+            uint32_t first, end;
+            prog_range(pg, first, end);
+            const uint32_t t0 = first + ci_t * kTcWords, t1 = min(t0 + kTcWords, end);
+            uint32_t s = t0;
+            for (;;) {
+                uint32_t k = 0;
+                for (; g < pg.ngroups && __ldg(pg.groups + 3 * g) <= s; ++g) k += __ldg(pg.groups + 3 * g + 2);
+                if (k) {
+                    combine();
+                    if (prt == 0)
+                        for (; k > 0; --k) P[0] = Cls64L::sq(m, P[0]);
+                }
+                const uint32_t e = g < pg.ngroups ? min(t1, __ldg(pg.groups + 3 * g)) : t1;
+                const uint32_t span = (e - s + kTcParts - 1) / kTcParts;
+                const uint32_t lo = min(s + span * prt, e), hi = min(lo + span, e);
+                const uint64_t *row = U + cl * kUStride + (lo - t0);
+                const uint32_t n = hi - lo;
+                uint32_t i = 0;
+                for (; i + kTcChains <= n; i += kTcChains) {
+#pragma unroll
+                    for (int k = 0; k < kTcChains; ++k) P[k] = mulw2(P[k], row[i + k], m.p, m.q32);
+                }
+                for (; i < n; ++i) P[0] = mulw2(P[0], row[i], m.p, m.q32);
+                s = e;
+                if (s >= t1) break;
+            }
+        }
+        if (!nhave || npi != cpi) finish(fin++);
+        cpi = npi;
+        ci_t = ni_t;
+        have = nhave;
+    }
+    if (!failed)
+        while (fin < nprog) finish(fin++);
 
     sync_tc();
     if (failed) {
@@ -360,8 +493,18 @@ __global__ void __launch_bounds__(kTcThreads, 1) setup_tc_kernel(ClassBuf<uint64
     if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tbase), "r"(kTmemCols) : "memory");
 }
 
-// One CTA of 256 threads per 64 candidates, one CTA per SM (shared memory).
-int launch_setup64w_tc(const ClassBuf<uint64_t> &c, const SetupArgs<WideWord> &a, uint32_t *flags, cudaStream_t st) {
+size_t tc_tile_bytes() { return kATile; }
+
+int launch_tc_pack(const WideWord *words, uint32_t first, uint32_t end, uint32_t ntiles, void *out, cudaStream_t st) {
+    if (!ntiles) return 0;
+    const uint32_t n = ntiles * kTcWords * (kTcBytes / 8);
+    tc_pack_kernel<<<(n + 255) / 256, 256, 0, st>>>(words, first, end, ntiles, reinterpret_cast<uint4 *>(out));
+    return 1;
+}
+
+// One CTA of 512 threads per 64 candidates, one CTA per SM (shared memory).
+int launch_setup64w_tc(const ClassBuf<uint64_t> &c, const SetupArgs<WideWord> &a, const TcTiles &ta,
+                       const TcTiles &tb, uint32_t *flags, cudaStream_t st) {
     if (!c.cap) return 0;
     static bool configured[64] = {false};
     int dev = 0;
@@ -372,7 +515,7 @@ int launch_setup64w_tc(const ClassBuf<uint64_t> &c, const SetupArgs<WideWord> &a
             return 0;
         configured[dev] = true;
     }
-    setup_tc_kernel<<<(c.cap + kTcCands - 1) / kTcCands, kTcThreads, kSmemBytes, st>>>(c, a, flags);
+    setup_tc_kernel<<<(c.cap + kTcCands - 1) / kTcCands, kTcThreads, kSmemBytes, st>>>(c, a, ta, tb, flags);
     return 1;
 }
 
