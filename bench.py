@@ -470,16 +470,21 @@ def hit_order(f):
     return f[np.lexsort((f["nc"], f["type"], np.abs(f["nc"].astype(np.int64)), f["p"]))]
 
 
-def mixed_roofline(jobs, outcomes, gpu_s, peaks):
+def mixed_roofline(jobs, outcomes, gpu_s, peaks, tc_s=0.0, setup_tc=True):
     """Multiply-pipe roofline of a batched run: the algorithmic multiplies of
     every search (per candidate: its setup program's table words and squarings
     -- pfc_setup_program_size -- and its walk steps: n for !, composite n for
     the compositorial, prime n for #, both for -! -c), weighted by the measured
     issue rates (IMAD 1, IMAD.WIDE and IMAD.HI by their rates relative to
-    IMAD), over the batch's GPU time.  Per unit (see arith.cuh, walk.cuh):
-    896-bit word 36 IMAD.WIDE + 2 IMAD (class 32), 76 + 3 (class 64 below
-    2^64/3); 64-bit word and class-64 squaring 8 IMAD.WIDE + 2 IMAD; class-32
-    squaring IMAD.WIDE + IMAD + IMAD.HI; walk steps as step_recipe.  Restores,
+    IMAD), over the batch's GPU time (iterations plus the tensor-core setups
+    between them).  Per unit (see arith.cuh, walk.cuh, setup_tc.cu): 896-bit
+    word 36 IMAD.WIDE + 2 IMAD (class 32); class 64 below 2^64/3 76 + 3 on the
+    integer pipe, or with the tensor-core setup 10 + 3 (the one-round
+    reduction of the folded word and the two-round product) with the fold's
+    112 x 8 byte-plane multiply-adds on the tensor pipe, reported apart
+    against the measured dense bf16 peak (fp16 runs at the same rate); 64-bit
+    word and class-64 squaring 8 IMAD.WIDE + 2 IMAD; class-32 squaring
+    IMAD.WIDE + IMAD + IMAD.HI; walk steps as step_recipe.  Restores,
     corrections and replays are overhead, as in the single-search roofline.
     A search whose p range crosses 2^31 or 2^64/3 is counted in the class of
     its upper end."""
@@ -487,7 +492,9 @@ def mixed_roofline(jobs, outcomes, gpu_s, peaks):
     w = peaks["imad"] / peaks["imad_wide"]
     h = peaks["imad"] / peaks["mul_hi"]
     lazy_end = 0x5555555555555556
-    unit = {32: (36 * w + 2, w + 1 + h), 64: (76 * w + 3, 8 * w + 2), 65: (8 * w + 2, 8 * w + 2)}
+    unit = {32: (36 * w + 2, w + 1 + h), 64: ((10 if setup_tc else 76) * w + 3, 8 * w + 2),
+            65: (8 * w + 2, 8 * w + 2)}
+    tc_macs = 0.0
     top = max(s.nmax for s in jobs) + 1
     isp = np.ones(top, dtype=bool)
     isp[:2] = False
@@ -510,13 +517,34 @@ def mixed_roofline(jobs, outcomes, gpu_s, peaks):
         step = sum(k * peaks["imad"] / peaks[name] for name, k in recipe.items())
         cw, cs = unit[cls]
         total += outcomes[i].primecount * (words * cw + sq * cs + steps * step)
+        if cls == 64 and setup_tc:
+            tc_macs += outcomes[i].primecount * words * 112 * 8
+    gpu_s = gpu_s + tc_s
     achieved = total / gpu_s
     return {"bound": "int (multiply pipe)", "achieved": achieved / 1e12, "peak": peaks["imad"] / 1e12,
             "unit": "Tops/s IMAD-equivalent (IMAD.WIDE, IMAD.HI weighted by measured rates)",
             "frac": achieved / peaks["imad"], "traffic": None,
             "kernel": "batch_kernel (every class and kind of the batch, over its GPU time)",
             "alg_ops": total, "gpu_s": gpu_s, "searches_crossing_a_class_boundary": crossing,
-            "peak_source": "measured in this run (pfc_bench_int_peak, 32-bit IMAD chains)"}
+            "peak_source": "measured in this run (pfc_bench_int_peak, 32-bit IMAD chains)",
+            "tensor_setup": tensor_line(2 * tc_macs, tc_s)}
+
+
+def tensor_line(flops, seconds):
+    """The tensor-core setups' fold over their own GPU span, against the
+    measured dense bf16 peak (MEASURED_PEAKS.json, burst)."""
+    if not flops or not seconds:
+        return None
+    peak = None
+    try:
+        with open(os.path.join(os.path.dirname(os.path.abspath(__file__)), "MEASURED_PEAKS.json")) as f:
+            peak = float(json.load(f)["bf16_tflops"])
+    except (OSError, ValueError, KeyError):
+        pass
+    achieved = flops / seconds / 1e12
+    return {"flops": flops, "seconds": seconds, "achieved_tflops": achieved, "peak_tflops": peak,
+            "frac": achieved / peak if peak else None,
+            "peak_source": "MEASURED_PEAKS.json bf16_tflops (burst)" if peak else None}
 
 
 def run_mixed(ctx, njobs, warmup, steps=1, iteration_work=None, peaks=None):
@@ -547,7 +575,8 @@ def run_mixed(ctx, njobs, warmup, steps=1, iteration_work=None, peaks=None):
     same_s = all((out_s[i].term_checksum, out_s[i].primecount) == (out_p[i].term_checksum, out_p[i].primecount)
                  for i in range(len(jobs)))
     lat_p = sv.fcfs_latencies(arrivals, service)
-    roof = mixed_roofline(jobs, out_b, timing["gpu_s"], peaks) if peaks else None
+    roof = mixed_roofline(jobs, out_b, timing["gpu_s"], peaks, tc_s=timing["setup_tc_s"],
+                          setup_tc=ctx.setup_tc) if peaks else None
     return {
         "workload": "first %d of the 512 mixed searches (seed 0)" % len(jobs),
         "pairs": int(pairs),
@@ -558,6 +587,7 @@ def run_mixed(ctx, njobs, warmup, steps=1, iteration_work=None, peaks=None):
         "batched_s": t_b, "plain_s": t_p, "plain_table_build_s": create, "finalize_s": t_fin,
         "finalize_verify": "device",
         "iterations": int(timing["iterations"]), "tasks": int(timing["tasks"]),
+        "batched_time": {k: timing[k] for k in ("gpu_s", "setup_tc_s", "prep_s", "admit_s", "step_s")},
         "iteration_work": iteration_work if iteration_work else "default (1.6e12 candidate-steps, throughput policy)",
         "identical_results": bool(same and same_s),
         "roofline": roof,

@@ -52,7 +52,7 @@ class BatchTimes(ctypes.Structure):
     """pfc_batch_times: where a batch's time went."""
     _fields_ = [("step_s", ctypes.c_double), ("gpu_s", ctypes.c_double), ("gpu32_s", ctypes.c_double),
                 ("gpu64_s", ctypes.c_double), ("prep_s", ctypes.c_double), ("admit_s", ctypes.c_double),
-                ("iterations", ctypes.c_uint64), ("tasks", ctypes.c_uint64)]
+                ("setup_tc_s", ctypes.c_double), ("iterations", ctypes.c_uint64), ("tasks", ctypes.c_uint64)]
 
 
 class PFCError(RuntimeError):
@@ -150,6 +150,8 @@ class Context:
     def __init__(self, device=0, budget=0):
         self.h = ctypes.c_void_p()
         _ck(lib().pfc_ctx_create(device, budget, ctypes.byref(self.h)), "pfc_ctx_create")
+        # the tensor-core setup's state as pfc_ctx_create set it from the environment
+        self.setup_tc = os.environ.get("PFCSIEVE_SETUP_TC", "1")[:1] != "0"
 
     def close(self):
         if self.h:
@@ -201,6 +203,7 @@ class Context:
     def set_setup_tc(self, on):
         """Fold the lazy class-64 setup's table words on the tensor cores (default on)."""
         _ck(lib().pfc_ctx_set_setup_tc(self.h, int(bool(on))), "pfc_ctx_set_setup_tc")
+        self.setup_tc = bool(on)
 
     def set_walk_variant(self, cls, fused, variant):
         _ck(lib().pfc_ctx_set_walk_variant(self.h, cls, int(fused), variant), "pfc_ctx_set_walk_variant")

@@ -385,6 +385,11 @@ struct BatchJob {
     std::vector<WideWord> wordsw;      // class 64 below 2^64/3
     std::vector<SetupSeg> segs32, segs64;
     uint32_t nsetup32 = 0, nsetup64 = 0;
+    // class 64 below 2^64/3 on the tensor cores: the wide programs' groups
+    // (first program's, then the second's) and their shapes
+    bool tc = false;
+    std::vector<uint32_t> tcgroups;
+    uint32_t tc_ng[2] = {0, 0}, tc_fsq[2] = {0, 0}, tc_nw[2] = {0, 0}, tc_end[2] = {0, 0}, tc_ntiles[2] = {0, 0};
     uint64_t c32a = 0, c32b = 0, c64a = 0, c64b = 0;
     uint32_t nwalk = 0;
     bool use32 = false, use64 = false;
@@ -394,6 +399,8 @@ struct BatchJob {
     DArr<uint32_t> d_cmult, d_qlist;
     DArr<uint64_t> d_words64;
     DArr<WideWord> d_wordsw;
+    DArr<uint32_t> d_tcgroups;
+    DArr<uint8_t> d_tct;            // fp16 tiles of the wide programs
     DArr<SetupSeg> d_segs32, d_segs64;
     DevClass<uint32_t> c32;
     DevClass<uint64_t> c64;
@@ -480,6 +487,21 @@ static void prepare_job(BatchJob *j, const std::vector<uint32_t> &cache) {
     j->nsetup64 = wide ? append_prog(aw, 0, j->segs64, j->wordsw) : append_prog(a64, 0, j->segs64, j->words64);
     j->c32a = a32.corr;
     j->c64a = wide ? aw.corr : a64.corr;
+    if (wide) {
+        const HostProg<WideWord> *pr[2] = {&aw, &bw};
+        for (int k = 0; k < (fc ? 2 : 1); ++k) {
+            const std::vector<uint32_t> &gr = pr[k]->groups;
+            j->tcgroups.insert(j->tcgroups.end(), gr.begin(), gr.end());
+            j->tc_ng[k] = (uint32_t)(gr.size() / 3);
+            j->tc_fsq[k] = pr[k]->final_sq;
+            j->tc_nw[k] = (uint32_t)pr[k]->words.size();
+            if (gr.size() >= 3) {
+                j->tc_end[k] = gr[gr.size() - 2];
+                j->tc_ntiles[k] = (j->tc_end[k] - gr[0] + 127) / 128;
+            }
+        }
+        j->tc = true;
+    }
     if (fc) {
         // fork: the compositorial residue is complete here
         j->segs32.push_back({j->nsetup32++, 2u, 0u, 1u});
@@ -562,6 +584,10 @@ struct pfc_batch {
     uint64_t iterations = 0;
     // timing: kernel spans (CUDA events) and host phases (wall clock)
     cudaEvent_t ev_start = nullptr, ev_end[kStreams] = {};
+    cudaEvent_t ev_tc[kStreams] = {};    // tensor-core setups of admitted searches, per stream
+    cudaEvent_t ev_tc0 = nullptr, ev_tc1 = nullptr;   // their span on the context stream
+    bool tc_pending = false;             // a span not yet added to tc_s
+    double tc_s = 0;
     double gpu_s = 0, gpu32_s = 0, gpu64_s = 0, prep_s = 0, admit_s = 0, step_s = 0;
     uint64_t tasks = 0;
     size_t t32_n = 0, t64_n = 0;   // task counts of the iteration in flight
@@ -610,6 +636,8 @@ void release_device(pfc_batch *b, BatchJob *j) {
     j->d_words32.release(c);
     j->d_words64.release(c);
     j->d_wordsw.release(c);
+    j->d_tcgroups.release(c);
+    j->d_tct.release(c);
     j->d_segs32.release(c);
     j->d_segs64.release(c);
     j->d_cmult.release(c);
@@ -648,6 +676,10 @@ int upload_job(pfc_batch *b, BatchJob *j) {
     cudaError_t e = j->d_words32.upload(c, j->words32);
     if (e == cudaSuccess) e = j->d_words64.upload(c, j->words64);
     if (e == cudaSuccess) e = j->d_wordsw.upload(c, j->wordsw);
+    const bool tc = j->tc && j->use64 && c->setup_tc;
+    const size_t tb = tc_tile_bytes(), nt = (size_t)j->tc_ntiles[0] + j->tc_ntiles[1];
+    if (e == cudaSuccess && tc) e = j->d_tcgroups.upload(c, j->tcgroups);
+    if (e == cudaSuccess && tc) e = j->d_tct.alloc(c, std::max<size_t>(nt * tb, 16));
     if (e == cudaSuccess) e = j->d_segs32.upload(c, j->segs32);
     if (e == cudaSuccess) e = j->d_segs64.upload(c, j->segs64);
     if (e == cudaSuccess) e = j->d_cmult.upload(c, j->cmult);
@@ -657,6 +689,15 @@ int upload_job(pfc_batch *b, BatchJob *j) {
     if (e != cudaSuccess) {
         release_device(b, j);
         return cuda_fail(e);
+    }
+    if (tc) {
+        const uint32_t *g = j->tcgroups.data();
+        const uint32_t first_b = j->tc_ng[1] ? g[3 * j->tc_ng[0]] : 0;
+        c->launches += launch_tc_pack(j->d_wordsw.p, j->tc_ng[0] ? g[0] : 0, j->tc_end[0], j->tc_ntiles[0], j->d_tct.p,
+                                      c->st);
+        c->launches += launch_tc_pack(j->d_wordsw.p + j->tc_nw[0], first_b, j->tc_end[1], j->tc_ntiles[1],
+                                      j->d_tct.p + (size_t)j->tc_ntiles[0] * tb, c->st);
+        CK(cudaGetLastError());
     }
     return launch_job_gen(b, j);
 }
@@ -754,7 +795,52 @@ int admit_prepared(pfc_batch *b) {
         c->h2d += sizeof(v32[f]) + sizeof(v64[f]);
     }
     CK(cudaStreamSynchronize(c->st));
+    // class-64 setups below 2^64/3 on the tensor cores, one launch per fresh
+    // search spread over the batch streams; the next iteration, recorded on
+    // the context stream, waits for them, and the searches' class-64
+    // timelines start at their walks
+    if (c->setup_tc) {
+        bool used[pfc_batch::kStreams] = {};
+        int k = 0;
+        CK(cudaEventRecord(b->ev_tc0, c->st));
+        for (BatchJob *j : fresh) {
+            // (a timeline without walk steps keeps its setup windows: the
+            // window that ends it also adds the check terms)
+            if (!j->d_tct.p || !j->n64 || !j->nwalk) continue;
+            const int si = k++ % pfc_batch::kStreams;
+            if (!used[si]) CK(cudaStreamWaitEvent(b->st[si], b->ev_tc0, 0));
+            used[si] = true;
+            SetupArgs<WideWord> sw;
+            memset(&sw, 0, sizeof(sw));
+            sw.mode = j->mode;
+            Prog<WideWord> *pg[2] = {&sw.a, &sw.b};
+            uint32_t goff = 0, woff = 0;
+            for (int q = 0; q < 2; ++q) {
+                pg[q]->words = j->d_wordsw.p + woff;
+                pg[q]->groups = j->d_tcgroups.p + goff;
+                pg[q]->ngroups = j->tc_ng[q];
+                pg[q]->final_sq = j->tc_fsq[q];
+                pg[q]->corr = q == 0 ? j->c64a : j->c64b;
+                goff += 3 * j->tc_ng[q];
+                woff += j->tc_nw[q];
+            }
+            const TcTiles ta{j->d_tct.p, j->tc_ntiles[0]},
+                tb{j->d_tct.p + (size_t)j->tc_ntiles[0] * tc_tile_bytes(), j->tc_ntiles[1]};
+            c->launches += launch_setup64w_tc(j->c64.view(b->stats.p[j->slot].counts + 1), sw, ta, tb,
+                                              &b->stats.p[j->slot].flags, b->st[si]);
+            j->pos64 = j->nsetup64;
+        }
+        for (int si = 0; si < pfc_batch::kStreams; ++si)
+            if (used[si]) {
+                CK(cudaEventRecord(b->ev_tc[si], b->st[si]));
+                CK(cudaStreamWaitEvent(c->st, b->ev_tc[si], 0));
+            }
+        CK(cudaEventRecord(b->ev_tc1, c->st));
+        b->tc_pending = true;
+        CK(cudaGetLastError());
+    }
     for (BatchJob *j : fresh) {
+        free_vec(j->tcgroups);
         free_vec(j->words32);  // on the device now
         free_vec(j->words64);
         free_vec(j->wordsw);
@@ -985,6 +1071,12 @@ int finish_iteration(pfc_batch *b, uint32_t L) {
     pfc_ctx *c = b->ctx;
     CK(cudaStreamSynchronize(c->st));
     ++b->iterations;
+    if (b->tc_pending) {
+        float ms = 0;
+        CK(cudaEventElapsedTime(&ms, b->ev_tc0, b->ev_tc1));
+        b->tc_s += ms * 1e-3;
+        b->tc_pending = false;
+    }
     float ms32 = 0, ms64 = 0;
     for (int i = 0; i < pfc_batch::kStreams; ++i) {
         if (!b->used[i]) continue;
@@ -1074,6 +1166,8 @@ int retire_finished(pfc_batch *b) {
             j->status = rerun_alone(b, j);
         } else if (j->flags & 1u) {
             j->status = PFC_ERR_VALIDATION;
+        } else if (j->flags & 2u) {
+            j->status = PFC_ERR_CUDA;   // a tensor-core setup wait gave up
         }
     }
     b->running.swap(still);
@@ -1099,6 +1193,10 @@ extern "C" int pfc_batch_create(pfc_ctx *c, pfc_batch **out) {
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->ev, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreate(&b->ev_start);
     for (int i = 0; i < pfc_batch::kStreams && e == cudaSuccess; ++i) e = cudaEventCreate(&b->ev_end[i]);
+    for (int i = 0; i < pfc_batch::kStreams && e == cudaSuccess; ++i)
+        e = cudaEventCreateWithFlags(&b->ev_tc[i], cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreate(&b->ev_tc0);
+    if (e == cudaSuccess) e = cudaEventCreate(&b->ev_tc1);
     if (e == cudaSuccess) e = b->stats.alloc(c, pfc_batch::kSlots);
     if (e == cudaSuccess) e = b->jobs32.alloc(c, pfc_batch::kSlots);
     if (e == cudaSuccess) e = b->jobs64.alloc(c, pfc_batch::kSlots);
@@ -1141,8 +1239,11 @@ extern "C" int pfc_batch_destroy(pfc_batch *b) {
     if (b->h_hitcount) cudaFreeHost(b->h_hitcount);
     if (b->ev) cudaEventDestroy(b->ev);
     if (b->ev_start) cudaEventDestroy(b->ev_start);
+    if (b->ev_tc0) cudaEventDestroy(b->ev_tc0);
+    if (b->ev_tc1) cudaEventDestroy(b->ev_tc1);
     for (int i = 0; i < pfc_batch::kStreams; ++i) {
         if (b->ev_end[i]) cudaEventDestroy(b->ev_end[i]);
+        if (b->ev_tc[i]) cudaEventDestroy(b->ev_tc[i]);
         if (b->st[i]) cudaStreamDestroy(b->st[i]);
     }
     delete b;
@@ -1267,6 +1368,7 @@ extern "C" int pfc_batch_timing(pfc_batch *b, pfc_batch_times *t) {
     t->gpu64_s = b->gpu64_s;
     t->prep_s = b->prep_s;
     t->admit_s = b->admit_s;
+    t->setup_tc_s = b->tc_s;
     t->iterations = b->iterations;
     t->tasks = b->tasks;
     return PFC_OK;

@@ -84,6 +84,46 @@ def test_batch_matches_oracle_on_small_cases(ctx):
             assert np.array_equal(hits, ohits), case
 
 
+# class 64 below 2^64/3: the batch sets these searches up on the tensor cores
+# at admission (one launch per search) and walks them in its windows
+TC_MIX = [MIX[2], MIX[5], MIX[10], MIX[11],
+          (5, 30000, 33000, 2**45, 2**45 + 2 * 10**6),
+          (4, 101, 50000, 2**55, 2**55 + 10**6),
+          (2, 60000, 60300, 2**50, 2**50 + 10**6)]   # a primorial n range without primes: setup windows
+
+
+def test_batch_tensor_core_setup_equals_the_integer_setup(ctx):
+    """Searches of the lazy class-64 range in a batch whose context sets them
+    up on the tensor cores give exactly what they give alone with the
+    integer-pipe setup."""
+    with pfc.Context(0) as ref:
+        ref.set_setup_tc(False)
+        want = [alone(ref, case) for case in TC_MIX]
+    with pfc.Batch(ctx) as b:
+        ids = [b.submit(*c) for c in TC_MIX]
+        b.run()
+        for case, jid, w in zip(TC_MIX, ids, want):
+            got = batched(b, jid)
+            assert got[:2] == w[:2], case
+            assert np.array_equal(got[2], w[2]), case
+
+
+def test_batch_tensor_core_setup_matches_the_oracle(ctx):
+    cases = [(1, 3000, 3400, 2**40, 2**40 + 2 * 10**5), (5, 1500, 1800, 2**47, 2**47 + 10**5),
+             (2, 4000, 4600, 2**61, 2**61 + 10**5)]
+    with pfc.Batch(ctx) as b:
+        ids = [b.submit(*c) for c in cases]
+        b.run()
+        for case, jid in zip(cases, ids):
+            termsum, count, hits = batched(b, jid)
+            mode, nmin, nmax, pmin, pmax = case
+            cands = o.candidates(pmin, pmax)
+            ohits, oterm, _ = o.sieve(mode, nmin, nmax, cands, threads=THREADS)
+            assert count == len(cands), case
+            assert termsum == oterm, case
+            assert np.array_equal(hits, ohits), case
+
+
 def test_jobs_joining_a_running_batch(ctx):
     """Continuous batching: searches submitted between iterations start at
     the next one and still give their stand-alone results."""
@@ -184,7 +224,9 @@ def test_memory_budget_admission():
     equals the stand-alone one."""
     cases = [(1, 2000, 6000, 2**40 + k * 10**8, 2**40 + k * 10**8 + 2 * 10**7) for k in range(6)]
     with pfc.Context(0, budget=96 << 20) as small:
-        with pfc.Batch(small) as b:
+        # iterations short enough that the admitted searches are still
+        # running while the others wait for their memory
+        with pfc.Batch(small, iteration_work=5e8) as b:
             ids = [b.submit(*c) for c in cases]
             max_active, saw_queue = 0, False
             while True:

@@ -82,13 +82,22 @@ def test_batched_roofline_counts():
             S(4, 5000, 6000, 2**40, 2**40 + 10**6),          # class 64 below 2^64/3, composite n only
             S(2, 5000, 6000, 2**63 + 10**6, 2**63 + 2 * 10**6)]  # class 64 above 2^64/3, prime n only
     out = {i: types.SimpleNamespace(primecount=100 + i) for i in range(3)}
-    r = bench.mixed_roofline(jobs, out, 2.0, peaks)
     primes = sum(1 for q in range(5000, 6000) if all(q % d for d in range(2, int(q ** 0.5) + 1)))
     w1, s1 = pfc.setup_program_size(1, 5000)
     w4, s4 = pfc.setup_program_size(4, 5000)
     w2, s2 = pfc.setup_program_size(2, 5000, wide=False)
-    want = (100 * (w1 * (36 * w + 2) + s1 * (w + 1 + h) + 1000 * (2 * w + 1))
-            + 101 * (w4 * (76 * w + 3) + s4 * (8 * w + 2) + (1000 - primes) * (4 * w + 1))
-            + 102 * (w2 * (8 * w + 2) + s2 * (8 * w + 2) + primes * (7 * w + 2)))
-    assert abs(r["alg_ops"] - want) < 1e-6 * want
-    assert abs(r["frac"] - want / 2.0 / 20e12) < 1e-9
+    for setup_tc, word64 in ((False, 76), (True, 10)):
+        # with the tensor-core setup the class-64 word's fold leaves the
+        # integer pipe (10 IMAD.WIDE + 3 IMAD remain) and its GPU span joins
+        tc_s = 0.5 if setup_tc else 0.0
+        r = bench.mixed_roofline(jobs, out, 2.0, peaks, tc_s=tc_s, setup_tc=setup_tc)
+        want = (100 * (w1 * (36 * w + 2) + s1 * (w + 1 + h) + 1000 * (2 * w + 1))
+                + 101 * (w4 * (word64 * w + 3) + s4 * (8 * w + 2) + (1000 - primes) * (4 * w + 1))
+                + 102 * (w2 * (8 * w + 2) + s2 * (8 * w + 2) + primes * (7 * w + 2)))
+        assert abs(r["alg_ops"] - want) < 1e-6 * want
+        assert abs(r["frac"] - want / (2.0 + tc_s) / 20e12) < 1e-9
+        if setup_tc:
+            assert r["tensor_setup"]["flops"] == 2 * 101 * w4 * 112 * 8
+            assert abs(r["tensor_setup"]["achieved_tflops"] - 2 * 101 * w4 * 112 * 8 / 0.5 / 1e12) < 1e-12
+        else:
+            assert r["tensor_setup"] is None
