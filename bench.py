@@ -470,14 +470,14 @@ def hit_order(f):
     return f[np.lexsort((f["nc"], f["type"], np.abs(f["nc"].astype(np.int64)), f["p"]))]
 
 
-def mixed_roofline(jobs, outcomes, gpu_s, peaks, tc_s=0.0, setup_tc=True):
+def mixed_roofline(jobs, outcomes, seconds, peaks, tc_s=0.0, setup_tc=True):
     """Multiply-pipe roofline of a batched run: the algorithmic multiplies of
     every search (per candidate: its setup program's table words and squarings
     -- pfc_setup_program_size -- and its walk steps: n for !, composite n for
     the compositorial, prime n for #, both for -! -c), weighted by the measured
     issue rates (IMAD 1, IMAD.WIDE and IMAD.HI by their rates relative to
-    IMAD), over the batch's GPU time (iterations plus the tensor-core setups
-    between them).  Per unit (see arith.cuh, walk.cuh, setup_tc.cu): 896-bit
+    IMAD), over the batch's wall time inside pfc_batch_step (iterations and
+    the tensor-core setups of admitted searches overlap).  Per unit (see arith.cuh, walk.cuh, setup_tc.cu): 896-bit
     word 36 IMAD.WIDE + 2 IMAD (class 32); class 64 below 2^64/3 76 + 3 on the
     integer pipe, or with the tensor-core setup 10 + 3 (the one-round
     reduction of the folded word and the two-round product) with the fold's
@@ -519,20 +519,20 @@ def mixed_roofline(jobs, outcomes, gpu_s, peaks, tc_s=0.0, setup_tc=True):
         total += outcomes[i].primecount * (words * cw + sq * cs + steps * step)
         if cls == 64 and setup_tc:
             tc_macs += outcomes[i].primecount * words * 112 * 8
-    gpu_s = gpu_s + tc_s
-    achieved = total / gpu_s
+    achieved = total / seconds
     return {"bound": "int (multiply pipe)", "achieved": achieved / 1e12, "peak": peaks["imad"] / 1e12,
             "unit": "Tops/s IMAD-equivalent (IMAD.WIDE, IMAD.HI weighted by measured rates)",
             "frac": achieved / peaks["imad"], "traffic": None,
-            "kernel": "batch_kernel (every class and kind of the batch, over its GPU time)",
-            "alg_ops": total, "gpu_s": gpu_s, "searches_crossing_a_class_boundary": crossing,
+            "kernel": "batch_kernel and setup_tc_kernel (every class and kind of the batch, over its wall time)",
+            "alg_ops": total, "seconds": seconds, "searches_crossing_a_class_boundary": crossing,
             "peak_source": "measured in this run (pfc_bench_int_peak, 32-bit IMAD chains)",
-            "tensor_setup": tensor_line(2 * tc_macs, tc_s)}
+            "tensor_setup": tensor_line(2 * tc_macs, seconds)}
 
 
 def tensor_line(flops, seconds):
-    """The tensor-core setups' fold over their own GPU span, against the
-    measured dense bf16 peak (MEASURED_PEAKS.json, burst)."""
+    """The tensor-core setups' fold over the batch's wall time (the setups
+    overlap the iterations), against the measured dense bf16 peak
+    (MEASURED_PEAKS.json, burst)."""
     if not flops or not seconds:
         return None
     peak = None
@@ -575,7 +575,7 @@ def run_mixed(ctx, njobs, warmup, steps=1, iteration_work=None, peaks=None):
     same_s = all((out_s[i].term_checksum, out_s[i].primecount) == (out_p[i].term_checksum, out_p[i].primecount)
                  for i in range(len(jobs)))
     lat_p = sv.fcfs_latencies(arrivals, service)
-    roof = mixed_roofline(jobs, out_b, timing["gpu_s"], peaks, tc_s=timing["setup_tc_s"],
+    roof = mixed_roofline(jobs, out_b, timing["step_s"], peaks, tc_s=timing["setup_tc_s"],
                           setup_tc=ctx.setup_tc) if peaks else None
     return {
         "workload": "first %d of the 512 mixed searches (seed 0)" % len(jobs),

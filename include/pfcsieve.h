@@ -384,7 +384,8 @@ typedef struct {
     double gpu32_s, gpu64_s;/* per size class (the two class kernels overlap) */
     double prep_s;          /* host tables of new searches (overlaps the kernels) */
     double admit_s;         /* uploads and candidate generation of new searches */
-    double setup_tc_s;      /* tensor-core setups of new searches (GPU span, between iterations) */
+    double setup_tc_s;      /* tensor-core setups of new searches: summed GPU spans (throughput
+                               policy: overlapping the iterations; latency: chunks before them) */
     uint64_t iterations, tasks;
 } pfc_batch_times;
 int pfc_batch_timing(pfc_batch *b, pfc_batch_times *t);

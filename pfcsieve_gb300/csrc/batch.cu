@@ -33,6 +33,7 @@
 #include <deque>
 #include <map>
 #include <memory>
+#include <thread>
 #include <vector>
 
 #ifdef _OPENMP
@@ -388,6 +389,13 @@ struct BatchJob {
     // class 64 below 2^64/3 on the tensor cores: the wide programs' groups
     // (first program's, then the second's) and their shapes
     bool tc = false;
+    bool tc_wait = false;            // its class-64 setup is still running (no class-64 window yet)
+    cudaEvent_t tc_ev0 = nullptr, tc_ev1 = nullptr;   // around that setup (throughput policy)
+    SetupArgs<WideWord> tc_args{};   // the setup launch (programs, tiles)
+    TcTiles tc_ta{}, tc_tb{};
+    uint32_t tc_block = 0, tc_blocks = 0;   // latency policy: next candidate block, blocks in all
+    uint64_t tc_iter = 0;            // iteration that launched the last blocks
+    double tc_block_cost = 0;        // budget units (multiplies) per block
     std::vector<uint32_t> tcgroups;
     uint32_t tc_ng[2] = {0, 0}, tc_fsq[2] = {0, 0}, tc_nw[2] = {0, 0}, tc_end[2] = {0, 0}, tc_ntiles[2] = {0, 0};
     uint64_t c32a = 0, c32b = 0, c64a = 0, c64b = 0;
@@ -547,6 +555,13 @@ static void free_vec(std::vector<W> &v) {
 
 using namespace pfc;
 
+// a tensor-core setup tile of one candidate block (128 words x 64
+// candidates, about 9,000 SM cycles) in the budget's units: multiplies at
+// 64 per SM cycle
+constexpr double kTcTileCost = 9000.0 * 64.0;
+// share of a latency-policy iteration's budget given to setup chunks
+constexpr double kTcChunkShare = 0.5;
+
 // default work of one iteration in candidate-steps, per policy
 constexpr double kThroughputIterWork = 1.6e12;
 constexpr double kLatencyIterWork = 5e10;
@@ -584,10 +599,16 @@ struct pfc_batch {
     uint64_t iterations = 0;
     // timing: kernel spans (CUDA events) and host phases (wall clock)
     cudaEvent_t ev_start = nullptr, ev_end[kStreams] = {};
-    cudaEvent_t ev_tc[kStreams] = {};    // tensor-core setups of admitted searches, per stream
-    cudaEvent_t ev_tc0 = nullptr, ev_tc1 = nullptr;   // their span on the context stream
-    bool tc_pending = false;             // a span not yet added to tc_s
-    double tc_s = 0;
+    // tensor-core setups of admitted searches: their own streams, after the
+    // uploads (ev_tc0 on the context stream); iterations do not wait for them
+    static constexpr int kTcStreams = 4;
+    double iter_budget = 0;              // this iteration's budget (multiplies), set by build_tasks
+    cudaEvent_t ev_ck0 = nullptr, ev_ck1 = nullptr;   // around an iteration's setup chunks
+    bool ck_pending = false;
+    cudaStream_t tcst[kTcStreams] = {};
+    cudaEvent_t ev_tc0 = nullptr;
+    int tc_next = 0;
+    double tc_s = 0;                     // summed durations of those setups
     double gpu_s = 0, gpu32_s = 0, gpu64_s = 0, prep_s = 0, admit_s = 0, step_s = 0;
     uint64_t tasks = 0;
     size_t t32_n = 0, t64_n = 0;   // task counts of the iteration in flight
@@ -638,6 +659,10 @@ void release_device(pfc_batch *b, BatchJob *j) {
     j->d_wordsw.release(c);
     j->d_tcgroups.release(c);
     j->d_tct.release(c);
+    if (j->tc_ev0) cudaEventDestroy(j->tc_ev0);
+    if (j->tc_ev1) cudaEventDestroy(j->tc_ev1);
+    j->tc_ev0 = j->tc_ev1 = nullptr;
+    j->tc_wait = false;
     j->d_segs32.release(c);
     j->d_segs64.release(c);
     j->d_cmult.release(c);
@@ -795,22 +820,21 @@ int admit_prepared(pfc_batch *b) {
         c->h2d += sizeof(v32[f]) + sizeof(v64[f]);
     }
     CK(cudaStreamSynchronize(c->st));
-    // class-64 setups below 2^64/3 on the tensor cores, one launch per fresh
-    // search spread over the batch streams; the next iteration, recorded on
-    // the context stream, waits for them, and the searches' class-64
-    // timelines start at their walks
+    // class-64 setups below 2^64/3 on the tensor cores.  The search's
+    // class-64 timeline starts at its walk, which joins the iterations once
+    // the setup has finished (build_tasks).  Throughput policy: one launch per
+    // fresh search on the setup streams, overlapping the iterations.  Latency
+    // policy: the setup runs in chunks of candidate blocks ahead of each
+    // iteration (launch_iteration), within a share of the iteration's
+    // budget, so that small searches are not held up behind large setups.
     if (c->setup_tc) {
-        bool used[pfc_batch::kStreams] = {};
-        int k = 0;
+        bool waited[pfc_batch::kTcStreams] = {};
         CK(cudaEventRecord(b->ev_tc0, c->st));
         for (BatchJob *j : fresh) {
             // (a timeline without walk steps keeps its setup windows: the
             // window that ends it also adds the check terms)
             if (!j->d_tct.p || !j->n64 || !j->nwalk) continue;
-            const int si = k++ % pfc_batch::kStreams;
-            if (!used[si]) CK(cudaStreamWaitEvent(b->st[si], b->ev_tc0, 0));
-            used[si] = true;
-            SetupArgs<WideWord> sw;
+            SetupArgs<WideWord> &sw = j->tc_args;
             memset(&sw, 0, sizeof(sw));
             sw.mode = j->mode;
             Prog<WideWord> *pg[2] = {&sw.a, &sw.b};
@@ -824,19 +848,27 @@ int admit_prepared(pfc_batch *b) {
                 goff += 3 * j->tc_ng[q];
                 woff += j->tc_nw[q];
             }
-            const TcTiles ta{j->d_tct.p, j->tc_ntiles[0]},
-                tb{j->d_tct.p + (size_t)j->tc_ntiles[0] * tc_tile_bytes(), j->tc_ntiles[1]};
-            c->launches += launch_setup64w_tc(j->c64.view(b->stats.p[j->slot].counts + 1), sw, ta, tb,
-                                              &b->stats.p[j->slot].flags, b->st[si]);
+            j->tc_ta = TcTiles{j->d_tct.p, j->tc_ntiles[0]};
+            j->tc_tb = TcTiles{j->d_tct.p + (size_t)j->tc_ntiles[0] * tc_tile_bytes(), j->tc_ntiles[1]};
+            j->tc_blocks = tc_setup_blocks(j->n64);
+            j->tc_block_cost = kTcTileCost * ((double)j->tc_ntiles[0] + j->tc_ntiles[1]);
             j->pos64 = j->nsetup64;
-        }
-        for (int si = 0; si < pfc_batch::kStreams; ++si)
-            if (used[si]) {
-                CK(cudaEventRecord(b->ev_tc[si], b->st[si]));
-                CK(cudaStreamWaitEvent(c->st, b->ev_tc[si], 0));
+            j->tc_wait = true;
+            if (b->policy == PFC_BATCH_LATENCY) {
+                j->tc_block = 0;
+                continue;
             }
-        CK(cudaEventRecord(b->ev_tc1, c->st));
-        b->tc_pending = true;
+            const int si = b->tc_next++ % pfc_batch::kTcStreams;
+            if (!waited[si]) CK(cudaStreamWaitEvent(b->tcst[si], b->ev_tc0, 0));
+            waited[si] = true;
+            CK(cudaEventCreate(&j->tc_ev0));
+            CK(cudaEventCreate(&j->tc_ev1));
+            CK(cudaEventRecord(j->tc_ev0, b->tcst[si]));
+            c->launches += launch_setup64w_tc(j->c64.view(b->stats.p[j->slot].counts + 1), sw, j->tc_ta, j->tc_tb,
+                                              &b->stats.p[j->slot].flags, b->tcst[si]);
+            CK(cudaEventRecord(j->tc_ev1, b->tcst[si]));
+            j->tc_block = j->tc_blocks;
+        }
         CK(cudaGetLastError());
     }
     for (BatchJob *j : fresh) {
@@ -911,7 +943,20 @@ uint32_t build_tasks(pfc_batch *b) {
                                 ? b->work_per_iter
                                 : (b->policy == PFC_BATCH_LATENCY ? kLatencyIterWork : kThroughputIterWork);
     const double budget = per_iter * 6.0;   // candidate-steps -> multiplies
+    b->iter_budget = budget;
     const double cta_share = budget / (3.0 * b->ctx->sms);
+    for (BatchJob *j : b->running) {   // tensor-core setups that have finished
+        if (!j->tc_wait) continue;
+        if (!j->tc_ev1) {   // chunks: done once the iteration that ran the last ones has finished
+            if (j->tc_block >= j->tc_blocks && b->iterations > j->tc_iter) j->tc_wait = false;
+            continue;
+        }
+        const cudaError_t q = cudaEventQuery(j->tc_ev1);
+        if (q == cudaErrorNotReady) continue;
+        float ms = 0;
+        if (q == cudaSuccess && cudaEventElapsedTime(&ms, j->tc_ev0, j->tc_ev1) == cudaSuccess) b->tc_s += ms * 1e-3;
+        j->tc_wait = false;   // an error surfaces at the next synchronisation
+    }
     std::vector<std::pair<double, BatchJob *>> order;
     order.reserve(b->running.size());
     for (BatchJob *j : b->running) {
@@ -931,7 +976,7 @@ uint32_t build_tasks(pfc_batch *b) {
             worst = std::max(worst, std::max(per_cta(j, false, kSetupTask) * c32.setup,
                                              per_cta(j, false, kWalkTask) * c32.walk));
         }
-        if (j->pos64 < j->tot64) {
+        if (j->pos64 < j->tot64 && !j->tc_wait) {
             jrate += j->n64 * (j->pos64 < j->nsetup64 ? c64.setup : c64.walk);
             worst = std::max(worst, per_cta(j, true, kSetupTask) * std::max(c64.setup, c64.walk));
         }
@@ -967,7 +1012,7 @@ uint32_t build_tasks(pfc_batch *b) {
         for (int cls = 0; cls < 2; ++cls) {
             const uint32_t pos = cls ? j->pos64 : j->pos32, tot = cls ? j->tot64 : j->tot32;
             const uint32_t ns = cls ? j->nsetup64 : j->nsetup32, n = cls ? j->n64 : j->n32;
-            if (pos >= tot || n == 0 || j->wait) continue;
+            if (pos >= tot || n == 0 || j->wait || (cls && j->tc_wait)) continue;
             uint32_t hi = (uint32_t)std::min<uint64_t>((uint64_t)pos + (j->win ? j->win : L), tot);
             // a window that reaches the end of the setup stops there: the walk
             // starts in the next iteration, in the walk kernel, and the general
@@ -1017,6 +1062,12 @@ static void launch_list(pfc_batch *b, int l, const JobDev<typename T::W> *jobs, 
     b->ctx->launches++;
 }
 
+bool tc_chunks_pending(const pfc_batch *b) {
+    for (const BatchJob *j : b->running)
+        if (j->tc_wait && !j->tc_ev1 && j->tc_block < j->tc_blocks) return true;
+    return false;
+}
+
 int launch_iteration(pfc_batch *b) {
     pfc_ctx *c = b->ctx;
     for (int l = 0; l < pfc_batch::kLists; ++l)
@@ -1027,6 +1078,31 @@ int launch_iteration(pfc_batch *b) {
             CK(cudaMemcpyAsync(b->wins[l][k].p, b->w[l][k].data(), n * sizeof(Window), cudaMemcpyHostToDevice, c->st));
             c->h2d += n * sizeof(Window);
         }
+    // latency policy: chunks of pending tensor-core setups, smallest first,
+    // ahead of the iteration's windows on the context stream
+    if (tc_chunks_pending(b)) {
+        std::vector<std::pair<double, BatchJob *>> pend;
+        for (BatchJob *j : b->running)
+            if (j->tc_wait && !j->tc_ev1 && j->tc_block < j->tc_blocks)
+                pend.push_back({(j->tc_blocks - j->tc_block) * j->tc_block_cost, j});
+        std::sort(pend.begin(), pend.end(), [](const auto &x, const auto &y) { return x.first < y.first; });
+        double left = b->iter_budget * kTcChunkShare;
+        CK(cudaEventRecord(b->ev_ck0, c->st));
+        for (auto &pj : pend) {
+            BatchJob *j = pj.second;
+            if (left <= 0) break;
+            const double fit = std::floor(left / std::max(j->tc_block_cost, 1.0));
+            const uint32_t n = (uint32_t)std::min<double>(j->tc_blocks - j->tc_block, std::max<double>(fit, c->sms));
+            c->launches += launch_setup64w_tc(j->c64.view(b->stats.p[j->slot].counts + 1), j->tc_args, j->tc_ta,
+                                              j->tc_tb, &b->stats.p[j->slot].flags, c->st, j->tc_block, n);
+            j->tc_block += n;
+            if (j->tc_block >= j->tc_blocks) j->tc_iter = b->iterations;
+            left -= n * j->tc_block_cost;
+        }
+        CK(cudaEventRecord(b->ev_ck1, c->st));
+        b->ck_pending = true;
+        CK(cudaGetLastError());
+    }
     CK(cudaEventRecord(b->ev_start, c->st));
     for (int i = 0; i < pfc_batch::kStreams; ++i) {
         b->used[i] = false;
@@ -1071,11 +1147,11 @@ int finish_iteration(pfc_batch *b, uint32_t L) {
     pfc_ctx *c = b->ctx;
     CK(cudaStreamSynchronize(c->st));
     ++b->iterations;
-    if (b->tc_pending) {
+    if (b->ck_pending) {
         float ms = 0;
-        CK(cudaEventElapsedTime(&ms, b->ev_tc0, b->ev_tc1));
+        CK(cudaEventElapsedTime(&ms, b->ev_ck0, b->ev_ck1));
         b->tc_s += ms * 1e-3;
-        b->tc_pending = false;
+        b->ck_pending = false;
     }
     float ms32 = 0, ms64 = 0;
     for (int i = 0; i < pfc_batch::kStreams; ++i) {
@@ -1187,16 +1263,22 @@ extern "C" int pfc_batch_create(pfc_ctx *c, pfc_batch **out) {
     pfc_batch *b = new (std::nothrow) pfc_batch();
     if (!b) return PFC_ERR_NOMEM;
     b->ctx = c;
-    cudaError_t e = cudaSuccess;
+    // iterations on the highest stream priority, tensor-core setups on the
+    // lowest: a setup CTA holds a whole SM, and under priorities the block
+    // scheduler gives freed SMs to pending iteration CTAs first, so setups
+    // fill the iterations' tails and gaps instead of delaying small searches
+    int least = 0, greatest = 0;
+    cudaError_t e = cudaDeviceGetStreamPriorityRange(&least, &greatest);
     for (int i = 0; i < pfc_batch::kStreams && e == cudaSuccess; ++i)
-        e = cudaStreamCreateWithFlags(&b->st[i], cudaStreamNonBlocking);
+        e = cudaStreamCreateWithPriority(&b->st[i], cudaStreamNonBlocking, greatest);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->ev, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreate(&b->ev_start);
     for (int i = 0; i < pfc_batch::kStreams && e == cudaSuccess; ++i) e = cudaEventCreate(&b->ev_end[i]);
-    for (int i = 0; i < pfc_batch::kStreams && e == cudaSuccess; ++i)
-        e = cudaEventCreateWithFlags(&b->ev_tc[i], cudaEventDisableTiming);
-    if (e == cudaSuccess) e = cudaEventCreate(&b->ev_tc0);
-    if (e == cudaSuccess) e = cudaEventCreate(&b->ev_tc1);
+    for (int i = 0; i < pfc_batch::kTcStreams && e == cudaSuccess; ++i)
+        e = cudaStreamCreateWithPriority(&b->tcst[i], cudaStreamNonBlocking, least);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->ev_tc0, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreate(&b->ev_ck0);
+    if (e == cudaSuccess) e = cudaEventCreate(&b->ev_ck1);
     if (e == cudaSuccess) e = b->stats.alloc(c, pfc_batch::kSlots);
     if (e == cudaSuccess) e = b->jobs32.alloc(c, pfc_batch::kSlots);
     if (e == cudaSuccess) e = b->jobs64.alloc(c, pfc_batch::kSlots);
@@ -1225,6 +1307,8 @@ extern "C" int pfc_batch_destroy(pfc_batch *b) {
     cudaSetDevice(c->device);
     for (int i = 0; i < pfc_batch::kStreams; ++i)
         if (b->st[i]) cudaStreamSynchronize(b->st[i]);
+    for (int i = 0; i < pfc_batch::kTcStreams; ++i)
+        if (b->tcst[i]) cudaStreamSynchronize(b->tcst[i]);
     cudaStreamSynchronize(c->st);
     for (auto &kv : b->all) release_device(b, kv.second.get());
     b->stats.release(c);
@@ -1240,10 +1324,12 @@ extern "C" int pfc_batch_destroy(pfc_batch *b) {
     if (b->ev) cudaEventDestroy(b->ev);
     if (b->ev_start) cudaEventDestroy(b->ev_start);
     if (b->ev_tc0) cudaEventDestroy(b->ev_tc0);
-    if (b->ev_tc1) cudaEventDestroy(b->ev_tc1);
+    if (b->ev_ck0) cudaEventDestroy(b->ev_ck0);
+    if (b->ev_ck1) cudaEventDestroy(b->ev_ck1);
+    for (int i = 0; i < pfc_batch::kTcStreams; ++i)
+        if (b->tcst[i]) cudaStreamDestroy(b->tcst[i]);
     for (int i = 0; i < pfc_batch::kStreams; ++i) {
         if (b->ev_end[i]) cudaEventDestroy(b->ev_end[i]);
-        if (b->ev_tc[i]) cudaEventDestroy(b->ev_tc[i]);
         if (b->st[i]) cudaStreamDestroy(b->st[i]);
     }
     delete b;
@@ -1293,10 +1379,20 @@ extern "C" int pfc_batch_step(pfc_batch *b, uint32_t *active, uint32_t *queued) 
     CK(cudaSetDevice(b->ctx->device));
     const double ts = now_s();
     for (int pass = 0; pass < 2; ++pass) {
-        const uint32_t L = build_tasks(b);
-        bool work = false;
+        uint32_t L = build_tasks(b);
+        bool work = tc_chunks_pending(b);
         for (auto &row : b->ctas)
             for (uint64_t n : row) work |= n > 0;
+        if (!work && pass == 0) {
+            // everything running waits for a tensor-core setup: the call
+            // returns after a short pause (searches submitted meanwhile are
+            // admitted by the next call) instead of blocking on one setup
+            for (BatchJob *j : b->running)
+                if (j->tc_wait) {
+                    std::this_thread::sleep_for(std::chrono::microseconds(200));
+                    break;
+                }
+        }
         if (work) {
             const int rc = launch_iteration(b);
             if (rc) return rc;

@@ -144,8 +144,11 @@ struct TcTiles {
 };
 size_t tc_tile_bytes();
 int launch_tc_pack(const WideWord *words, uint32_t first, uint32_t end, uint32_t ntiles, void *out, cudaStream_t st);
+// (candidate blocks of 64: [block0, block0 + nblocks), nblocks 0 to the end)
+uint32_t tc_setup_blocks(uint32_t cands);
 int launch_setup64w_tc(const ClassBuf<uint64_t> &c, const SetupArgs<WideWord> &a, const TcTiles &ta,
-                       const TcTiles &tb, uint32_t *err, cudaStream_t st);
+                       const TcTiles &tb, uint32_t *err, cudaStream_t st, uint32_t block0 = 0,
+                       uint32_t nblocks = 0);
 // start residues of a split walk: boundary k's into s0/s1 + (k-1) * c.cap
 int launch_split_setup32(const ClassBuf<uint32_t> &c, const SplitSetup<WideWord> &ss, uint32_t *s0, uint32_t *s1,
                          cudaStream_t st);

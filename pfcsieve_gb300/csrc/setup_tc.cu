@@ -199,11 +199,12 @@ __global__ void tc_pack_kernel(const WideWord *words, uint32_t first, uint32_t e
 }
 
 __global__ void __launch_bounds__(kTcThreads, 1) setup_tc_kernel(ClassBuf<uint64_t> c, SetupArgs<WideWord> a,
-                                                                 TcTiles ta, TcTiles tb, uint32_t *flags) {
+                                                                 TcTiles ta, TcTiles tb, uint32_t *flags,
+                                                                 uint32_t block0) {
     extern __shared__ __align__(1024) unsigned char sm[];
     const uint32_t tid = threadIdx.x, warp = tid / 32;
     const uint32_t cnt = min(*c.count, c.cap);
-    const uint32_t c0 = blockIdx.x * kTcCands;
+    const uint32_t c0 = (blockIdx.x + block0) * kTcCands;
     if (c0 >= cnt) return;   // whole CTA idle
 
     uint64_t *U = reinterpret_cast<uint64_t *>(sm + kOffU);
@@ -502,10 +503,16 @@ int launch_tc_pack(const WideWord *words, uint32_t first, uint32_t end, uint32_t
     return 1;
 }
 
-// One CTA of 512 threads per 64 candidates, one CTA per SM (shared memory).
+// One CTA of 512 threads per 64 candidates, one CTA per SM (shared memory);
+// blocks [block0, block0 + nblocks) of the class buffer (nblocks 0: to the end).
+uint32_t tc_setup_blocks(uint32_t cands) { return (cands + kTcCands - 1) / kTcCands; }
+
 int launch_setup64w_tc(const ClassBuf<uint64_t> &c, const SetupArgs<WideWord> &a, const TcTiles &ta,
-                       const TcTiles &tb, uint32_t *flags, cudaStream_t st) {
+                       const TcTiles &tb, uint32_t *flags, cudaStream_t st, uint32_t block0, uint32_t nblocks) {
     if (!c.cap) return 0;
+    const uint32_t all = tc_setup_blocks(c.cap);
+    if (block0 >= all) return 0;
+    if (nblocks == 0 || nblocks > all - block0) nblocks = all - block0;
     static bool configured[64] = {false};
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 0;
@@ -515,7 +522,7 @@ int launch_setup64w_tc(const ClassBuf<uint64_t> &c, const SetupArgs<WideWord> &a
             return 0;
         configured[dev] = true;
     }
-    setup_tc_kernel<<<(c.cap + kTcCands - 1) / kTcCands, kTcThreads, kSmemBytes, st>>>(c, a, ta, tb, flags);
+    setup_tc_kernel<<<nblocks, kTcThreads, kSmemBytes, st>>>(c, a, ta, tb, flags, block0);
     return 1;
 }
 

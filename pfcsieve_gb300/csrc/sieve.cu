@@ -69,14 +69,10 @@ __global__ void __launch_bounds__(256) split_setup_kernel(ClassBuf<typename T::W
 
 // One walk launch over all candidates of a class (see walk_streams): NC
 // candidates per thread (or the two chains of one, FUSED), blocks of B steps.
-// SPLIT: sub-range blockIdx.y of a split walk (kernels.cuh SplitArgs).  The
-// lazy class-64 walk in blocks of 32 is bounded to registers for three CTAs
-// per SM (80 instead of 92, a 20-byte spill): 75.4 ms against 76.9 ms on the
-// primorial search near 2^62.  Split walks are bounded the same way (they
-// reached 99 registers, two CTAs per SM, unbounded).
-template <class T, int NC, bool FUSED, int B, bool SPLIT = false>
-__global__ void __launch_bounds__(256, ((std::is_same<T, Cls64L>::value && B == 32) || SPLIT) ? 3 : 1) walk_kernel(ClassBuf<typename T::W> c, WalkArgs a, HitBuf h,
-                                                   SplitArgs<typename T::W> sp) {
+// SPLIT: sub-range blockIdx.y of a split walk (kernels.cuh SplitArgs).
+template <class T, int NC, bool FUSED, int B, bool SPLIT>
+__device__ __forceinline__ void walk_body(ClassBuf<typename T::W> c, WalkArgs a, HitBuf h,
+                                          SplitArgs<typename T::W> sp) {
     using W = typename T::W;
     constexpr int NS = FUSED ? 2 : NC;   // streams per thread
     const uint32_t cnt = min(*c.count, c.cap);
@@ -139,6 +135,26 @@ __global__ void __launch_bounds__(256, ((std::is_same<T, Cls64L>::value && B == 
             }
     }
 }
+
+// Two kernels over the same body.  walk_kernel carries only the CTA size:
+// with it ptxas settles the fused class-32 walk at 80 registers, three CTAs
+// per SM (stating a minimum of one CTA per SM instead let it take 96, two
+// CTAs: 843 against 793 ms on the combined search).  walk_kernel3 asks for
+// three CTAs per SM: the lazy class-64 walk in blocks of 32 (80 registers
+// instead of 92, a 20-byte spill: 75.4 against 76.9 ms on the primorial
+// search near 2^62) and split walks (99 registers, two CTAs, unbounded).
+template <class T, int NC, bool FUSED, int B, bool SPLIT = false>
+__global__ void __launch_bounds__(256) walk_kernel(ClassBuf<typename T::W> c, WalkArgs a, HitBuf h,
+                                                   SplitArgs<typename T::W> sp) {
+    walk_body<T, NC, FUSED, B, SPLIT>(c, a, h, sp);
+}
+template <class T, int NC, bool FUSED, int B, bool SPLIT = false>
+__global__ void __launch_bounds__(256, 3) walk_kernel3(ClassBuf<typename T::W> c, WalkArgs a, HitBuf h,
+                                                       SplitArgs<typename T::W> sp) {
+    walk_body<T, NC, FUSED, B, SPLIT>(c, a, h, sp);
+}
+template <class T, int B, bool SPLIT>
+constexpr bool walk_bounded() { return (std::is_same<T, Cls64L>::value && B == 32) || SPLIT; }
 
 // Multiplier tables of one chunk [lo, lo + len): the compositorial's (n at
 // composite n, 1 at prime n) when `out` is set and the factorial's (n) when
@@ -307,7 +323,10 @@ static int launch_one(const ClassBuf<typename T::W> &c, const WalkArgs &a, const
     const uint32_t per_block = threads * NC;
     SplitArgs<typename T::W> none{};
     none.n = 1;
-    walk_kernel<T, NC, FUSED, B><<<(c.cap + per_block - 1) / per_block, threads, 0, st>>>(c, a, h, none);
+    if constexpr (walk_bounded<T, B, false>())
+        walk_kernel3<T, NC, FUSED, B><<<(c.cap + per_block - 1) / per_block, threads, 0, st>>>(c, a, h, none);
+    else
+        walk_kernel<T, NC, FUSED, B><<<(c.cap + per_block - 1) / per_block, threads, 0, st>>>(c, a, h, none);
     return 1;
 }
 
@@ -318,7 +337,7 @@ static int launch_split(const ClassBuf<typename T::W> &c, const WalkArgs &a, con
     const unsigned threads = walk_cta_threads(c.cap * sp.n, NC, device_sms());
     const uint32_t per_block = threads * NC;
     const dim3 grid((c.cap + per_block - 1) / per_block, sp.n);
-    walk_kernel<T, NC, FUSED, B, true><<<grid, threads, 0, st>>>(c, a, h, sp);
+    walk_kernel3<T, NC, FUSED, B, true><<<grid, threads, 0, st>>>(c, a, h, sp);
     return 1;
 }
 

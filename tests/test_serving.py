@@ -95,9 +95,9 @@ def test_batched_roofline_counts():
                 + 101 * (w4 * (word64 * w + 3) + s4 * (8 * w + 2) + (1000 - primes) * (4 * w + 1))
                 + 102 * (w2 * (8 * w + 2) + s2 * (8 * w + 2) + primes * (7 * w + 2)))
         assert abs(r["alg_ops"] - want) < 1e-6 * want
-        assert abs(r["frac"] - want / (2.0 + tc_s) / 20e12) < 1e-9
+        assert abs(r["frac"] - want / 2.0 / 20e12) < 1e-9
         if setup_tc:
             assert r["tensor_setup"]["flops"] == 2 * 101 * w4 * 112 * 8
-            assert abs(r["tensor_setup"]["achieved_tflops"] - 2 * 101 * w4 * 112 * 8 / 0.5 / 1e12) < 1e-12
+            assert abs(r["tensor_setup"]["achieved_tflops"] - 2 * 101 * w4 * 112 * 8 / 2.0 / 1e12) < 1e-12
         else:
             assert r["tensor_setup"] is None
