@@ -81,6 +81,16 @@ WORKLOADS = {
                             desc="-# n=[101,1e6) p=[2^62,2^62+5e6)"),
     "combined-small": dict(mode=5, nmin=101, nmax=20000, pmin=10**9, pmax=10**9 + 10**7,
                            desc="-! -c n=[101,20000) p=[1e9,1.01e9)"),
+    # setup-bound searches of class 64 below 2^64/3 (large n0, short n range)
+    # for --setup-ab, and a small one for ncu captures of the setup kernels
+    "setup-factorial": dict(mode=1, nmin=9 * 10**6, nmax=9 * 10**6 + 1000, pmin=2**40, pmax=2**40 + 4 * 10**6,
+                            desc="-! n=[9e6,9e6+1000) p=[2^40,2^40+4e6)"),
+    "setup-combined": dict(mode=5, nmin=5 * 10**6, nmax=5 * 10**6 + 1000, pmin=2**50, pmax=2**50 + 4 * 10**6,
+                           desc="-! -c n=[5e6,5e6+1000) p=[2^50,2^50+4e6)"),
+    "setup-primorial": dict(mode=2, nmin=9 * 10**6, nmax=9 * 10**6 + 1000, pmin=2**62, pmax=2**62 + 4 * 10**6,
+                            desc="-# n=[9e6,9e6+1000) p=[2^62,2^62+4e6)"),
+    "setup-factorial-small": dict(mode=1, nmin=2 * 10**6, nmax=2 * 10**6 + 100, pmin=2**40, pmax=2**40 + 10**6,
+                                  desc="-! n=[2e6,2e6+100) p=[2^40,2^40+1e6)"),
 }
 
 
@@ -102,6 +112,8 @@ def parse():
                     help="searches of the mixed workload (the full set is 512)")
     ap.add_argument("--no-reference-opencl", action="store_true",
                     help="skip timing the reference's OpenCL program")
+    ap.add_argument("--setup-ab", action="store_true",
+                    help="time the setup kernel of the workload with the integer-pipe and the tensor-core fold")
     ap.add_argument("--capture", action="store_true",
                     help="profiling case: two rounds of the stage calls (gen, setup, iterate, check) on the "
                          "workload with the default walk variants and nothing else, for ncu (-s 1 -c 1 on a "
@@ -816,6 +828,44 @@ def run_ours(args, wl, world, rank, local, dist):
         print(json.dumps(line), flush=True)
 
 
+def run_setup_ab(wl, reps=3):
+    """The workload's setup kernel with the table-word fold on the integer
+    pipe and on the tensor cores (pfc_ctx_set_setup_tc): the median of `reps`
+    CUDA-event timings of pfc_setup on the context stream after the same
+    candidate generation, then the whole search, whose totals must agree."""
+    import torch
+
+    import pfcsieve_gb300 as pfc
+    line = {"setup_ab": wl["desc"]}
+    totals = {}
+    for tc in (False, True):
+        with pfc.Context(0) as ctx:
+            ctx.set_setup_tc(tc)
+            stream = torch.cuda.ExternalStream(ctx.stream)
+            with pfc.Job(ctx, wl["mode"], wl["nmin"], wl["nmax"], wl["pmin"], wl["pmax"]) as job:
+                ms = []
+                for _ in range(reps + 1):
+                    job.gen(wl["pmin"], wl["pmax"])
+                    a = torch.cuda.Event(enable_timing=True)
+                    b = torch.cuda.Event(enable_timing=True)
+                    a.record(stream)
+                    job.setup()
+                    b.record(stream)
+                    job.iterate(wl["nmin"], wl["nmax"])
+                    job.check()
+                    job.drain_hits()
+                    torch.cuda.synchronize()
+                    ms.append(a.elapsed_time(b))
+                termsum, count = job.totals()
+        key = "tensor" if tc else "integer"
+        line[key + "_setup_ms"] = float(np.median(ms[1:]))
+        totals[key] = (termsum, count)
+    line["candidates"] = totals["tensor"][1] // (reps + 1)
+    line["identical_totals"] = totals["tensor"] == totals["integer"]
+    line["speedup"] = line["integer_setup_ms"] / line["tensor_setup_ms"]
+    print(json.dumps(line), flush=True)
+
+
 def run_capture(wl):
     """Two rounds of the stage calls on a fresh context, for profilers."""
     import pfcsieve_gb300 as pfc
@@ -835,6 +885,9 @@ def main():
     wl = WORKLOADS[args.workload]
     if args.capture:
         run_capture(wl)
+        return
+    if args.setup_ab:
+        run_setup_ab(wl)
         return
     world, rank, local = dist_env()
     dist = dist_init(world)
