@@ -58,6 +58,7 @@ struct pfc_job {
 
     uint64_t termsum = 0, primecount = 0;
     int stage = 0;              // 0 idle, 1 generated, 2 set up, 3 checked
+    bool stats_fresh = true;    // h_stats mirrors the device stats (no work enqueued since the last read)
     uint32_t next_it = 0;       // next n (or prime index) for pfc_iterate
     uint64_t seg_lo = 0, seg_hi = 0;
     bool use32 = false, use64 = false;   // size classes the segment can hold
@@ -248,6 +249,50 @@ static bool build_progs(unsigned mode, uint32_t startN, const std::vector<uint32
     return build_power_prog(startN, 1, primes, a) && build_product_prog(below, b);
 }
 
+// primes up to lim from the context's list (grown when a larger limit is
+// asked for; callers bound every use by value)
+static const std::vector<uint32_t> &ctx_primes(pfc_ctx *c, uint32_t lim) {
+    if (lim > c->primes_lim || c->primes.empty()) {
+        c->primes = primes_between(2, lim);
+        c->primes_lim = lim;
+    }
+    return c->primes;
+}
+
+// the setup programs of (mode, startN) in the word types asked for, from the
+// context's cache or built into it; nullptr if a program cannot be built
+static std::shared_ptr<const ProgSet> ctx_progs(pfc_ctx *c, unsigned mode, uint32_t startN, bool wide, bool narrow) {
+    const std::pair<unsigned, uint32_t> key(mode, startN);
+    auto it = c->progs.find(key);
+    std::shared_ptr<ProgSet> ps = it != c->progs.end() ? it->second : nullptr;
+    if (ps && (!wide || ps->has_wide) && (!narrow || ps->has_narrow)) return ps;
+    auto fresh = std::make_shared<ProgSet>(ps ? *ps : ProgSet());
+    if ((wide && !fresh->has_wide) || (narrow && !fresh->has_narrow)) {
+        const std::vector<uint32_t> &primes = ctx_primes(c, std::max<uint32_t>(startN, 2));
+        const std::vector<uint32_t> below(primes.begin(), std::upper_bound(primes.begin(), primes.end(), startN));
+        if (wide && !fresh->has_wide) {
+            if (!build_progs(mode, startN, primes, below, fresh->wa, fresh->wb)) return nullptr;
+            fresh->has_wide = true;
+        }
+        if (narrow && !fresh->has_narrow) {
+            if (!build_progs(mode, startN, primes, below, fresh->na, fresh->nb)) return nullptr;
+            fresh->has_narrow = true;
+        }
+    }
+    if (ps) c->prog_bytes -= ps->bytes();
+    else c->prog_order.push_back(key);
+    c->progs[key] = fresh;
+    c->prog_bytes += fresh->bytes();
+    while (c->prog_bytes > pfc_ctx::kProgCacheBytes && c->prog_order.size() > 1) {   // drop the oldest
+        auto old = c->progs.find(c->prog_order.front());
+        if (old->first == key) break;
+        c->prog_bytes -= old->second->bytes();
+        c->progs.erase(old);
+        c->prog_order.pop_front();
+    }
+    return fresh;
+}
+
 extern "C" int pfc_setup_program_size(unsigned mode, uint32_t nmin, int wide, uint64_t *words,
                                       uint64_t *squarings) {
     if (!words || !squarings) return PFC_ERR_ARG;
@@ -297,21 +342,21 @@ extern "C" int pfc_job_create(pfc_ctx *c, unsigned mode, uint32_t nmin, uint32_t
 
     const uint32_t startN = nmin - 1;
     const uint32_t plim = (mode & PFC_COMPOSITORIAL) ? nmax : std::max(startN, nmax - 1);
-    const std::vector<uint32_t> primes = primes_between(2, plim);
-    const std::vector<uint32_t> below(primes.begin(), std::upper_bound(primes.begin(), primes.end(), startN));
-    HostProg<WideWord> a32, b32;
-    HostProg<uint64_t> a64, b64;
-    HostProg<WideWord> aw, bw;
+    const std::vector<uint32_t> &primes = ctx_primes(c, plim);
     const bool need32 = pmin < kClassSplit;
     const bool needw = pmax > kClassSplit && pmin < kLazyEnd;
     const bool need64 = pmax > kLazyEnd;
-    bool ok = (!need32 || build_progs(mode, startN, primes, below, a32, b32)) &&
-              (!needw || build_progs(mode, startN, primes, below, aw, bw)) &&
-              (!need64 || build_progs(mode, startN, primes, below, a64, b64));
-    if (!ok) {
+    // class 32 and class 64 below 2^64/3 share the 896-bit programs
+    const std::shared_ptr<const ProgSet> ps = ctx_progs(c, mode, startN, need32 || needw, need64);
+    if (!ps) {
         delete j;
         return PFC_ERR_ARG;
     }
+    const HostProg<WideWord> empty_w;
+    const HostProg<uint64_t> empty_n;
+    const HostProg<WideWord> &a32 = need32 ? ps->wa : empty_w, &b32 = need32 ? ps->wb : empty_w;
+    const HostProg<WideWord> &aw = needw ? ps->wa : empty_w, &bw = needw ? ps->wb : empty_w;
+    const HostProg<uint64_t> &a64 = need64 ? ps->na : empty_n, &b64 = need64 ? ps->nb : empty_n;
     j->setup_mulmods32 = a32.mulmods() + b32.mulmods();
     j->setup_mulmods64 = need64 ? a64.mulmods() + b64.mulmods() : aw.mulmods() + bw.mulmods();
 
@@ -349,6 +394,7 @@ extern "C" int pfc_job_create(pfc_ctx *c, unsigned mode, uint32_t nmin, uint32_t
         } else {
             e = cudaMallocHost((void **)&j->h_stats, sizeof(SegStats));
         }
+        if (e == cudaSuccess) memset(j->h_stats, 0, sizeof(SegStats));   // mirrors the zeroed device stats
     }
     if (e == cudaSuccess) e = j->hits.alloc(c, 1u << 20);
     if (e == cudaSuccess) e = cudaStreamSynchronize(c->st);
@@ -429,6 +475,7 @@ static int enqueue_gen(pfc_job *j, uint64_t lo, uint64_t hi) {
 extern "C" int pfc_gen_candidates(pfc_job *j, uint64_t p_lo, uint64_t p_hi) {
     if (!j || p_lo < j->pmin || p_hi > j->pmax || p_hi <= p_lo) return PFC_ERR_ARG;
     CK(cudaSetDevice(j->ctx->device));
+    j->stats_fresh = false;
     int rc = ensure_class_caps(j, p_lo, p_hi);
     if (rc) return rc;
     return enqueue_gen(j, p_lo, p_hi);
@@ -492,6 +539,7 @@ extern "C" int pfc_setup(pfc_job *j) {
     if (!j) return PFC_ERR_ARG;
     if (j->stage < 1) return PFC_ERR_STATE;
     CK(cudaSetDevice(j->ctx->device));
+    j->stats_fresh = false;
     return enqueue_setup(j);
 }
 
@@ -651,20 +699,15 @@ static int split_prepare(pfc_job *j) {
                           std::max(j->split_wa.size(), j->split_na.size()) == S - 1 &&
                           memcmp(start, j->split_start, sizeof(uint32_t) * (S + 1)) == 0;
         if (!same) {
-            // the value before each boundary's first multiplier
-            std::vector<uint32_t> startN(S);
-            for (uint32_t k = 1; k < S; ++k)
-                startN[k] = (j->mode == PFC_PRIMORIAL ? j->h_qlist[start[k]] : start[k]) - 1;
-            const std::vector<uint32_t> primes = primes_between(2, startN[S - 1]);
-            std::vector<HostProg<WideWord>> wa(S), wb(S);
-            std::vector<HostProg<uint64_t>> na(S), nb(S);
+            // the value before each boundary's first multiplier; the
+            // boundaries' programs come from the context's cache
+            std::vector<std::shared_ptr<const ProgSet>> ps(S);
             uint64_t cost = 0;
             for (uint32_t k = 1; k < S; ++k) {
-                const std::vector<uint32_t> below(primes.begin(),
-                                                  std::upper_bound(primes.begin(), primes.end(), startN[k]));
-                if (wide && !build_progs(j->mode, startN[k], primes, below, wa[k], wb[k])) return PFC_ERR_ARG;
-                if (narrow && !build_progs(j->mode, startN[k], primes, below, na[k], nb[k])) return PFC_ERR_ARG;
-                cost += wide ? prog_cost(wa[k], wb[k]) : prog_cost(na[k], nb[k]);
+                const uint32_t startN = (j->mode == PFC_PRIMORIAL ? j->h_qlist[start[k]] : start[k]) - 1;
+                ps[k] = ctx_progs(c, j->mode, startN, wide, narrow);
+                if (!ps[k]) return PFC_ERR_ARG;
+                cost += wide ? prog_cost(ps[k]->wa, ps[k]->wb) : prog_cost(ps[k]->na, ps[k]->nb);
             }
             if (cost * 6 > walk) continue;   // boundaries too dear: fewer sub-ranges or none
             for (auto &pg : j->split_wa) pg.release(c);
@@ -677,12 +720,12 @@ static int split_prepare(pfc_job *j) {
             j->split_nb.assign(narrow ? S - 1 : 0, DevProg<uint64_t>());
             for (uint32_t k = 1; k < S; ++k) {
                 if (wide) {
-                    CK(j->split_wa[k - 1].upload(c, wa[k]));
-                    CK(j->split_wb[k - 1].upload(c, wb[k]));
+                    CK(j->split_wa[k - 1].upload(c, ps[k]->wa));
+                    CK(j->split_wb[k - 1].upload(c, ps[k]->wb));
                 }
                 if (narrow) {
-                    CK(j->split_na[k - 1].upload(c, na[k]));
-                    CK(j->split_nb[k - 1].upload(c, nb[k]));
+                    CK(j->split_na[k - 1].upload(c, ps[k]->na));
+                    CK(j->split_nb[k - 1].upload(c, ps[k]->nb));
                 }
             }
             j->split_wide = wide;
@@ -754,6 +797,7 @@ extern "C" int pfc_iterate(pfc_job *j, uint32_t n_lo, uint32_t n_hi) {
     if (!j || n_hi < n_lo) return PFC_ERR_ARG;
     if (j->stage < 2) return PFC_ERR_STATE;
     CK(cudaSetDevice(j->ctx->device));
+    j->stats_fresh = false;
     uint32_t lo = n_lo, hi = n_hi;
     if (j->mode == PFC_PRIMORIAL) {   // n range -> prime index range
         lo = (uint32_t)(std::lower_bound(j->h_qlist.begin(), j->h_qlist.end(), n_lo) - j->h_qlist.begin());
@@ -793,6 +837,7 @@ static int read_stats(pfc_job *j) {
     j->ctx->d2h += sizeof(SegStats);
     CK(cudaMemcpyAsync(j->h_stats, j->stats.p, sizeof(SegStats), cudaMemcpyDeviceToHost, j->ctx->st));
     CK(cudaStreamSynchronize(j->ctx->st));
+    j->stats_fresh = true;
     return PFC_OK;
 }
 
@@ -850,6 +895,7 @@ static int segment_body_stream(pfc_job *j) {
     const int rc = enqueue_segment_body(j);
     if (rc) return rc;
     CK(cudaStreamSynchronize(j->ctx->st));
+    j->stats_fresh = true;
     return PFC_OK;
 }
 
@@ -913,6 +959,7 @@ static int segment_body_graph(pfc_job *j) {
     c->launches += j->graph_kernels;
     c->d2h += sizeof(SegStats);
     CK(cudaStreamSynchronize(c->st));
+    j->stats_fresh = true;
     return PFC_OK;
 }
 
@@ -922,41 +969,48 @@ extern "C" int pfc_segment(pfc_job *j, uint64_t p_lo, uint64_t p_hi) {
     CK(cudaSetDevice(c->device));
     int rc = ensure_class_caps(j, p_lo, p_hi);
     if (rc) return rc;
-    // generate; grow and regenerate if a class overflowed
+    if (!j->stats_fresh) {   // stage calls left work or hits the host has not seen
+        rc = read_stats(j);
+        if (rc) return rc;
+    }
+    // generation and the segment body in one stream sequence (the grids are
+    // sized from the buffer capacities, so no wait for the candidate counts);
+    // a class or the hit list that overflowed is grown and the segment redone
+    // from the hits of earlier segments
+    const unsigned long long hit_base = j->h_stats->hits;
     for (int attempt = 0;; ++attempt) {
         rc = enqueue_gen(j, p_lo, p_hi);
         if (rc) return rc;
-        CK(cudaMemcpyAsync(j->h_stats, j->stats.p, sizeof(SegStats), cudaMemcpyDeviceToHost, c->st));
-        CK(cudaStreamSynchronize(c->st));
-        const uint32_t n32 = j->h_stats->counts[0], n64 = j->h_stats->counts[1];
-        const bool over32 = n32 > (j->c32.p.p ? j->c32.cap : 0);
-        const bool over64 = n64 > (j->c64.p.p ? j->c64.cap : 0);
-        if (!over32 && !over64) break;
-        if (attempt >= 2) return PFC_ERR_CAND_OVERFLOW;
-        if (over32) CK(j->c32.ensure(c, (uint32_t)std::min<uint64_t>(4000000000ull, n32 + n32 / 8 + 1024)));
-        if (over64) CK(j->c64.ensure(c, (uint32_t)std::min<uint64_t>(4000000000ull, n64 + n64 / 8 + 1024)));
-    }
-    rc = split_prepare(j);
-    if (rc) return rc;
-    const unsigned long long hit_base = j->h_stats->hits;
-    for (int attempt = 0;; ++attempt) {
+        rc = split_prepare(j);
+        if (rc) return rc;
         // a graph pays off from the second segment of a job on: capturing and
         // instantiating it costs about as much as one small segment
         rc = (c->graphs && j->segments > 0) ? segment_body_graph(j) : segment_body_stream(j);
         if (rc) return rc;
         j->stage = 2;
         j->next_it = iter_end(j);
+        const uint32_t n32 = j->h_stats->counts[0], n64 = j->h_stats->counts[1];
+        const bool over32 = n32 > (j->c32.p.p ? j->c32.cap : 0);
+        const bool over64 = n64 > (j->c64.p.p ? j->c64.cap : 0);
         const unsigned long long nh = j->h_stats->hits;
-        if (nh <= j->hits.n) break;
-        if (attempt >= 2) return PFC_ERR_HIT_OVERFLOW;
-        // grow the hit list, keep the hits of earlier segments, redo this one
-        DArr<pfc_factor> bigger;
-        CK(bigger.alloc(c, (size_t)(nh + nh / 4 + 4096)));
-        if (hit_base) CK(cudaMemcpyAsync(bigger.p, j->hits.p, hit_base * sizeof(pfc_factor), cudaMemcpyDeviceToDevice, c->st));
-        CK(cudaStreamSynchronize(c->st));
-        j->hits.release(c);
-        j->hits = bigger;
+        const bool overhits = nh > j->hits.n;
+        if (!over32 && !over64 && !overhits) break;
+        if (attempt >= 3) return over32 || over64 ? PFC_ERR_CAND_OVERFLOW : PFC_ERR_HIT_OVERFLOW;
+        if (over32) CK(j->c32.ensure(c, (uint32_t)std::min<uint64_t>(4000000000ull, n32 + n32 / 8 + 1024)));
+        if (over64) CK(j->c64.ensure(c, (uint32_t)std::min<uint64_t>(4000000000ull, n64 + n64 / 8 + 1024)));
+        if (overhits && !over32 && !over64) {
+            // grow the hit list, keep the hits of earlier segments
+            DArr<pfc_factor> bigger;
+            CK(bigger.alloc(c, (size_t)(nh + nh / 4 + 4096)));
+            if (hit_base)
+                CK(cudaMemcpyAsync(bigger.p, j->hits.p, hit_base * sizeof(pfc_factor), cudaMemcpyDeviceToDevice, c->st));
+            CK(cudaStreamSynchronize(c->st));
+            j->hits.release(c);
+            j->hits = bigger;
+        }
         CK(cudaMemcpyAsync(hitcount_ptr(j), &hit_base, sizeof(hit_base), cudaMemcpyHostToDevice, c->st));
+        CK(cudaStreamSynchronize(c->st));
+        j->h_stats->hits = hit_base;
     }
     return commit_segment(j);
 }
@@ -972,8 +1026,10 @@ extern "C" int pfc_drain_hits(pfc_job *j, pfc_factor *buf, size_t cap, size_t *n
     if (!j || !n || (!buf && cap)) return PFC_ERR_ARG;
     pfc_ctx *c = j->ctx;
     CK(cudaSetDevice(c->device));
-    int rc = read_stats(j);
-    if (rc) return rc;
+    if (!j->stats_fresh) {   // after a segment or a check the host copy is current
+        const int rc = read_stats(j);
+        if (rc) return rc;
+    }
     const unsigned long long nh = j->h_stats->hits;
     *n = (size_t)nh;
     if (nh > j->hits.n) return PFC_ERR_HIT_OVERFLOW;   // device list incomplete
@@ -981,11 +1037,13 @@ extern "C" int pfc_drain_hits(pfc_job *j, pfc_factor *buf, size_t cap, size_t *n
     if (copy) {
         c->d2h += copy * sizeof(pfc_factor);
         CK(cudaMemcpyAsync(buf, j->hits.p, copy * sizeof(pfc_factor), cudaMemcpyDeviceToHost, c->st));
-        CK(cudaStreamSynchronize(c->st));
     }
-    if (nh > cap) return PFC_ERR_HIT_OVERFLOW;
-    CK(cudaMemsetAsync(hitcount_ptr(j), 0, sizeof(unsigned long long), c->st));
-    CK(cudaStreamSynchronize(c->st));
+    if (nh > cap) {
+        if (copy) CK(cudaStreamSynchronize(c->st));
+        return PFC_ERR_HIT_OVERFLOW;
+    }
+    if (nh) CK(cudaMemsetAsync(hitcount_ptr(j), 0, sizeof(unsigned long long), c->st));
+    if (copy) CK(cudaStreamSynchronize(c->st));   // buf is filled; the reset is ordered before later work
     j->h_stats->hits = 0;
     return PFC_OK;
 }

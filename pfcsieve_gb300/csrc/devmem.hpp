@@ -5,6 +5,10 @@
 
 #include <algorithm>
 #include <cstdint>
+#include <deque>
+#include <map>
+#include <memory>
+#include <utility>
 #include <vector>
 
 #include "host.hpp"
@@ -36,6 +40,16 @@ struct pfc_ctx {
     uint32_t *vbits = nullptr;
     uint32_t vbits_top = 0;
     size_t vbits_bytes = 0;
+    // host tables kept between the context's jobs: the primes up to the
+    // largest limit asked for so far, and the setup programs per (mode,
+    // startN), oldest dropped first beyond kProgCacheBytes (searches of one n
+    // range over many p ranges, and the split walks' boundaries, reuse them)
+    std::vector<uint32_t> primes;
+    uint32_t primes_lim = 0;
+    std::map<std::pair<unsigned, uint32_t>, std::shared_ptr<pfc::ProgSet>> progs;
+    std::deque<std::pair<unsigned, uint32_t>> prog_order;
+    size_t prog_bytes = 0;
+    static constexpr size_t kProgCacheBytes = 64u << 20;
 };
 
 namespace pfc {

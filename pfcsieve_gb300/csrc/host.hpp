@@ -33,6 +33,20 @@ struct HostProg {
     uint64_t mulmods() const;   // device multiplications per candidate (excl. correction)
 };
 
+// The setup programs of one (mode, startN) in the two word types a context
+// caches (a and b as pfc_job_create builds them; b only for the combined
+// search), each built on first use.
+struct ProgSet {
+    HostProg<WideWord> wa, wb;
+    HostProg<uint64_t> na, nb;
+    bool has_wide = false, has_narrow = false;
+    size_t bytes() const {
+        return (wa.words.size() + wb.words.size()) * sizeof(WideWord) +
+               (na.words.size() + nb.words.size()) * sizeof(uint64_t) +
+               (wa.groups.size() + wb.groups.size() + na.groups.size() + nb.groups.size()) * sizeof(uint32_t);
+    }
+};
+
 // prod over primes q <= startN of q^(e_q - sub), e_q = Legendre exponent of q
 // in startN!, in Horner form over the bits of the exponent.  sub = 0 gives
 // startN!, sub = 1 gives startN!/startN# (the product of the composites).
