@@ -40,8 +40,13 @@ struct pfc_job {
     DevProg<WideWord> a32, b32;   // class 32 (896-bit words)
     DevProg<uint64_t> a64, b64;   // class 64 at or above 2^64/3 (64-bit words)
     DevProg<WideWord> aw, bw;     // class 64 below 2^64/3 (896-bit words)
-    DArr<uint8_t> tct;            // aw, bw as fp16 tiles for the tensor-core setup (packed on first use)
-    uint32_t tc_first[2] = {0, 0}, tc_end[2] = {0, 0}, tc_ntiles[2] = {0, 0};
+    // the tensor-core setup: aw, bw in their paired form (TcProg), packed into
+    // fp16 tiles on first use
+    TcProg tcp[2];
+    DArr<uint8_t> tct;
+    DArr<uint32_t> tc_src, tc_groups;
+    Prog<WideWord> tc_view[2] = {};
+    uint32_t tc_ntiles[2] = {0, 0};
     bool tc_packed = false;
     uint64_t setup_mulmods32 = 0, setup_mulmods64 = 0;
     DArr<uint32_t> primebits;
@@ -219,6 +224,8 @@ static int job_release(pfc_job *j) {
     j->aw.release(c);
     j->bw.release(c);
     j->tct.release(c);
+    j->tc_src.release(c);
+    j->tc_groups.release(c);
     j->primebits.release(c);
     j->qlist.release(c);
     j->cmult.release(c);
@@ -360,13 +367,14 @@ extern "C" int pfc_job_create(pfc_ctx *c, unsigned mode, uint32_t nmin, uint32_t
     j->setup_mulmods32 = a32.mulmods() + b32.mulmods();
     j->setup_mulmods64 = need64 ? a64.mulmods() + b64.mulmods() : aw.mulmods() + bw.mulmods();
 
-    const HostProg<WideWord> *wide[2] = {&aw, &bw};
-    for (int k = 0; k < 2; ++k) {
-        const std::vector<uint32_t> &gr = wide[k]->groups;
-        if (gr.size() >= 3) {
-            j->tc_first[k] = gr[0];
-            j->tc_end[k] = gr[gr.size() - 2];
-            j->tc_ntiles[k] = (j->tc_end[k] - j->tc_first[k] + 127) / 128;
+    if (needw) {
+        const HostProg<WideWord> *wide[2] = {&aw, &bw};
+        for (int k = 0; k < 2; ++k) {
+            if (!build_tc_prog(*wide[k], j->tcp[k])) {
+                delete j;
+                return PFC_ERR_ARG;
+            }
+            j->tc_ntiles[k] = ((uint32_t)j->tcp[k].src.size() + tc_tile_words() - 1) / tc_tile_words();
         }
     }
 
@@ -487,11 +495,27 @@ static int tc_prepare(pfc_job *j) {
     if (j->tc_packed) return PFC_OK;
     pfc_ctx *c = j->ctx;
     const size_t tb = tc_tile_bytes(), na = j->tc_ntiles[0], nb = j->tc_ntiles[1];
+    const TcProg &pa = j->tcp[0], &pb = j->tcp[1];
+    std::vector<uint32_t> src(pa.src), groups(pa.groups);
+    src.insert(src.end(), pb.src.begin(), pb.src.end());
+    groups.insert(groups.end(), pb.groups.begin(), pb.groups.end());
     CK(j->tct.alloc(c, std::max<size_t>((na + nb) * tb, 16)));
-    c->launches += launch_tc_pack(j->aw.words.p, j->tc_first[0], j->tc_end[0], (uint32_t)na, j->tct.p, c->st);
-    c->launches += launch_tc_pack(j->bw.words.p, j->tc_first[1], j->tc_end[1], (uint32_t)nb, j->tct.p + na * tb, c->st);
+    CK(j->tc_src.upload(c, src));
+    CK(j->tc_groups.upload(c, groups));
+    c->launches += launch_tc_pack(j->aw.words.p, j->tc_src.p, (uint32_t)pa.src.size(), (uint32_t)na, j->tct.p, c->st);
+    c->launches += launch_tc_pack(j->bw.words.p, j->tc_src.p + pa.src.size(), (uint32_t)pb.src.size(), (uint32_t)nb,
+                                  j->tct.p + na * tb, c->st);
     CK(cudaGetLastError());
-    j->tc_packed = true;
+    for (int k = 0; k < 2; ++k) {
+        const TcProg &tp = j->tcp[k];
+        Prog<WideWord> &v = j->tc_view[k];
+        v.words = nullptr;
+        v.groups = j->tc_groups.p + (k ? pa.groups.size() : 0);
+        v.ngroups = (uint32_t)(tp.groups.size() / 3);
+        v.final_sq = tp.final_sq;
+        v.corr = tp.corr;
+    }
+    j->tc_packed = true;   // (pageable uploads are staged before the calls return)
     return PFC_OK;
 }
 
@@ -521,8 +545,11 @@ static int enqueue_setup(pfc_job *j) {
             if (rc) return rc;
             const TcTiles ta{j->tct.p, j->tc_ntiles[0]},
                 tb{j->tct.p + (size_t)j->tc_ntiles[0] * tc_tile_bytes(), j->tc_ntiles[1]};
+            SetupArgs<WideWord> stc = sw;
+            stc.a = j->tc_view[0];
+            stc.b = j->tc_view[1];
             CK(cudaMemsetAsync(&j->stats.p->tc_err, 0, sizeof(uint32_t), c->st));
-            c->launches += launch_setup64w_tc(j->c64.view(counts_ptr(j) + 1), sw, ta, tb, &j->stats.p->tc_err, c->st);
+            c->launches += launch_setup64w_tc(j->c64.view(counts_ptr(j) + 1), stc, ta, tb, &j->stats.p->tc_err, c->st);
         } else if (j->seg_hi <= kLazyEnd) {
             c->launches += launch_setup64w(j->c64.view(counts_ptr(j) + 1), sw, c->st);
         } else {

@@ -396,8 +396,12 @@ struct BatchJob {
     uint32_t tc_block = 0, tc_blocks = 0;   // latency policy: next candidate block, blocks in all
     uint64_t tc_iter = 0;            // iteration that launched the last blocks
     double tc_block_cost = 0;        // budget units (multiplies) per block
-    std::vector<uint32_t> tcgroups;
-    uint32_t tc_ng[2] = {0, 0}, tc_fsq[2] = {0, 0}, tc_nw[2] = {0, 0}, tc_end[2] = {0, 0}, tc_ntiles[2] = {0, 0};
+    // (the paired programs, host.hpp TcProg: word sources and groups of the
+    // first program then the second's; tc_nw counts the 896-bit words of the
+    // first program, tc_pw the paired words of each)
+    std::vector<uint32_t> tcsrc, tcgroups;
+    uint32_t tc_ng[2] = {0, 0}, tc_fsq[2] = {0, 0}, tc_nw[2] = {0, 0}, tc_pw[2] = {0, 0}, tc_ntiles[2] = {0, 0};
+    uint64_t tc_corr[2] = {0, 0};
     uint64_t c32a = 0, c32b = 0, c64a = 0, c64b = 0;
     uint32_t nwalk = 0;
     bool use32 = false, use64 = false;
@@ -407,7 +411,7 @@ struct BatchJob {
     DArr<uint32_t> d_cmult, d_qlist;
     DArr<uint64_t> d_words64;
     DArr<WideWord> d_wordsw;
-    DArr<uint32_t> d_tcgroups;
+    DArr<uint32_t> d_tcgroups, d_tcsrc;
     DArr<uint8_t> d_tct;            // fp16 tiles of the wide programs
     DArr<SetupSeg> d_segs32, d_segs64;
     DevClass<uint32_t> c32;
@@ -497,18 +501,22 @@ static void prepare_job(BatchJob *j, const std::vector<uint32_t> &cache) {
     j->c64a = wide ? aw.corr : a64.corr;
     if (wide) {
         const HostProg<WideWord> *pr[2] = {&aw, &bw};
-        for (int k = 0; k < (fc ? 2 : 1); ++k) {
-            const std::vector<uint32_t> &gr = pr[k]->groups;
-            j->tcgroups.insert(j->tcgroups.end(), gr.begin(), gr.end());
-            j->tc_ng[k] = (uint32_t)(gr.size() / 3);
-            j->tc_fsq[k] = pr[k]->final_sq;
-            j->tc_nw[k] = (uint32_t)pr[k]->words.size();
-            if (gr.size() >= 3) {
-                j->tc_end[k] = gr[gr.size() - 2];
-                j->tc_ntiles[k] = (j->tc_end[k] - gr[0] + 127) / 128;
-            }
-        }
         j->tc = true;
+        for (int k = 0; k < (fc ? 2 : 1); ++k) {
+            TcProg tp;
+            if (!build_tc_prog(*pr[k], tp)) {
+                j->tc = false;
+                break;
+            }
+            j->tcsrc.insert(j->tcsrc.end(), tp.src.begin(), tp.src.end());
+            j->tcgroups.insert(j->tcgroups.end(), tp.groups.begin(), tp.groups.end());
+            j->tc_ng[k] = (uint32_t)(tp.groups.size() / 3);
+            j->tc_fsq[k] = tp.final_sq;
+            j->tc_corr[k] = tp.corr;
+            j->tc_nw[k] = (uint32_t)pr[k]->words.size();
+            j->tc_pw[k] = (uint32_t)tp.src.size();
+            j->tc_ntiles[k] = (j->tc_pw[k] + tc_tile_words() - 1) / tc_tile_words();
+        }
     }
     if (fc) {
         // fork: the compositorial residue is complete here
@@ -555,7 +563,7 @@ static void free_vec(std::vector<W> &v) {
 
 using namespace pfc;
 
-// a tensor-core setup tile of one candidate block (128 words x 64
+// a tensor-core setup tile of one candidate block (128 paired words x 32
 // candidates, about 9,000 SM cycles) in the budget's units: multiplies at
 // 64 per SM cycle
 constexpr double kTcTileCost = 9000.0 * 64.0;
@@ -658,6 +666,7 @@ void release_device(pfc_batch *b, BatchJob *j) {
     j->d_words64.release(c);
     j->d_wordsw.release(c);
     j->d_tcgroups.release(c);
+    j->d_tcsrc.release(c);
     j->d_tct.release(c);
     if (j->tc_ev0) cudaEventDestroy(j->tc_ev0);
     if (j->tc_ev1) cudaEventDestroy(j->tc_ev1);
@@ -704,6 +713,7 @@ int upload_job(pfc_batch *b, BatchJob *j) {
     const bool tc = j->tc && j->use64 && c->setup_tc;
     const size_t tb = tc_tile_bytes(), nt = (size_t)j->tc_ntiles[0] + j->tc_ntiles[1];
     if (e == cudaSuccess && tc) e = j->d_tcgroups.upload(c, j->tcgroups);
+    if (e == cudaSuccess && tc) e = j->d_tcsrc.upload(c, j->tcsrc);
     if (e == cudaSuccess && tc) e = j->d_tct.alloc(c, std::max<size_t>(nt * tb, 16));
     if (e == cudaSuccess) e = j->d_segs32.upload(c, j->segs32);
     if (e == cudaSuccess) e = j->d_segs64.upload(c, j->segs64);
@@ -716,12 +726,9 @@ int upload_job(pfc_batch *b, BatchJob *j) {
         return cuda_fail(e);
     }
     if (tc) {
-        const uint32_t *g = j->tcgroups.data();
-        const uint32_t first_b = j->tc_ng[1] ? g[3 * j->tc_ng[0]] : 0;
-        c->launches += launch_tc_pack(j->d_wordsw.p, j->tc_ng[0] ? g[0] : 0, j->tc_end[0], j->tc_ntiles[0], j->d_tct.p,
-                                      c->st);
-        c->launches += launch_tc_pack(j->d_wordsw.p + j->tc_nw[0], first_b, j->tc_end[1], j->tc_ntiles[1],
-                                      j->d_tct.p + (size_t)j->tc_ntiles[0] * tb, c->st);
+        c->launches += launch_tc_pack(j->d_wordsw.p, j->d_tcsrc.p, j->tc_pw[0], j->tc_ntiles[0], j->d_tct.p, c->st);
+        c->launches += launch_tc_pack(j->d_wordsw.p + j->tc_nw[0], j->d_tcsrc.p + j->tc_pw[0], j->tc_pw[1],
+                                      j->tc_ntiles[1], j->d_tct.p + (size_t)j->tc_ntiles[0] * tb, c->st);
         CK(cudaGetLastError());
     }
     return launch_job_gen(b, j);
@@ -838,15 +845,14 @@ int admit_prepared(pfc_batch *b) {
             memset(&sw, 0, sizeof(sw));
             sw.mode = j->mode;
             Prog<WideWord> *pg[2] = {&sw.a, &sw.b};
-            uint32_t goff = 0, woff = 0;
-            for (int q = 0; q < 2; ++q) {
-                pg[q]->words = j->d_wordsw.p + woff;
+            uint32_t goff = 0;
+            for (int q = 0; q < 2; ++q) {   // the paired programs (the tiles hold their words)
+                pg[q]->words = nullptr;
                 pg[q]->groups = j->d_tcgroups.p + goff;
                 pg[q]->ngroups = j->tc_ng[q];
                 pg[q]->final_sq = j->tc_fsq[q];
-                pg[q]->corr = q == 0 ? j->c64a : j->c64b;
+                pg[q]->corr = j->tc_corr[q];
                 goff += 3 * j->tc_ng[q];
-                woff += j->tc_nw[q];
             }
             j->tc_ta = TcTiles{j->d_tct.p, j->tc_ntiles[0]};
             j->tc_tb = TcTiles{j->d_tct.p + (size_t)j->tc_ntiles[0] * tc_tile_bytes(), j->tc_ntiles[1]};
@@ -873,6 +879,7 @@ int admit_prepared(pfc_batch *b) {
     }
     for (BatchJob *j : fresh) {
         free_vec(j->tcgroups);
+        free_vec(j->tcsrc);
         free_vec(j->words32);  // on the device now
         free_vec(j->words64);
         free_vec(j->wordsw);

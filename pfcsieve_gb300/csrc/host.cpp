@@ -169,6 +169,25 @@ static bool finish_prog(HostProg<W> &p) {
     return true;
 }
 
+bool build_tc_prog(const HostProg<WideWord> &p, TcProg &out) {
+    out = TcProg();
+    HostProg<uint64_t> shape;   // the groups of the paired words, for the drift correction
+    for (size_t g = 0; g + 2 < p.groups.size(); g += 3) {
+        const uint32_t b = p.groups[g], e = p.groups[g + 1];
+        const uint32_t first = (uint32_t)out.src.size();
+        for (uint32_t w = b; w < e; w += 2) out.src.push_back(w + 1 < e ? (w | 0x80000000u) : w);
+        shape.groups.push_back(first);
+        shape.groups.push_back((uint32_t)out.src.size());
+        shape.groups.push_back(p.groups[g + 2]);
+    }
+    shape.final_sq = p.final_sq;
+    if (!finish_prog(shape)) return false;
+    out.groups = shape.groups;
+    out.final_sq = shape.final_sq;
+    out.corr = shape.corr;
+    return true;
+}
+
 template <class W>
 bool build_power_prog(uint32_t startN, uint32_t sub, const std::vector<uint32_t> &primes, HostProg<W> &out) {
     out = HostProg<W>();

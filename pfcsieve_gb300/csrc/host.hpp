@@ -33,6 +33,20 @@ struct HostProg {
     uint64_t mulmods() const;   // device multiplications per candidate (excl. correction)
 };
 
+// The tensor-core form of a 896-bit program: within each group, consecutive
+// pairs of words are multiplied into one 1792-bit word (a group's odd last
+// word stays alone), so the device multiplies half as many words into its
+// accumulator.  src[i]: index of the first 896-bit word of word i, with bit 31
+// set when the next word is multiplied in too.  groups, final_sq and corr are
+// those of this word count (each word lowers the power of R by one).
+struct TcProg {
+    std::vector<uint32_t> src;
+    std::vector<uint32_t> groups;
+    uint32_t final_sq = 0;
+    uint64_t corr = 0;
+};
+bool build_tc_prog(const HostProg<WideWord> &p, TcProg &out);
+
 // The setup programs of one (mode, startN) in the two word types a context
 // caches (a and b as pfc_job_create builds them; b only for the combined
 // search), each built on first use.

@@ -134,16 +134,21 @@ int launch_setup64(const ClassBuf<uint64_t> &c, const SetupArgs<uint64_t> &a, cu
 // class 64 below 2^64/3 with 896-bit table words
 int launch_setup64w(const ClassBuf<uint64_t> &c, const SetupArgs<WideWord> &a, cudaStream_t st);
 // the same with the table-word fold on the tensor cores (setup_tc.cu): each
-// program's words first packed once into fp16 byte tiles of 128 words
-// (tc_tile_bytes() each; tile i holds words first + 128 i ..), then the
-// setup over those tiles; a wait that gives up sets *err (the segment then
-// fails with PFC_ERR_CUDA)
+// program in its paired form (host.hpp TcProg: 1792-bit words, each the
+// product of one or two 896-bit words, src[i] = first word | pair << 31)
+// first packed once into fp16 byte tiles of tc_tile_words() words
+// (tc_tile_bytes() each; tile i holds paired words 128 i ..), then the setup
+// over those tiles with the paired programs' groups, final squarings and
+// corrections in `a`; a wait that gives up sets *err (the segment then fails
+// with PFC_ERR_CUDA)
 struct TcTiles {
     const void *tiles;   // device, ntiles * tc_tile_bytes(), 16-byte aligned
     uint32_t ntiles;
 };
 size_t tc_tile_bytes();
-int launch_tc_pack(const WideWord *words, uint32_t first, uint32_t end, uint32_t ntiles, void *out, cudaStream_t st);
+uint32_t tc_tile_words();
+int launch_tc_pack(const WideWord *words, const uint32_t *src, uint32_t nw, uint32_t ntiles, void *out,
+                   cudaStream_t st);
 // (candidate blocks of 64: [block0, block0 + nblocks), nblocks 0 to the end)
 uint32_t tc_setup_blocks(uint32_t cands);
 int launch_setup64w_tc(const ClassBuf<uint64_t> &c, const SetupArgs<WideWord> &a, const TcTiles &ta,

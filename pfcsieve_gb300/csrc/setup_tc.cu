@@ -1,45 +1,51 @@
 // setup_tc.cu -- the setup of class-64 candidates below 2^64/3 (the lazy
 // class) with the table-word fold on the tensor cores (tcgen05).
 //
-// The setup evaluates a program of 896-bit table words Z (products of
-// primes, kernels.cuh Prog) into each candidate's residue.  The costly part
-// on the integer pipe is the fold of each word against the candidate's
-// position residues, T = sum_b z_b w_b with w_b = 2^(8b+32) mod p: an exact
-// integer contraction (words x bytes) x (bytes x candidates).  Here it runs
-// on the tensor cores in fp16 with fp32 accumulation and stays exact:
-//   * a word is its 112 bytes z_b (0..255, exact in fp16);
+// The setup evaluates a program of table words Z (products of primes,
+// kernels.cuh Prog) into each candidate's residue.  The costly part on the
+// integer pipe is the fold of each word against the candidate's position
+// residues, T = sum_b z_b w_b with w_b = 2^(8b+32) mod p: an exact integer
+// contraction (words x bytes) x (bytes x candidates).  Here it runs on the
+// tensor cores in fp16 with fp32 accumulation and stays exact:
+//   * the words are 1792-bit: each is the product of a pair of the program's
+//     896-bit words (host.hpp TcProg), so half as many words reach the
+//     CUDA cores; a word is its 224 bytes z_b (0..255, exact in fp16);
 //   * a candidate's 64-bit residues w_b are split into 8 byte planes
 //     W_a[b] = byte a of w_b (0..255);
-//   * D_a[word, cand] = 2^23 + sum_b z_b W_a[b]: the first MMA of each plane
-//     writes 2048 * 4096 = 2^23 into every sum, and sum_b z_b W_a[b] <=
-//     112 * 255 * 255 < 2^23, so every partial sum is an integer in
-//     [2^23, 2^24), exact in fp32, and the fp32 bits of D_a are
+//   * the bytes are summed in two halves of 112, each into its own fp32
+//     accumulator: D_{a,h}[word, cand] = 2^23 + sum_{b in half h} z_b W_a[b].
+//     The first MMA of each half writes 2048 * 4096 = 2^23 into every sum, and
+//     a half's sum is at most 112 * 255 * 255 < 2^23, so every partial sum is
+//     an integer in [2^23, 2^24), exact in fp32, and the fp32 bits of D are
 //     0x4B000000 + the integer sum;
-//   * T = sum_a (D_a - 2^23) 2^(8a) < 2^79 is assembled on the CUDA cores.
-// The program's words are first laid out as fp16 byte tiles of 128 words
-// (A operand, M = 128, K = 112, the shared-memory image; tc_pack_kernel,
-// once per job).  One CTA of 512 threads owns 64 candidates: their byte
-// planes stay in shared memory as the MMA's B operand, K-major, one 8-row
-// core group per candidate (row = plane), so that one MMA with N = 256 covers
-// 32 candidates x 8 planes and a candidate's 8 sums are adjacent TMEM
-// columns (512 columns, word = TMEM lane; per half of the candidates a bias
-// MMA and seven MMAs of K = 16, 16 per tile).  Per tile t:
+//   * T = sum_a (D_{a,0} + D_{a,1} - 2^24) 2^(8a) < 2^79 is assembled on the
+//     CUDA cores.
+// The programs are first laid out as fp16 byte tiles of 128 words (A operand,
+// M = 128, K = 224, the shared-memory image; tc_pack_kernel multiplies the
+// word pairs, once per job).  One CTA of 512 threads owns 32 candidates:
+// their byte planes stay in shared memory as the MMA's B operand, K-major,
+// one 8-row core group per candidate (row = plane), so that one MMA with
+// N = 256 covers the 32 candidates x 8 planes and a candidate's 8 sums of a
+// half are adjacent TMEM columns (two halves x 256 columns, word = TMEM lane;
+// per half a bias MMA and seven MMAs of K = 16, 16 per tile).  Per tile t:
 //   1. each thread reads one word's sums for a share of the candidates
-//      (tcgen05.ld, 8 candidates x 8 planes per load; the four warps of a
-//      lane quadrant split the candidates), assembles T and reduces it by one
-//      Montgomery round, u = (T + m p) / 2^32 with m = -T p^-1 mod 2^32, so
-//      u = T 2^-32 = Z (mod p) and u < 2^48 + p, stored in shared memory;
+//      (tcgen05.ld, 4 candidates x 8 planes per load and half; the four warps
+//      of a lane quadrant split the candidates), assembles T and reduces it
+//      by one Montgomery round, u = (T + m p) / 2^32 with m = -T p^-1 mod 2^32,
+//      so u = T 2^-32 = Z (mod p) and u < 2^48 + p, stored in shared memory;
 //      meanwhile tile t+1 arrives by one bulk copy (cp.async.bulk);
 //   2. the products of tile t+1 are issued; they run while
-//   3. each candidate's eight threads multiply an eighth of the tile's u into
-//      their running products, two independent chains per thread (two lazy
-//      rounds per product; a product lowers the power of R by one, as a
+//   3. each candidate's sixteen threads multiply a sixteenth of the tile's u
+//      into their running products, two independent chains per thread (two
+//      lazy rounds per product; a product lowers the power of R by one, as a
 //      word on the integer pipe does).  At a group start that carries
 //      squarings (Horner over exponent bits) and at the end of a program the
-//      products are combined into the accumulator, which is then squared.
-// The result equals setup_kernel<Cls64L>'s: same program, exact arithmetic,
-// canonical residues at the end.  Every wait is bounded; after a timeout the
-// kernel sets bit 1 of `flags`, frees its TMEM and stores nothing.
+//      products are combined into the accumulator (a tree over the sixteen
+//      threads), which is then squared.
+// The result equals setup_kernel<Cls64L>'s: the same product of the same
+// words in the same Horner order, exact arithmetic, canonical residues at the
+// end.  Every wait is bounded; after a timeout the kernel sets bit 1 of
+// `flags`, frees its TMEM and stores nothing.
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -51,24 +57,24 @@ namespace {
 
 constexpr int kTcThreads = 512;
 constexpr int kTcGroups = kTcThreads / 128;   // warp groups (each covers the 128 TMEM lanes)
-constexpr int kTcParts = kTcThreads / 64;     // threads per candidate in the products
 constexpr int kTcWords = 128;                 // words per tile: MMA M, TMEM lanes
-constexpr int kTcCands = 64;                  // candidates per CTA
-constexpr int kTcBytes = 112;                 // bytes of a 896-bit word: MMA K
+constexpr int kTcCands = 32;                  // candidates per CTA: N = 32 x 8 planes = 256
+constexpr int kTcParts = kTcThreads / kTcCands;   // threads per candidate in the products
+constexpr int kTcBytes = 224;                 // bytes of a 1792-bit word: MMA K
+constexpr int kTcHalfBytes = kTcBytes / 2;    // bytes summed into one accumulator
 constexpr int kTcPlanes = 8;                  // byte planes of a 64-bit residue
-constexpr int kTcHalf = 32;                   // candidates per MMA: N = 32 x 8 planes = 256
-constexpr int kTcChains = 4;                  // independent product chains per thread
-constexpr uint32_t kRowGroup = (kTcBytes / 8) * 128;              // 1792 B between 8-row core groups
+constexpr int kTcChains = 2;                  // independent product chains per thread
+constexpr uint32_t kRowGroup = (kTcBytes / 8) * 128;              // 3584 B between 8-row core groups
 constexpr uint32_t kBiasRowGroup = 2 * 128;                       // bias tiles: K = 16
-constexpr uint32_t kATile = (kTcWords / 8) * kRowGroup;           // 28,672 B
+constexpr uint32_t kATile = (kTcWords / 8) * kRowGroup;           // 57,344 B
 constexpr uint32_t kBTile = kTcCands * kRowGroup;                 // 114,688 B: row group = candidate
 constexpr uint32_t kUStride = kTcWords + 1;   // u64 per candidate row; odd: column reads hit distinct banks
 constexpr uint32_t kOffA = 0;
 constexpr uint32_t kOffB = kOffA + kATile;
 constexpr uint32_t kOffABias = kOffB + kBTile;                                // 128 x 16, column 0 = 2048
 constexpr uint32_t kOffBBias = kOffABias + (kTcWords / 8) * kBiasRowGroup;    // 256 x 16, column 0 = 4096
-constexpr uint32_t kOffU = kOffBBias + kTcHalf * kBiasRowGroup;               // u64 [64 cands][kUStride]
-constexpr uint32_t kOffPart = kOffU + kTcCands * kUStride * 8;      // u64 [parts][64] running products
+constexpr uint32_t kOffU = kOffBBias + kTcCands * kBiasRowGroup;              // u64 [32 cands][kUStride]
+constexpr uint32_t kOffPart = kOffU + kTcCands * kUStride * 8;      // u64 [parts][32] running products
 constexpr uint32_t kOffCand = kOffPart + kTcParts * kTcCands * 8;   // p (u64) and q (u32) per candidate
 constexpr uint32_t kOffMisc = kOffCand + kTcCands * 16;             // 2 mbarriers, TMEM address, timeout flag
 constexpr uint32_t kSmemBytes = kOffMisc + 64;
@@ -77,7 +83,8 @@ static_assert(kOffB % 16 == 0 && kOffABias % 16 == 0 && kOffBBias % 16 == 0 && k
                   kOffMisc % 8 == 0,
               "setup_tc alignment");
 static_assert(kATile % 16 == 0, "bulk copies move multiples of 16 bytes");
-constexpr uint32_t kTmemCols = 512;           // 64 candidates x 8 planes (column = 8 c + plane)
+static_assert(kTcHalfBytes % 16 == 0 && (kTcParts & (kTcParts - 1)) == 0, "setup_tc shape");
+constexpr uint32_t kTmemCols = 512;           // 2 halves x 32 candidates x 8 planes (column = 256 h + 8 c + plane)
 constexpr long kWaitLimit = 1L << 26;         // mbarrier polls before giving up
 constexpr uint32_t kBiasBits = 0x4B000000u;   // fp32 bits of 2^23
 
@@ -113,16 +120,6 @@ __device__ __forceinline__ uint4 f16x8(uint64_t bytes8) {
                       f16x2_of_bytes<true>(hi));
 }
 
-// bytes 8 k8 .. 8 k8 + 7 of a 896-bit word (32 limbs of 28 bits)
-__device__ __forceinline__ uint64_t word_bytes8(const uint32_t *limb, int k8) {
-    const int bit = 64 * k8, i = bit / 28, o = bit % 28;
-    // bits [bit, bit + 64) lie in limbs i .. i + 3 (o + 64 <= 91 < 112)
-    unsigned __int128 acc = 0;
-    for (int j = 0; j < 4; ++j)
-        if (i + j < kWideLimbs) acc |= (unsigned __int128)limb[i + j] << (28 * j);
-    return (uint64_t)(acc >> o);
-}
-
 __device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity) {
     for (long it = 0; it < kWaitLimit; ++it) {
         uint32_t ok;
@@ -136,32 +133,17 @@ __device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity) {
     return false;
 }
 
-// the sums of this thread's word (TMEM lane) for candidates c0..c0+7:
-// v[8 j + a] = plane a of candidate c0 + j
-__device__ __forceinline__ void load_sums(uint32_t taddr, uint32_t c0, uint32_t (&v)[64]) {
+// 32 columns of this thread's TMEM lane from column `col`
+__device__ __forceinline__ void ld32(uint32_t taddr, uint32_t col, uint32_t (&v)[32]) {
     asm volatile(
-        "tcgen05.ld.sync.aligned.32x32b.x64.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
-        "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31,%32,%33,%34,%35,%36,%37,%38,%39,"
-        "%40,%41,%42,%43,%44,%45,%46,%47,%48,%49,%50,%51,%52,%53,%54,%55,%56,%57,%58,%59,%60,%61,%62,%63}, [%64];"
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+        "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
         : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
           "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15]),
           "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]), "=r"(v[20]), "=r"(v[21]), "=r"(v[22]), "=r"(v[23]),
-          "=r"(v[24]), "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]), "=r"(v[29]), "=r"(v[30]), "=r"(v[31]),
-          "=r"(v[32]), "=r"(v[33]), "=r"(v[34]), "=r"(v[35]), "=r"(v[36]), "=r"(v[37]), "=r"(v[38]), "=r"(v[39]),
-          "=r"(v[40]), "=r"(v[41]), "=r"(v[42]), "=r"(v[43]), "=r"(v[44]), "=r"(v[45]), "=r"(v[46]), "=r"(v[47]),
-          "=r"(v[48]), "=r"(v[49]), "=r"(v[50]), "=r"(v[51]), "=r"(v[52]), "=r"(v[53]), "=r"(v[54]), "=r"(v[55]),
-          "=r"(v[56]), "=r"(v[57]), "=r"(v[58]), "=r"(v[59]), "=r"(v[60]), "=r"(v[61]), "=r"(v[62]), "=r"(v[63])
-        : "r"(taddr + 8 * c0)
+          "=r"(v[24]), "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]), "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
+        : "r"(taddr + col)
         : "memory");
-    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-}
-
-// sum_{a<4} e_a 2^(8a) from the fp32 bits kBiasBits + e_a of four planes
-// (e_a < 2^23: a pair e_0 + e_1 2^8 < 2^32, and the bias of the shifted
-// plane leaves 32 bits)
-__device__ __forceinline__ uint64_t planes4(uint32_t b0, uint32_t b1, uint32_t b2, uint32_t b3) {
-    const uint32_t lo = b0 + (b1 << 8) - kBiasBits, hi = b2 + (b3 << 8) - kBiasBits;
-    return (uint64_t)lo + ((uint64_t)hi << 16);
 }
 
 __device__ __forceinline__ void sync_tc() {
@@ -186,16 +168,46 @@ __device__ __forceinline__ void prog_range(const Prog<WideWord> &pg, uint32_t &f
 
 }  // namespace
 
-// One thread per (tile, word, 8-byte group): the fp16 shared-memory image of
-// the program's words [first, end) in tiles of 128 (zeros past the end).
-__global__ void tc_pack_kernel(const WideWord *words, uint32_t first, uint32_t end, uint32_t ntiles, uint4 *out) {
-    constexpr uint32_t kPer = kTcWords * (kTcBytes / 8);
+// One thread per word slot of a tile: the 1792-bit word (the product of a
+// pair of 896-bit words, or one alone; zero past the end) as 224 fp16 bytes
+// in the tile's shared-memory image.  The product is formed column by column
+// in radix 2^28 (a column sums at most 32 products of 28-bit limbs, below
+// 2^61 with its carry) and written eight bytes at a time.
+__global__ void tc_pack_kernel(const WideWord *words, const uint32_t *src, uint32_t nw, uint32_t ntiles, uint4 *out) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= ntiles * kPer) return;
-    const uint32_t tile = i / kPer, word = (i % kPer) / (kTcBytes / 8), k8 = i % (kTcBytes / 8);
-    const uint32_t w = first + tile * kTcWords + word;
-    const uint64_t bytes = w < end ? word_bytes8(words[w].limb, (int)k8) : 0;
-    out[(tile * kATile + tile_off(word, k8)) / 16] = f16x8(bytes);
+    if (i >= ntiles * kTcWords) return;
+    const uint32_t tile = i / kTcWords, slot = i % kTcWords;
+    uint32_t x[kWideLimbs], y[kWideLimbs];
+    const bool have = i < nw;
+    const uint32_t s = have ? __ldg(src + i) : 0u;
+    const bool pair = have && (s >> 31);
+    const uint32_t w = s & 0x7FFFFFFFu;
+#pragma unroll
+    for (int k = 0; k < kWideLimbs; ++k) {
+        x[k] = have ? words[w].limb[k] : 0u;
+        y[k] = pair ? words[w + 1].limb[k] : (k == 0 ? 1u : 0u);
+    }
+    unsigned char *tb = reinterpret_cast<unsigned char *>(out) + (size_t)tile * kATile;
+    uint64_t carry = 0, bits = 0;
+    int nbits = 0;
+    uint32_t k8 = 0;
+    for (int c = 0; c < 2 * kWideLimbs; ++c) {
+        uint64_t col = carry;
+        for (int a = c < kWideLimbs ? 0 : c - kWideLimbs + 1; a <= c && a < kWideLimbs; ++a)
+            col += (uint64_t)x[a] * y[c - a];
+        const uint64_t limb = col & ((1ull << kWideRadixBits) - 1u);
+        carry = col >> kWideRadixBits;
+        // 28 new bits above the nbits (< 64) already gathered
+        bits |= limb << nbits;
+        if (nbits + kWideRadixBits >= 64) {   // 64 bits complete
+            *reinterpret_cast<uint4 *>(tb + tile_off(slot, k8++)) = f16x8(bits);
+            const int used = 64 - nbits;      // bits of this limb in the completed group
+            bits = used < kWideRadixBits ? limb >> used : 0;
+            nbits = kWideRadixBits - used;
+        } else {
+            nbits += kWideRadixBits;
+        }
+    }
 }
 
 __global__ void __launch_bounds__(kTcThreads, 1) setup_tc_kernel(ClassBuf<uint64_t> c, SetupArgs<WideWord> a,
@@ -241,7 +253,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) setup_tc_kernel(ClassBuf<uint64
     }
 
     // bias tiles: A column 0 = 2048, B column 0 = 4096 (fp16), the rest 0
-    for (uint32_t r = tid; r < kTcWords + 8 * kTcHalf; r += kTcThreads) {
+    for (uint32_t r = tid; r < kTcWords + 8 * kTcCands; r += kTcThreads) {
         const bool isa = r < kTcWords;
         const uint32_t row = isa ? r : r - kTcWords;
         unsigned char *base = sm + (isa ? kOffABias : kOffBBias);
@@ -252,7 +264,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) setup_tc_kernel(ClassBuf<uint64
 
     // B operand: the candidate's residues w_b = 2^(8b+32) mod p as 8 byte
     // planes, the rows of the candidate's core group (each part writes its
-    // share of the 14 groups of 8 bytes, starting from 2^32 256^b0 mod p by
+    // share of the 28 groups of 8 bytes, starting from 2^32 256^b0 mod p by
     // square-and-multiply; the plane order is rotated by the candidate so
     // that a warp's stores spread over the banks)
     {
@@ -290,7 +302,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) setup_tc_kernel(ClassBuf<uint64
     const uint32_t quad = warp % 4, wgroup = warp / 4;      // TMEM lane quadrant, warp group
     const uint32_t word = quad * 32 + (tid % 32);           // this thread's word of a tile
     // f32 <- f16 x f16, both K-major, N = 256, M = 128
-    const uint32_t idesc = (1u << 4) | ((uint32_t)(8 * kTcHalf >> 3) << 17) | ((uint32_t)(kTcWords >> 4) << 24);
+    const uint32_t idesc = (1u << 4) | ((uint32_t)(8 * kTcCands >> 3) << 17) | ((uint32_t)(kTcWords >> 4) << 24);
     const int nprog = a.mode == (PFC_FACTORIAL | PFC_COMPOSITORIAL) ? 2 : 1;
 
     // tile i of program pi into the A region (one thread), completing on mbar_load
@@ -306,25 +318,28 @@ __global__ void __launch_bounds__(kTcThreads, 1) setup_tc_kernel(ClassBuf<uint64
             "l"(src), "r"(kATile), "r"(smem_u32(mbar_load))
             : "memory");
     };
-    // the tile's products, per half of the candidates after its bias product
+    // the tile's products: per half of the bytes, a bias product and seven
+    // K-steps into that half's 256 columns
     auto issue_mma = [&](uint32_t tbase) {
-        const uint32_t aaddr = smem_u32(sm + kOffA), abias = smem_u32(sm + kOffABias),
-                       bbias = smem_u32(sm + kOffBBias);
+        const uint32_t aaddr = smem_u32(sm + kOffA), baddr = smem_u32(sm + kOffB),
+                       abias = smem_u32(sm + kOffABias), bbias = smem_u32(sm + kOffBBias);
 #pragma unroll
-        for (int h = 0; h < kTcCands / kTcHalf; ++h) {
-            const uint32_t baddr = smem_u32(sm + kOffB + h * kTcHalf * kRowGroup), d = tbase + h * 8 * kTcHalf;
+        for (int h = 0; h < 2; ++h) {
+            const uint32_t d = tbase + h * 8 * kTcCands;
             asm volatile(
                 "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, 0, 0;\n\t"
                 "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d),
                 "l"(mdesc(abias, kBiasRowGroup)), "l"(mdesc(bbias, kBiasRowGroup)), "r"(idesc)
                 : "memory");
 #pragma unroll
-            for (int s = 0; s < kTcBytes / 16; ++s)
+            for (int s = 0; s < kTcHalfBytes / 16; ++s) {
+                const uint32_t off = (uint32_t)(h * (kTcHalfBytes / 16) + s) * 256;
                 asm volatile(
                     "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, 1, 0;\n\t"
                     "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d),
-                    "l"(mdesc(aaddr + s * 256, kRowGroup)), "l"(mdesc(baddr + s * 256, kRowGroup)), "r"(idesc)
+                    "l"(mdesc(aaddr + off, kRowGroup)), "l"(mdesc(baddr + off, kRowGroup)), "r"(idesc)
                     : "memory");
+            }
         }
         asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
                          smem_u32(mbar_mma))
@@ -358,22 +373,22 @@ __global__ void __launch_bounds__(kTcThreads, 1) setup_tc_kernel(ClassBuf<uint64
     uint32_t g = 0;          // first group of the current program whose squarings are still due
     int fin = 0;             // programs finished
 
-    // the threads' products into part 0's accumulator (uniform: every thread calls it)
+    // the threads' products into part 0's accumulator, a tree over the parts
+    // (uniform: every thread calls it)
     auto combine = [&]() {
 #pragma unroll
         for (int k = 1; k < kTcChains; ++k) {
             P[0] = mulw2(P[0], P[k], m.p, m.q32);
             P[k] = m.one;
         }
-        if (prt > 0) part[prt * kTcCands + cl] = P[0];
-        __syncthreads();
-        if (prt == 0) {
 #pragma unroll
-            for (int h = 1; h < kTcParts; ++h) P[0] = mulw2(P[0], part[h * kTcCands + cl], m.p, m.q32);
-        } else {
-            P[0] = m.one;
+        for (uint32_t stride = 1; stride < (uint32_t)kTcParts; stride <<= 1) {
+            part[prt * kTcCands + cl] = P[0];
+            __syncthreads();
+            if ((prt & (2 * stride - 1)) == 0) P[0] = mulw2(P[0], part[(prt + stride) * kTcCands + cl], m.p, m.q32);
+            __syncthreads();
         }
-        __syncthreads();
+        if (prt != 0) P[0] = m.one;
     };
     // end of program pi: remaining squarings, the power-of-R correction,
     // result; the combined search's second program (primorial words)
@@ -416,13 +431,22 @@ __global__ void __launch_bounds__(kTcThreads, 1) setup_tc_kernel(ClassBuf<uint64
         const bool nhave = next_tile(npi, ni_t, true);
         if (nhave && tid == 0) load_tile(npi, ni_t);   // the A region is free: the products are done
         // 1. u = T 2^-32 (mod p) for this thread's word and its warp group's candidates
-        for (uint32_t cc = wgroup * (kTcCands / kTcGroups); cc < (wgroup + 1) * (kTcCands / kTcGroups); cc += 8) {
-            uint32_t v[64];
-            load_sums(taddr, cc, v);
+        for (uint32_t cc = wgroup * (kTcCands / kTcGroups); cc < (wgroup + 1) * (kTcCands / kTcGroups); cc += 4) {
+            uint32_t v0[32], v1[32];
+            ld32(taddr, 8 * cc, v0);
+            ld32(taddr, 8 * kTcCands + 8 * cc, v1);
+            asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
-            for (int j = 0; j < 8; ++j) {
-                const uint64_t L = planes4(v[8 * j], v[8 * j + 1], v[8 * j + 2], v[8 * j + 3]);
-                const uint64_t H = planes4(v[8 * j + 4], v[8 * j + 5], v[8 * j + 6], v[8 * j + 7]);
+            for (int j = 0; j < 4; ++j) {
+                // plane sums e_a = D_{a,0} + D_{a,1} - 2^24 < 2^24 (the two bias
+                // patterns add to 2 x 0x4B000000 < 2^32)
+                uint32_t e[kTcPlanes];
+#pragma unroll
+                for (int pl = 0; pl < kTcPlanes; ++pl) e[pl] = v0[8 * j + pl] + v1[8 * j + pl] - 2u * kBiasBits;
+                const uint64_t L = (uint64_t)e[0] + ((uint64_t)e[1] << 8) + ((uint64_t)e[2] << 16) +
+                                   ((uint64_t)e[3] << 24);
+                const uint64_t H = (uint64_t)e[4] + ((uint64_t)e[5] << 8) + ((uint64_t)e[6] << 16) +
+                                   ((uint64_t)e[7] << 24);
                 // T = L + 2^32 H = tw0 + 2^32 M
                 const uint32_t tw0 = (uint32_t)L;
                 const uint64_t M = (L >> 32) + H;
@@ -495,15 +519,17 @@ __global__ void __launch_bounds__(kTcThreads, 1) setup_tc_kernel(ClassBuf<uint64
 }
 
 size_t tc_tile_bytes() { return kATile; }
+uint32_t tc_tile_words() { return kTcWords; }
 
-int launch_tc_pack(const WideWord *words, uint32_t first, uint32_t end, uint32_t ntiles, void *out, cudaStream_t st) {
+int launch_tc_pack(const WideWord *words, const uint32_t *src, uint32_t nw, uint32_t ntiles, void *out,
+                   cudaStream_t st) {
     if (!ntiles) return 0;
-    const uint32_t n = ntiles * kTcWords * (kTcBytes / 8);
-    tc_pack_kernel<<<(n + 255) / 256, 256, 0, st>>>(words, first, end, ntiles, reinterpret_cast<uint4 *>(out));
+    const uint32_t n = ntiles * kTcWords;
+    tc_pack_kernel<<<(n + 127) / 128, 128, 0, st>>>(words, src, nw, ntiles, reinterpret_cast<uint4 *>(out));
     return 1;
 }
 
-// One CTA of 512 threads per 64 candidates, one CTA per SM (shared memory);
+// One CTA of 512 threads per 32 candidates, one CTA per SM (shared memory);
 // blocks [block0, block0 + nblocks) of the class buffer (nblocks 0: to the end).
 uint32_t tc_setup_blocks(uint32_t cands) { return (cands + kTcCands - 1) / kTcCands; }
 
