@@ -35,7 +35,8 @@
 //      so u = T 2^-32 = Z (mod p) and u < 2^48 + p, stored in shared memory;
 //      meanwhile tile t+1 arrives by one bulk copy (cp.async.bulk);
 //   2. the products of tile t+1 are issued; they run while
-//   3. each candidate's sixteen threads multiply a sixteenth of the tile's u
+//   3. fifteen threads of each candidate (one per warp but the first, whose
+//      thread 0 issued the products) multiply a fifteenth of the tile's u
 //      into their running products, two independent chains per thread (two
 //      lazy rounds per product; a product lowers the power of R by one, as a
 //      word on the integer pipe does).  At a group start that carries
@@ -84,6 +85,7 @@ static_assert(kOffB % 16 == 0 && kOffABias % 16 == 0 && kOffBBias % 16 == 0 && k
               "setup_tc alignment");
 static_assert(kATile % 16 == 0, "bulk copies move multiples of 16 bytes");
 static_assert(kTcHalfBytes % 16 == 0 && (kTcParts & (kTcParts - 1)) == 0, "setup_tc shape");
+static_assert(kTcCands == 32, "a part of the products is a warp: part 0 is the warp that issues the MMAs");
 constexpr uint32_t kTmemCols = 512;           // 2 halves x 32 candidates x 8 planes (column = 256 h + 8 c + plane)
 constexpr long kWaitLimit = 1L << 26;         // mbarrier polls before giving up
 constexpr uint32_t kBiasBits = 0x4B000000u;   // fp32 bits of 2^23
@@ -484,9 +486,12 @@ __global__ void __launch_bounds__(kTcThreads, 1) setup_tc_kernel(ClassBuf<uint64
                     if (prt == 0)
                         for (; k > 0; --k) P[0] = Cls64L::sq(m, P[0]);
                 }
+                // the words go to parts 1.. : part 0 is warp 0, whose first
+                // thread has just issued the next tile's products (it waits
+                // while the tensor pipe takes them) and holds the accumulator
                 const uint32_t e = g < pg.ngroups ? min(t1, __ldg(pg.groups + 3 * g)) : t1;
-                const uint32_t span = (e - s + kTcParts - 1) / kTcParts;
-                const uint32_t lo = min(s + span * prt, e), hi = min(lo + span, e);
+                const uint32_t span = (e - s + kTcParts - 2) / (kTcParts - 1);
+                const uint32_t lo = prt ? min(s + span * (prt - 1), e) : e, hi = prt ? min(lo + span, e) : e;
                 const uint64_t *row = U + cl * kUStride + (lo - t0);
                 const uint32_t n = hi - lo;
                 uint32_t i = 0;
