@@ -89,6 +89,8 @@ WORKLOADS = {
                            desc="-! -c n=[5e6,5e6+1000) p=[2^50,2^50+4e6)"),
     "setup-primorial": dict(mode=2, nmin=9 * 10**6, nmax=9 * 10**6 + 1000, pmin=2**62, pmax=2**62 + 4 * 10**6,
                             desc="-# n=[9e6,9e6+1000) p=[2^62,2^62+4e6)"),
+    "setup-factorial32": dict(mode=1, nmin=9 * 10**6, nmax=9 * 10**6 + 1000, pmin=10**9, pmax=10**9 + 4 * 10**6,
+                              desc="-! n=[9e6,9e6+1000) p=[1e9,1e9+4e6)"),
     "setup-factorial-small": dict(mode=1, nmin=2 * 10**6, nmax=2 * 10**6 + 100, pmin=2**40, pmax=2**40 + 10**6,
                                   desc="-! n=[2e6,2e6+100) p=[2^40,2^40+1e6)"),
 }

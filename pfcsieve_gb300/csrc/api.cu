@@ -367,8 +367,8 @@ extern "C" int pfc_job_create(pfc_ctx *c, unsigned mode, uint32_t nmin, uint32_t
     j->setup_mulmods32 = a32.mulmods() + b32.mulmods();
     j->setup_mulmods64 = need64 ? a64.mulmods() + b64.mulmods() : aw.mulmods() + bw.mulmods();
 
-    if (needw) {
-        const HostProg<WideWord> *wide[2] = {&aw, &bw};
+    if (needw || need32) {   // the tensor-core setups of both classes use the paired form
+        const HostProg<WideWord> *wide[2] = {needw ? &aw : &a32, needw ? &bw : &b32};
         for (int k = 0; k < 2; ++k) {
             if (!build_tc_prog(*wide[k], j->tcp[k])) {
                 delete j;
@@ -502,8 +502,11 @@ static int tc_prepare(pfc_job *j) {
     CK(j->tct.alloc(c, std::max<size_t>((na + nb) * tb, 16)));
     CK(j->tc_src.upload(c, src));
     CK(j->tc_groups.upload(c, groups));
-    c->launches += launch_tc_pack(j->aw.words.p, j->tc_src.p, (uint32_t)pa.src.size(), (uint32_t)na, j->tct.p, c->st);
-    c->launches += launch_tc_pack(j->bw.words.p, j->tc_src.p + pa.src.size(), (uint32_t)pb.src.size(), (uint32_t)nb,
+    // the words: the lazy class-64 copy of the programs, or the class-32 one (the same programs)
+    const bool w64 = j->aw.view.ngroups || j->bw.view.ngroups;
+    const WideWord *wa = w64 ? j->aw.words.p : j->a32.words.p, *wb = w64 ? j->bw.words.p : j->b32.words.p;
+    c->launches += launch_tc_pack(wa, j->tc_src.p, (uint32_t)pa.src.size(), (uint32_t)na, j->tct.p, c->st);
+    c->launches += launch_tc_pack(wb, j->tc_src.p + pa.src.size(), (uint32_t)pb.src.size(), (uint32_t)nb,
                                   j->tct.p + na * tb, c->st);
     CK(cudaGetLastError());
     for (int k = 0; k < 2; ++k) {
@@ -520,6 +523,7 @@ static int tc_prepare(pfc_job *j) {
 }
 
 static bool tc_setup_applies(const pfc_job *j) { return j->use64 && j->seg_hi <= kLazyEnd && j->ctx->setup_tc; }
+static bool tc_setup32_applies(const pfc_job *j) { return j->use32 && j->ctx->setup_tc; }
 
 static int enqueue_setup(pfc_job *j) {
     pfc_ctx *c = j->ctx;
@@ -538,7 +542,21 @@ static int enqueue_setup(pfc_job *j) {
     sw.a = j->aw.view;
     sw.b = j->bw.view;
     sw.nnext0 = 0;
-    if (j->use32) c->launches += launch_setup32(j->c32.view(counts_ptr(j)), s32, c->st);
+    if (j->use32) {
+        if (tc_setup32_applies(j)) {
+            const int rc = tc_prepare(j);
+            if (rc) return rc;
+            const TcTiles ta{j->tct.p, j->tc_ntiles[0]},
+                tb{j->tct.p + (size_t)j->tc_ntiles[0] * tc_tile_bytes(), j->tc_ntiles[1]};
+            SetupArgs<WideWord> stc = s32;
+            stc.a = j->tc_view[0];
+            stc.b = j->tc_view[1];
+            CK(cudaMemsetAsync(&j->stats.p->tc_err, 0, sizeof(uint32_t), c->st));
+            c->launches += launch_setup32_tc(j->c32.view(counts_ptr(j)), stc, ta, tb, &j->stats.p->tc_err, c->st);
+        } else {
+            c->launches += launch_setup32(j->c32.view(counts_ptr(j)), s32, c->st);
+        }
+    }
     if (j->use64) {
         if (tc_setup_applies(j)) {
             const int rc = tc_prepare(j);
@@ -548,7 +566,7 @@ static int enqueue_setup(pfc_job *j) {
             SetupArgs<WideWord> stc = sw;
             stc.a = j->tc_view[0];
             stc.b = j->tc_view[1];
-            CK(cudaMemsetAsync(&j->stats.p->tc_err, 0, sizeof(uint32_t), c->st));
+            if (!tc_setup32_applies(j)) CK(cudaMemsetAsync(&j->stats.p->tc_err, 0, sizeof(uint32_t), c->st));
             c->launches += launch_setup64w_tc(j->c64.view(counts_ptr(j) + 1), stc, ta, tb, &j->stats.p->tc_err, c->st);
         } else if (j->seg_hi <= kLazyEnd) {
             c->launches += launch_setup64w(j->c64.view(counts_ptr(j) + 1), sw, c->st);
@@ -939,7 +957,7 @@ static int segment_body_graph(pfc_job *j) {
         if ((j->mode & PFC_COMPOSITORIAL) && j->cmult.n < need) CK(j->cmult.alloc(c, std::max<size_t>(need, 4096)));
         if ((j->mode & PFC_FACTORIAL) && j->ramp.n < need) CK(j->ramp.alloc(c, std::max<size_t>(need, 4096)));
     }
-    if (tc_setup_applies(j)) {
+    if (tc_setup_applies(j) || tc_setup32_applies(j)) {
         const int rc = tc_prepare(j);
         if (rc) return rc;
     }

@@ -154,6 +154,10 @@ uint32_t tc_setup_blocks(uint32_t cands);
 int launch_setup64w_tc(const ClassBuf<uint64_t> &c, const SetupArgs<WideWord> &a, const TcTiles &ta,
                        const TcTiles &tb, uint32_t *err, cudaStream_t st, uint32_t block0 = 0,
                        uint32_t nblocks = 0);
+// class 32 on the same tiles (the class-32 and lazy class-64 programs are the same)
+uint32_t tc_setup_blocks32(uint32_t cands);
+int launch_setup32_tc(const ClassBuf<uint32_t> &c, const SetupArgs<WideWord> &a, const TcTiles &ta,
+                      const TcTiles &tb, uint32_t *err, cudaStream_t st, uint32_t block0 = 0, uint32_t nblocks = 0);
 // start residues of a split walk: boundary k's into s0/s1 + (k-1) * c.cap
 int launch_split_setup32(const ClassBuf<uint32_t> &c, const SplitSetup<WideWord> &ss, uint32_t *s0, uint32_t *s1,
                          cudaStream_t st);

@@ -43,9 +43,12 @@
 //      squarings (Horner over exponent bits) and at the end of a program the
 //      products are combined into the accumulator (a tree over the sixteen
 //      threads), which is then squared.
-// The result equals setup_kernel<Cls64L>'s: the same product of the same
-// words in the same Horner order, exact arithmetic, canonical residues at the
-// end.  Every wait is bounded; after a timeout the kernel sets bit 1 of
+// Class 32 (p < 2^31) runs the same kernel with 4 byte planes, 64 candidates
+// per CTA (N = 64 x 4 = 256 again), T < 2^47 reduced by one 32-bit round and
+// one Montgomery product (R = 2^32) per word.  The result equals
+// setup_kernel<Cls64L>'s or setup_kernel<Cls32>'s: the same product of the
+// same words in the same Horner order, exact arithmetic, canonical residues
+// at the end.  Every wait is bounded; after a timeout the kernel sets bit 1 of
 // `flags`, frees its TMEM and stores nothing.
 #include <cuda_runtime.h>
 
@@ -59,34 +62,25 @@ namespace {
 constexpr int kTcThreads = 512;
 constexpr int kTcGroups = kTcThreads / 128;   // warp groups (each covers the 128 TMEM lanes)
 constexpr int kTcWords = 128;                 // words per tile: MMA M, TMEM lanes
-constexpr int kTcCands = 32;                  // candidates per CTA: N = 32 x 8 planes = 256
-constexpr int kTcParts = kTcThreads / kTcCands;   // threads per candidate in the products
+constexpr int kTcN = 256;                     // MMA N: candidates x byte planes
 constexpr int kTcBytes = 224;                 // bytes of a 1792-bit word: MMA K
 constexpr int kTcHalfBytes = kTcBytes / 2;    // bytes summed into one accumulator
-constexpr int kTcPlanes = 8;                  // byte planes of a 64-bit residue
 constexpr int kTcChains = 2;                  // independent product chains per thread
 constexpr uint32_t kRowGroup = (kTcBytes / 8) * 128;              // 3584 B between 8-row core groups
 constexpr uint32_t kBiasRowGroup = 2 * 128;                       // bias tiles: K = 16
 constexpr uint32_t kATile = (kTcWords / 8) * kRowGroup;           // 57,344 B
-constexpr uint32_t kBTile = kTcCands * kRowGroup;                 // 114,688 B: row group = candidate
-constexpr uint32_t kUStride = kTcWords + 1;   // u64 per candidate row; odd: column reads hit distinct banks
+constexpr uint32_t kBTile = (kTcN / 8) * kRowGroup;               // 114,688 B: rows = candidate x plane
+constexpr uint32_t kUStride = kTcWords + 1;   // words per candidate row; odd: column reads hit distinct banks
 constexpr uint32_t kOffA = 0;
 constexpr uint32_t kOffB = kOffA + kATile;
 constexpr uint32_t kOffABias = kOffB + kBTile;                                // 128 x 16, column 0 = 2048
 constexpr uint32_t kOffBBias = kOffABias + (kTcWords / 8) * kBiasRowGroup;    // 256 x 16, column 0 = 4096
-constexpr uint32_t kOffU = kOffBBias + kTcCands * kBiasRowGroup;              // u64 [32 cands][kUStride]
-constexpr uint32_t kOffPart = kOffU + kTcCands * kUStride * 8;      // u64 [parts][32] running products
-constexpr uint32_t kOffCand = kOffPart + kTcParts * kTcCands * 8;   // p (u64) and q (u32) per candidate
-constexpr uint32_t kOffMisc = kOffCand + kTcCands * 16;             // 2 mbarriers, TMEM address, timeout flag
-constexpr uint32_t kSmemBytes = kOffMisc + 64;
-static_assert(kSmemBytes <= 227 * 1024, "setup_tc shared memory");
-static_assert(kOffB % 16 == 0 && kOffABias % 16 == 0 && kOffBBias % 16 == 0 && kOffU % 16 == 0 &&
-                  kOffMisc % 8 == 0,
+constexpr uint32_t kOffU = kOffBBias + (kTcN / 8) * kBiasRowGroup;            // reduced words [cands][kUStride]
+static_assert(kOffB % 16 == 0 && kOffABias % 16 == 0 && kOffBBias % 16 == 0 && kOffU % 16 == 0,
               "setup_tc alignment");
 static_assert(kATile % 16 == 0, "bulk copies move multiples of 16 bytes");
-static_assert(kTcHalfBytes % 16 == 0 && (kTcParts & (kTcParts - 1)) == 0, "setup_tc shape");
-static_assert(kTcCands == 32, "a part of the products is a warp: part 0 is the warp that issues the MMAs");
-constexpr uint32_t kTmemCols = 512;           // 2 halves x 32 candidates x 8 planes (column = 256 h + 8 c + plane)
+static_assert(kTcHalfBytes % 16 == 0, "setup_tc shape");
+constexpr uint32_t kTmemCols = 2 * kTcN;      // 2 halves x 256 (column = 256 h + planes c + plane)
 constexpr long kWaitLimit = 1L << 26;         // mbarrier polls before giving up
 constexpr uint32_t kBiasBits = 0x4B000000u;   // fp32 bits of 2^23
 
@@ -168,6 +162,72 @@ __device__ __forceinline__ void prog_range(const Prog<WideWord> &pg, uint32_t &f
     }
 }
 
+// What differs between the size classes: the residue type, its byte planes,
+// the reduction of T and the product of a reduced word into a running value.
+template <class T>
+struct TcClass;
+
+// class 64 below 2^64/3: residues in [0, 2p) between squarings, lazy rounds
+template <>
+struct TcClass<Cls64L> {
+    using W = uint64_t;
+    using M = Mont64;
+    static constexpr int kPlanes = 8;
+    static constexpr uint64_t kIdle = 0x1FFFFFFFFFFFFFFFull;   // an idle slot works on 2^61 - 1
+    __device__ static __forceinline__ uint32_t qv(const M &m) { return m.q32; }   // -p^-1 mod 2^32
+    __device__ static __forceinline__ W two32(const M &m) {   // 2^32 mod p
+        return m.p > (1ull << 32) ? (1ull << 32) : (1ull << 32) - m.p;
+    }
+    // T = L + 2^32 H < 2^79: u = (T + m p) / 2^32 with m = -T p^-1 mod 2^32,
+    // so u = T 2^-32 (mod p) and u < 2^48 + p; tw0 + lo(m p0) = 2^32 [tw0 != 0]
+    __device__ static __forceinline__ W reduce(uint64_t L, uint64_t H, W p, uint32_t q) {
+        const uint32_t tw0 = (uint32_t)L;
+        const uint64_t Mh = (L >> 32) + H;
+        const uint32_t mm = tw0 * q;
+        const uint64_t lo = (uint64_t)mm * (uint32_t)p;
+        return Mh + (uint64_t)mm * (uint32_t)(p >> 32) + (lo >> 32) + (tw0 != 0 ? 1u : 0u);
+    }
+    __device__ static __forceinline__ W prod(const M &m, W s, W u) { return mulw2(s, u, m.p, m.q32); }
+    __device__ static __forceinline__ W sq(const M &m, W s) { return Cls64L::sq(m, s); }
+};
+
+// class 32: canonical residues, R = 2^32
+template <>
+struct TcClass<Cls32> {
+    using W = uint32_t;
+    using M = Mont32;
+    static constexpr int kPlanes = 4;
+    static constexpr uint32_t kIdle = 0x7FFFFFFFu;   // an idle slot works on 2^31 - 1
+    __device__ static __forceinline__ uint32_t qv(const M &m) { return m.pinv; }   // p^-1 mod 2^32
+    __device__ static __forceinline__ W two32(const M &m) { return m.one; }
+    // T = L < 2^48: with m = lo(T) p^-1 mod 2^32, T - m p = 0 (mod 2^32), so
+    // u = hi(T) - hi(m p) exactly, in (-p, 2^17), plus p when negative:
+    // u = T 2^-32 (mod p), u < 2^31
+    __device__ static __forceinline__ W reduce(uint64_t L, uint64_t, W p, uint32_t pinv) {
+        const uint32_t m1 = (uint32_t)L * pinv;
+        const int64_t u = (int64_t)(L >> 32) - (int64_t)(((uint64_t)m1 * p) >> 32);
+        return (W)(u < 0 ? u + p : u);
+    }
+    // s < p and u < 2^31: s u < p 2^32, one canonical round
+    __device__ static __forceinline__ W prod(const M &m, W s, W u) { return m.mul(s, u); }
+    __device__ static __forceinline__ W sq(const M &m, W s) { return m.mul(s, s); }
+};
+
+template <class T>
+struct TcLayout {
+    using W = typename TcClass<T>::W;
+    static constexpr int kPlanes = TcClass<T>::kPlanes;
+    static constexpr int kCands = kTcN / kPlanes;              // candidates per CTA
+    static constexpr int kParts = kTcThreads / kCands;         // threads per candidate in the products
+    static constexpr uint32_t kOffPart = kOffU + kCands * kUStride * sizeof(W);   // running products [parts][cands]
+    static constexpr uint32_t kOffCand = kOffPart + kParts * kCands * sizeof(W);  // p (W) and q (u32) per candidate
+    static constexpr uint32_t kOffMisc = (kOffCand + kCands * 12 + 15) & ~15u;    // 2 mbarriers, TMEM address, flag
+    static constexpr uint32_t kSmemBytes = kOffMisc + 64;
+    static_assert(kSmemBytes <= 227 * 1024, "setup_tc shared memory");
+    static_assert(kCands % 32 == 0 && (kParts & (kParts - 1)) == 0,
+                  "a part of the products is whole warps: part 0 holds the warp that issues the MMAs");
+};
+
 }  // namespace
 
 // One thread per word slot of a tile: the 1792-bit word (the product of a
@@ -212,23 +272,28 @@ __global__ void tc_pack_kernel(const WideWord *words, const uint32_t *src, uint3
     }
 }
 
-__global__ void __launch_bounds__(kTcThreads, 1) setup_tc_kernel(ClassBuf<uint64_t> c, SetupArgs<WideWord> a,
-                                                                 TcTiles ta, TcTiles tb, uint32_t *flags,
-                                                                 uint32_t block0) {
+template <class T>
+__global__ void __launch_bounds__(kTcThreads, 1)
+    setup_tc_kernel(ClassBuf<typename TcClass<T>::W> c, SetupArgs<WideWord> a, TcTiles ta, TcTiles tb,
+                    uint32_t *flags, uint32_t block0) {
+    using C = TcClass<T>;
+    using Lay = TcLayout<T>;
+    using W = typename C::W;
+    constexpr int kCands = Lay::kCands, kParts = Lay::kParts, kPlanes = Lay::kPlanes;
     extern __shared__ __align__(1024) unsigned char sm[];
     const uint32_t tid = threadIdx.x, warp = tid / 32;
     const uint32_t cnt = min(*c.count, c.cap);
-    const uint32_t c0 = (blockIdx.x + block0) * kTcCands;
+    const uint32_t c0 = (blockIdx.x + block0) * kCands;
     if (c0 >= cnt) return;   // whole CTA idle
 
-    uint64_t *U = reinterpret_cast<uint64_t *>(sm + kOffU);
-    uint64_t *part = reinterpret_cast<uint64_t *>(sm + kOffPart);
-    uint64_t *cand_p = reinterpret_cast<uint64_t *>(sm + kOffCand);
-    uint32_t *cand_q = reinterpret_cast<uint32_t *>(cand_p + kTcCands);
-    uint64_t *mbar_mma = reinterpret_cast<uint64_t *>(sm + kOffMisc);
-    uint64_t *mbar_load = reinterpret_cast<uint64_t *>(sm + kOffMisc + 8);
-    uint32_t *taddr_slot = reinterpret_cast<uint32_t *>(sm + kOffMisc + 16);
-    uint32_t *timeout = reinterpret_cast<uint32_t *>(sm + kOffMisc + 20);
+    W *U = reinterpret_cast<W *>(sm + kOffU);
+    W *part = reinterpret_cast<W *>(sm + Lay::kOffPart);
+    W *cand_p = reinterpret_cast<W *>(sm + Lay::kOffCand);
+    uint32_t *cand_q = reinterpret_cast<uint32_t *>(sm + Lay::kOffCand + kCands * 8);
+    uint64_t *mbar_mma = reinterpret_cast<uint64_t *>(sm + Lay::kOffMisc);
+    uint64_t *mbar_load = reinterpret_cast<uint64_t *>(sm + Lay::kOffMisc + 8);
+    uint32_t *taddr_slot = reinterpret_cast<uint32_t *>(sm + Lay::kOffMisc + 16);
+    uint32_t *timeout = reinterpret_cast<uint32_t *>(sm + Lay::kOffMisc + 20);
 
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(taddr_slot)),
@@ -242,20 +307,20 @@ __global__ void __launch_bounds__(kTcThreads, 1) setup_tc_kernel(ClassBuf<uint64
         *timeout = 0;
     }
 
-    // this thread's candidate and part: kTcParts threads per candidate (part 0
+    // this thread's candidate and part: kParts threads per candidate (part 0
     // holds the accumulator)
-    const uint32_t cl = tid % kTcCands, prt = tid / kTcCands;
+    const uint32_t cl = tid % kCands, prt = tid / kCands;
     const uint32_t ci = c0 + cl;
     const bool act = ci < cnt;
-    Mont64 m;
-    m.init(act ? c.p[ci] : 0x1FFFFFFFFFFFFFFFull);   // an idle slot works on 2^61 - 1
+    typename C::M m;
+    m.init(act ? c.p[ci] : (W)C::kIdle);
     if (prt == 0) {
         cand_p[cl] = m.p;
-        cand_q[cl] = m.q32;
+        cand_q[cl] = C::qv(m);
     }
 
     // bias tiles: A column 0 = 2048, B column 0 = 4096 (fp16), the rest 0
-    for (uint32_t r = tid; r < kTcWords + 8 * kTcCands; r += kTcThreads) {
+    for (uint32_t r = tid; r < kTcWords + kTcN; r += kTcThreads) {
         const bool isa = r < kTcWords;
         const uint32_t row = isa ? r : r - kTcWords;
         unsigned char *base = sm + (isa ? kOffABias : kOffBBias);
@@ -264,19 +329,19 @@ __global__ void __launch_bounds__(kTcThreads, 1) setup_tc_kernel(ClassBuf<uint64
         *reinterpret_cast<uint4 *>(base + tile_off(row, 1, kBiasRowGroup)) = make_uint4(0, 0, 0, 0);
     }
 
-    // B operand: the candidate's residues w_b = 2^(8b+32) mod p as 8 byte
-    // planes, the rows of the candidate's core group (each part writes its
+    // B operand: the candidate's residues w_b = 2^(8b+32) mod p as byte
+    // planes, rows kPlanes c .. kPlanes c + kPlanes - 1 (each part writes its
     // share of the 28 groups of 8 bytes, starting from 2^32 256^b0 mod p by
     // square-and-multiply; the plane order is rotated by the candidate so
     // that a warp's stores spread over the banks)
     {
-        constexpr uint32_t kChunk = (kTcBytes / 8 + kTcParts - 1) / kTcParts;
+        constexpr uint32_t kChunk = (kTcBytes / 8 + kParts - 1) / kParts;
         const uint32_t k8a = min(prt * kChunk, (uint32_t)(kTcBytes / 8)),
                        k8b = min(k8a + kChunk, (uint32_t)(kTcBytes / 8));
-        const uint64_t c256 = m.to_mont(256);
-        uint64_t x = m.p > (1ull << 32) ? (1ull << 32) : (1ull << 32) - m.p;   // 2^32 mod p
+        const W c256 = m.to_mont(256);
+        W x = C::two32(m);
         {
-            uint64_t pw = m.one, base = c256;
+            W pw = m.one, base = c256;
             for (uint32_t e = 8 * k8a; e; e >>= 1) {
                 if (e & 1) pw = m.mul(pw, base);
                 base = m.mul(base, base);
@@ -284,19 +349,19 @@ __global__ void __launch_bounds__(kTcThreads, 1) setup_tc_kernel(ClassBuf<uint64
             x = m.mul(x, pw);
         }
         for (uint32_t k8 = k8a; k8 < k8b; ++k8) {
-            uint64_t w[8];
+            W w[8];
 #pragma unroll
             for (int j = 0; j < 8; ++j) {
                 w[j] = x;
                 x = m.mul(x, c256);
             }
 #pragma unroll
-            for (int r = 0; r < kTcPlanes; ++r) {
-                const int pl = (r + (int)cl) % kTcPlanes;
+            for (int r = 0; r < kPlanes; ++r) {
+                const int pl = (r + (int)cl) % kPlanes;
                 uint64_t bytes = 0;
 #pragma unroll
-                for (int j = 0; j < 8; ++j) bytes |= ((w[j] >> (8 * pl)) & 0xFFull) << (8 * j);
-                *reinterpret_cast<uint4 *>(sm + kOffB + tile_off(8 * cl + pl, k8)) = f16x8(bytes);
+                for (int j = 0; j < 8; ++j) bytes |= (uint64_t)((w[j] >> (8 * pl)) & 0xFFu) << (8 * j);
+                *reinterpret_cast<uint4 *>(sm + kOffB + tile_off(kPlanes * cl + pl, k8)) = f16x8(bytes);
             }
         }
     }
@@ -304,7 +369,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) setup_tc_kernel(ClassBuf<uint64
     const uint32_t quad = warp % 4, wgroup = warp / 4;      // TMEM lane quadrant, warp group
     const uint32_t word = quad * 32 + (tid % 32);           // this thread's word of a tile
     // f32 <- f16 x f16, both K-major, N = 256, M = 128
-    const uint32_t idesc = (1u << 4) | ((uint32_t)(8 * kTcCands >> 3) << 17) | ((uint32_t)(kTcWords >> 4) << 24);
+    const uint32_t idesc = (1u << 4) | ((uint32_t)(kTcN >> 3) << 17) | ((uint32_t)(kTcWords >> 4) << 24);
     const int nprog = a.mode == (PFC_FACTORIAL | PFC_COMPOSITORIAL) ? 2 : 1;
 
     // tile i of program pi into the A region (one thread), completing on mbar_load
@@ -327,7 +392,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) setup_tc_kernel(ClassBuf<uint64
                        abias = smem_u32(sm + kOffABias), bbias = smem_u32(sm + kOffBBias);
 #pragma unroll
         for (int h = 0; h < 2; ++h) {
-            const uint32_t d = tbase + h * 8 * kTcCands;
+            const uint32_t d = tbase + h * kTcN;
             asm volatile(
                 "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, 0, 0;\n\t"
                 "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d),
@@ -368,8 +433,8 @@ __global__ void __launch_bounds__(kTcThreads, 1) setup_tc_kernel(ClassBuf<uint64
 
     uint32_t par_mma = 0, par_load = 0;
     bool failed = false;
-    uint64_t s0 = 0, s1 = 0;
-    uint64_t P[kTcChains];   // this part's running products (part 0, chain 0: the accumulator)
+    W s0 = 0, s1 = 0;
+    W P[kTcChains];          // this part's running products (part 0, chain 0: the accumulator)
 #pragma unroll
     for (int k = 0; k < kTcChains; ++k) P[k] = m.one;
     uint32_t g = 0;          // first group of the current program whose squarings are still due
@@ -380,14 +445,14 @@ __global__ void __launch_bounds__(kTcThreads, 1) setup_tc_kernel(ClassBuf<uint64
     auto combine = [&]() {
 #pragma unroll
         for (int k = 1; k < kTcChains; ++k) {
-            P[0] = mulw2(P[0], P[k], m.p, m.q32);
+            P[0] = C::prod(m, P[0], P[k]);
             P[k] = m.one;
         }
 #pragma unroll
-        for (uint32_t stride = 1; stride < (uint32_t)kTcParts; stride <<= 1) {
-            part[prt * kTcCands + cl] = P[0];
+        for (uint32_t stride = 1; stride < (uint32_t)kParts; stride <<= 1) {
+            part[prt * kCands + cl] = P[0];
             __syncthreads();
-            if ((prt & (2 * stride - 1)) == 0) P[0] = mulw2(P[0], part[(prt + stride) * kTcCands + cl], m.p, m.q32);
+            if ((prt & (2 * stride - 1)) == 0) P[0] = C::prod(m, P[0], part[(prt + stride) * kCands + cl]);
             __syncthreads();
         }
         if (prt != 0) P[0] = m.one;
@@ -399,10 +464,10 @@ __global__ void __launch_bounds__(kTcThreads, 1) setup_tc_kernel(ClassBuf<uint64
         const Prog<WideWord> &pg = pi == 0 ? a.a : a.b;
         combine();
         if (prt == 0) {
-            uint64_t acc = P[0];
+            W acc = P[0];
             for (; g < pg.ngroups; ++g)
-                for (uint32_t k = __ldg(pg.groups + 3 * g + 2); k > 0; --k) acc = Cls64L::sq(m, acc);
-            for (uint32_t k = 0; k < pg.final_sq; ++k) acc = Cls64L::sq(m, acc);
+                for (uint32_t k = __ldg(pg.groups + 3 * g + 2); k > 0; --k) acc = C::sq(m, acc);
+            for (uint32_t k = 0; k < pg.final_sq; ++k) acc = C::sq(m, acc);
             acc = m.mul(acc, m.mont_R_pow(pg.corr));
             if (nprog == 2 && pi == 0) s1 = acc;
             else s0 = acc;
@@ -433,32 +498,27 @@ __global__ void __launch_bounds__(kTcThreads, 1) setup_tc_kernel(ClassBuf<uint64
         const bool nhave = next_tile(npi, ni_t, true);
         if (nhave && tid == 0) load_tile(npi, ni_t);   // the A region is free: the products are done
         // 1. u = T 2^-32 (mod p) for this thread's word and its warp group's candidates
-        for (uint32_t cc = wgroup * (kTcCands / kTcGroups); cc < (wgroup + 1) * (kTcCands / kTcGroups); cc += 4) {
+        constexpr int kPerLoad = 32 / kPlanes;   // candidates per 32-column load
+        for (uint32_t cc = wgroup * (kCands / kTcGroups); cc < (wgroup + 1) * (kCands / kTcGroups); cc += kPerLoad) {
             uint32_t v0[32], v1[32];
-            ld32(taddr, 8 * cc, v0);
-            ld32(taddr, 8 * kTcCands + 8 * cc, v1);
+            ld32(taddr, kPlanes * cc, v0);
+            ld32(taddr, kTcN + kPlanes * cc, v1);
             asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
-            for (int j = 0; j < 4; ++j) {
+            for (int j = 0; j < kPerLoad; ++j) {
                 // plane sums e_a = D_{a,0} + D_{a,1} - 2^24 < 2^24 (the two bias
                 // patterns add to 2 x 0x4B000000 < 2^32)
-                uint32_t e[kTcPlanes];
+                uint32_t e[8];
 #pragma unroll
-                for (int pl = 0; pl < kTcPlanes; ++pl) e[pl] = v0[8 * j + pl] + v1[8 * j + pl] - 2u * kBiasBits;
+                for (int pl = 0; pl < 8; ++pl)
+                    e[pl] = pl < kPlanes ? v0[kPlanes * j + pl] + v1[kPlanes * j + pl] - 2u * kBiasBits : 0u;
+                // T = L + 2^32 H
                 const uint64_t L = (uint64_t)e[0] + ((uint64_t)e[1] << 8) + ((uint64_t)e[2] << 16) +
                                    ((uint64_t)e[3] << 24);
                 const uint64_t H = (uint64_t)e[4] + ((uint64_t)e[5] << 8) + ((uint64_t)e[6] << 16) +
                                    ((uint64_t)e[7] << 24);
-                // T = L + 2^32 H = tw0 + 2^32 M
-                const uint32_t tw0 = (uint32_t)L;
-                const uint64_t M = (L >> 32) + H;
                 const uint32_t cj = cc + j;
-                const uint64_t pj = cand_p[cj];
-                const uint32_t mm = tw0 * cand_q[cj];
-                // tw0 + lo(mm p0) = 2^32 [tw0 != 0]
-                const uint64_t lo = (uint64_t)mm * (uint32_t)pj;
-                U[cj * kUStride + word] =
-                    M + (uint64_t)mm * (uint32_t)(pj >> 32) + (lo >> 32) + (tw0 != 0 ? 1u : 0u);
+                U[cj * kUStride + word] = C::reduce(L, H, cand_p[cj], cand_q[cj]);
             }
         }
         // 2. the next tile's products (TMEM is free once every thread's loads
@@ -484,22 +544,22 @@ __global__ void __launch_bounds__(kTcThreads, 1) setup_tc_kernel(ClassBuf<uint64
                 if (k) {
                     combine();
                     if (prt == 0)
-                        for (; k > 0; --k) P[0] = Cls64L::sq(m, P[0]);
+                        for (; k > 0; --k) P[0] = C::sq(m, P[0]);
                 }
                 // the words go to parts 1.. : part 0 is warp 0, whose first
                 // thread has just issued the next tile's products (it waits
                 // while the tensor pipe takes them) and holds the accumulator
                 const uint32_t e = g < pg.ngroups ? min(t1, __ldg(pg.groups + 3 * g)) : t1;
-                const uint32_t span = (e - s + kTcParts - 2) / (kTcParts - 1);
+                const uint32_t span = (e - s + kParts - 2) / (kParts - 1);
                 const uint32_t lo = prt ? min(s + span * (prt - 1), e) : e, hi = prt ? min(lo + span, e) : e;
-                const uint64_t *row = U + cl * kUStride + (lo - t0);
+                const W *row = U + cl * kUStride + (lo - t0);
                 const uint32_t n = hi - lo;
                 uint32_t i = 0;
                 for (; i + kTcChains <= n; i += kTcChains) {
 #pragma unroll
-                    for (int k = 0; k < kTcChains; ++k) P[k] = mulw2(P[k], row[i + k], m.p, m.q32);
+                    for (int k = 0; k < kTcChains; ++k) P[k] = C::prod(m, P[k], row[i + k]);
                 }
-                for (; i < n; ++i) P[0] = mulw2(P[0], row[i], m.p, m.q32);
+                for (; i < n; ++i) P[0] = C::prod(m, P[0], row[i]);
                 s = e;
                 if (s >= t1) break;
             }
@@ -534,27 +594,41 @@ int launch_tc_pack(const WideWord *words, const uint32_t *src, uint32_t nw, uint
     return 1;
 }
 
-// One CTA of 512 threads per 32 candidates, one CTA per SM (shared memory);
-// blocks [block0, block0 + nblocks) of the class buffer (nblocks 0: to the end).
-uint32_t tc_setup_blocks(uint32_t cands) { return (cands + kTcCands - 1) / kTcCands; }
+// One CTA of 512 threads per 32 (class 64) or 64 (class 32) candidates, one
+// CTA per SM (shared memory); blocks [block0, block0 + nblocks) of the class
+// buffer (nblocks 0: to the end).
+uint32_t tc_setup_blocks(uint32_t cands) { return (cands + TcLayout<Cls64L>::kCands - 1) / TcLayout<Cls64L>::kCands; }
+uint32_t tc_setup_blocks32(uint32_t cands) { return (cands + TcLayout<Cls32>::kCands - 1) / TcLayout<Cls32>::kCands; }
 
-int launch_setup64w_tc(const ClassBuf<uint64_t> &c, const SetupArgs<WideWord> &a, const TcTiles &ta,
-                       const TcTiles &tb, uint32_t *flags, cudaStream_t st, uint32_t block0, uint32_t nblocks) {
+template <class T>
+static int launch_tc(const ClassBuf<typename TcClass<T>::W> &c, const SetupArgs<WideWord> &a, const TcTiles &ta,
+                     const TcTiles &tb, uint32_t *flags, cudaStream_t st, uint32_t block0, uint32_t nblocks) {
     if (!c.cap) return 0;
-    const uint32_t all = tc_setup_blocks(c.cap);
+    constexpr int kCands = TcLayout<T>::kCands;
+    const uint32_t all = (c.cap + kCands - 1) / kCands;
     if (block0 >= all) return 0;
     if (nblocks == 0 || nblocks > all - block0) nblocks = all - block0;
     static bool configured[64] = {false};
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 0;
     if (!configured[dev]) {
-        if (cudaFuncSetAttribute(setup_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemBytes) !=
-            cudaSuccess)
+        if (cudaFuncSetAttribute(setup_tc_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)TcLayout<T>::kSmemBytes) != cudaSuccess)
             return 0;
         configured[dev] = true;
     }
-    setup_tc_kernel<<<nblocks, kTcThreads, kSmemBytes, st>>>(c, a, ta, tb, flags, block0);
+    setup_tc_kernel<T><<<nblocks, kTcThreads, TcLayout<T>::kSmemBytes, st>>>(c, a, ta, tb, flags, block0);
     return 1;
+}
+
+int launch_setup64w_tc(const ClassBuf<uint64_t> &c, const SetupArgs<WideWord> &a, const TcTiles &ta,
+                       const TcTiles &tb, uint32_t *flags, cudaStream_t st, uint32_t block0, uint32_t nblocks) {
+    return launch_tc<Cls64L>(c, a, ta, tb, flags, st, block0, nblocks);
+}
+
+int launch_setup32_tc(const ClassBuf<uint32_t> &c, const SetupArgs<WideWord> &a, const TcTiles &ta,
+                      const TcTiles &tb, uint32_t *flags, cudaStream_t st, uint32_t block0, uint32_t nblocks) {
+    return launch_tc<Cls32>(c, a, ta, tb, flags, st, block0, nblocks);
 }
 
 }  // namespace pfc

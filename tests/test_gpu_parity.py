@@ -357,6 +357,11 @@ TC_CASES = [
     (5, 200000, 200050, 2**62, 2**62 + 20000),
     (2, 100000, 100050, 2**31 + 10, 2**31 + 40000),
     (4, 150000, 150050, 6 * 10**18, 6 * 10**18 + 40000),
+    # class 32 (four byte planes, 64 candidates per CTA), and both classes in one segment
+    (1, 20000, 20100, 10**9, 10**9 + 200000),
+    (5, 100000, 100050, 2**31 - 300000, 2**31 - 10),
+    (2, 150000, 150100, 10**7, 10**7 + 200000),
+    (4, 60000, 60100, 2**31 - 100000, 2**31 + 100000),
 ]
 
 
@@ -382,9 +387,10 @@ def test_tensor_core_setup_equals_the_integer_setup(case):
         assert np.array_equal(tc[k], ip[k])
 
 
-def test_tensor_core_setup_matches_the_oracle():
-    mode, nmin, nmax, lo, hi = TC_CASES[2]
-    totals, hits, p, s0, s1 = setup_run(TC_CASES[2], True)
+@pytest.mark.parametrize("case", [TC_CASES[2], TC_CASES[6]])
+def test_tensor_core_setup_matches_the_oracle(case):
+    mode, nmin, nmax, lo, hi = case
+    totals, hits, p, s0, s1 = setup_run(case, True)
     cands = o.candidates(lo, hi)
     assert np.array_equal(p, cands)
     ohits, _, terms = o.sieve(mode, nmin, nmax, cands, want_terms=True)
