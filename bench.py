@@ -491,12 +491,16 @@ def mixed_roofline(jobs, outcomes, seconds, peaks, tc_s=0.0, setup_tc=True):
     the compositorial, prime n for #, both for -! -c), weighted by the measured
     issue rates (IMAD 1, IMAD.WIDE and IMAD.HI by their rates relative to
     IMAD), over the batch's wall time inside pfc_batch_step (iterations and
-    the tensor-core setups of admitted searches overlap).  Per unit (see arith.cuh, walk.cuh, setup_tc.cu): 896-bit
-    word 36 IMAD.WIDE + 2 IMAD (class 32); class 64 below 2^64/3 76 + 3 on the
-    integer pipe, or with the tensor-core setup 10 + 3 (the one-round
-    reduction of the folded word and the two-round product) with the fold's
-    112 x 8 byte-plane multiply-adds on the tensor pipe, reported apart
-    against the measured dense bf16 peak (fp16 runs at the same rate); 64-bit
+    the tensor-core setups of admitted searches overlap).  Per unit (see
+    arith.cuh, walk.cuh, setup_tc.cu): 896-bit word on the integer pipe
+    36 IMAD.WIDE + 2 IMAD (class 32), 76 + 3 (class 64 below 2^64/3); with the
+    tensor-core setup, which multiplies pairs of them into 1792-bit words, per
+    896-bit word 1.5 + 1 (class 32: half a 32-bit reduction and half a
+    Montgomery product) and 5 + 1.5 (class 64: half the one-round reduction and
+    half the two-round product), with the fold's 112 x 4 (class 32) or 112 x 8
+    (class 64) byte-plane multiply-adds per 896-bit word on the tensor pipe,
+    reported apart against the measured dense bf16 peak (fp16 runs at the same
+    rate); 64-bit
     word and class-64 squaring 8 IMAD.WIDE + 2 IMAD; class-32 squaring
     IMAD.WIDE + IMAD + IMAD.HI; walk steps as step_recipe.  Restores,
     corrections and replays are overhead, as in the single-search roofline.
@@ -506,7 +510,8 @@ def mixed_roofline(jobs, outcomes, seconds, peaks, tc_s=0.0, setup_tc=True):
     w = peaks["imad"] / peaks["imad_wide"]
     h = peaks["imad"] / peaks["mul_hi"]
     lazy_end = 0x5555555555555556
-    unit = {32: (36 * w + 2, w + 1 + h), 64: ((10 if setup_tc else 76) * w + 3, 8 * w + 2),
+    unit = {32: ((1.5 * w + 1) if setup_tc else (36 * w + 2), w + 1 + h),
+            64: ((5 * w + 1.5) if setup_tc else (76 * w + 3), 8 * w + 2),
             65: (8 * w + 2, 8 * w + 2)}
     tc_macs = 0.0
     top = max(s.nmax for s in jobs) + 1
@@ -531,8 +536,8 @@ def mixed_roofline(jobs, outcomes, seconds, peaks, tc_s=0.0, setup_tc=True):
         step = sum(k * peaks["imad"] / peaks[name] for name, k in recipe.items())
         cw, cs = unit[cls]
         total += outcomes[i].primecount * (words * cw + sq * cs + steps * step)
-        if cls == 64 and setup_tc:
-            tc_macs += outcomes[i].primecount * words * 112 * 8
+        if cls in (32, 64) and setup_tc:
+            tc_macs += outcomes[i].primecount * words * 112 * (8 if cls == 64 else 4)
     achieved = total / seconds
     return {"bound": "int (multiply pipe)", "achieved": achieved / 1e12, "peak": peaks["imad"] / 1e12,
             "unit": "Tops/s IMAD-equivalent (IMAD.WIDE, IMAD.HI weighted by measured rates)",

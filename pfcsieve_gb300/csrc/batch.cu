@@ -389,13 +389,14 @@ struct BatchJob {
     // class 64 below 2^64/3 on the tensor cores: the wide programs' groups
     // (first program's, then the second's) and their shapes
     bool tc = false;
-    bool tc_wait = false;            // its class-64 setup is still running (no class-64 window yet)
-    cudaEvent_t tc_ev0 = nullptr, tc_ev1 = nullptr;   // around that setup (throughput policy)
-    SetupArgs<WideWord> tc_args{};   // the setup launch (programs, tiles)
+    // per size class (0: class 32, 1: class 64 below 2^64/3)
+    bool tc_wait[2] = {false, false};    // its setup is still running (no window of the class yet)
+    cudaEvent_t tc_ev0[2] = {}, tc_ev1[2] = {};   // around that setup (throughput policy)
+    uint32_t tc_block[2] = {0, 0}, tc_blocks[2] = {0, 0};   // latency policy: next candidate block, blocks
+    uint64_t tc_iter[2] = {0, 0};    // iteration that launched the last blocks
+    double tc_block_cost[2] = {0, 0};   // budget units (multiplies) per block
+    SetupArgs<WideWord> tc_args{};   // the setup launch (programs, tiles), both classes
     TcTiles tc_ta{}, tc_tb{};
-    uint32_t tc_block = 0, tc_blocks = 0;   // latency policy: next candidate block, blocks in all
-    uint64_t tc_iter = 0;            // iteration that launched the last blocks
-    double tc_block_cost = 0;        // budget units (multiplies) per block
     // (the paired programs, host.hpp TcProg: word sources and groups of the
     // first program then the second's; tc_nw counts the 896-bit words of the
     // first program, tc_pw the paired words of each)
@@ -668,10 +669,12 @@ void release_device(pfc_batch *b, BatchJob *j) {
     j->d_tcgroups.release(c);
     j->d_tcsrc.release(c);
     j->d_tct.release(c);
-    if (j->tc_ev0) cudaEventDestroy(j->tc_ev0);
-    if (j->tc_ev1) cudaEventDestroy(j->tc_ev1);
-    j->tc_ev0 = j->tc_ev1 = nullptr;
-    j->tc_wait = false;
+    for (int k = 0; k < 2; ++k) {
+        if (j->tc_ev0[k]) cudaEventDestroy(j->tc_ev0[k]);
+        if (j->tc_ev1[k]) cudaEventDestroy(j->tc_ev1[k]);
+        j->tc_ev0[k] = j->tc_ev1[k] = nullptr;
+        j->tc_wait[k] = false;
+    }
     j->d_segs32.release(c);
     j->d_segs64.release(c);
     j->d_cmult.release(c);
@@ -710,7 +713,7 @@ int upload_job(pfc_batch *b, BatchJob *j) {
     cudaError_t e = j->d_words32.upload(c, j->words32);
     if (e == cudaSuccess) e = j->d_words64.upload(c, j->words64);
     if (e == cudaSuccess) e = j->d_wordsw.upload(c, j->wordsw);
-    const bool tc = j->tc && j->use64 && c->setup_tc;
+    const bool tc = j->tc && (j->use64 || j->use32) && c->setup_tc;
     const size_t tb = tc_tile_bytes(), nt = (size_t)j->tc_ntiles[0] + j->tc_ntiles[1];
     if (e == cudaSuccess && tc) e = j->d_tcgroups.upload(c, j->tcgroups);
     if (e == cudaSuccess && tc) e = j->d_tcsrc.upload(c, j->tcsrc);
@@ -755,6 +758,14 @@ JobDev<W> job_view(pfc_batch *b, BatchJob *j, const DevClass<W> &cls, int which,
     d.termsum = &b->stats.p[j->slot].termsum;
     d.flags = &b->stats.p[j->slot].flags;
     return d;
+}
+
+// The tensor-core setup of one class of a search: candidate blocks
+// [block0, block0 + n) (n 0: all), flags into the search's slot.
+int tc_launch(pfc_batch *b, BatchJob *j, int cls, cudaStream_t st, uint32_t block0, uint32_t n) {
+    BatchStats *bs = b->stats.p + j->slot;   // device address
+    return cls ? launch_setup64w_tc(j->c64.view(bs->counts + 1), j->tc_args, j->tc_ta, j->tc_tb, &bs->flags, st, block0, n)
+               : launch_setup32_tc(j->c32.view(bs->counts), j->tc_args, j->tc_ta, j->tc_tb, &bs->flags, st, block0, n);
 }
 
 // Move prepared searches onto the device while slots and the memory budget
@@ -827,20 +838,21 @@ int admit_prepared(pfc_batch *b) {
         c->h2d += sizeof(v32[f]) + sizeof(v64[f]);
     }
     CK(cudaStreamSynchronize(c->st));
-    // class-64 setups below 2^64/3 on the tensor cores.  The search's
-    // class-64 timeline starts at its walk, which joins the iterations once
-    // the setup has finished (build_tasks).  Throughput policy: one launch per
-    // fresh search on the setup streams, overlapping the iterations.  Latency
-    // policy: the setup runs in chunks of candidate blocks ahead of each
-    // iteration (launch_iteration), within a share of the iteration's
-    // budget, so that small searches are not held up behind large setups.
+    // setups of class 32 and of class 64 below 2^64/3 on the tensor cores.
+    // The search's timeline of the class starts at its walk, which joins the
+    // iterations once the setup has finished (build_tasks).  Throughput
+    // policy: one setup launch per fresh search and class on the setup
+    // streams, overlapping the iterations.  Latency policy: the setup runs in
+    // chunks of candidate blocks ahead of each iteration (launch_iteration),
+    // within a share of the iteration's budget, so that small searches are
+    // not held up behind large setups.
     if (c->setup_tc) {
         bool waited[pfc_batch::kTcStreams] = {};
         CK(cudaEventRecord(b->ev_tc0, c->st));
         for (BatchJob *j : fresh) {
             // (a timeline without walk steps keeps its setup windows: the
             // window that ends it also adds the check terms)
-            if (!j->d_tct.p || !j->n64 || !j->nwalk) continue;
+            if (!j->d_tct.p || !j->nwalk) continue;
             SetupArgs<WideWord> &sw = j->tc_args;
             memset(&sw, 0, sizeof(sw));
             sw.mode = j->mode;
@@ -856,24 +868,27 @@ int admit_prepared(pfc_batch *b) {
             }
             j->tc_ta = TcTiles{j->d_tct.p, j->tc_ntiles[0]};
             j->tc_tb = TcTiles{j->d_tct.p + (size_t)j->tc_ntiles[0] * tc_tile_bytes(), j->tc_ntiles[1]};
-            j->tc_blocks = tc_setup_blocks(j->n64);
-            j->tc_block_cost = kTcTileCost * ((double)j->tc_ntiles[0] + j->tc_ntiles[1]);
-            j->pos64 = j->nsetup64;
-            j->tc_wait = true;
-            if (b->policy == PFC_BATCH_LATENCY) {
-                j->tc_block = 0;
-                continue;
+            for (int cls = 0; cls < 2; ++cls) {
+                const uint32_t n = cls ? j->n64 : j->n32;
+                if (!n) continue;
+                j->tc_blocks[cls] = cls ? tc_setup_blocks(n) : tc_setup_blocks32(n);
+                j->tc_block_cost[cls] = kTcTileCost * ((double)j->tc_ntiles[0] + j->tc_ntiles[1]);
+                (cls ? j->pos64 : j->pos32) = cls ? j->nsetup64 : j->nsetup32;
+                j->tc_wait[cls] = true;
+                if (b->policy == PFC_BATCH_LATENCY) {
+                    j->tc_block[cls] = 0;
+                    continue;
+                }
+                const int si = b->tc_next++ % pfc_batch::kTcStreams;
+                if (!waited[si]) CK(cudaStreamWaitEvent(b->tcst[si], b->ev_tc0, 0));
+                waited[si] = true;
+                CK(cudaEventCreate(&j->tc_ev0[cls]));
+                CK(cudaEventCreate(&j->tc_ev1[cls]));
+                CK(cudaEventRecord(j->tc_ev0[cls], b->tcst[si]));
+                c->launches += tc_launch(b, j, cls, b->tcst[si], 0, 0);
+                CK(cudaEventRecord(j->tc_ev1[cls], b->tcst[si]));
+                j->tc_block[cls] = j->tc_blocks[cls];
             }
-            const int si = b->tc_next++ % pfc_batch::kTcStreams;
-            if (!waited[si]) CK(cudaStreamWaitEvent(b->tcst[si], b->ev_tc0, 0));
-            waited[si] = true;
-            CK(cudaEventCreate(&j->tc_ev0));
-            CK(cudaEventCreate(&j->tc_ev1));
-            CK(cudaEventRecord(j->tc_ev0, b->tcst[si]));
-            c->launches += launch_setup64w_tc(j->c64.view(b->stats.p[j->slot].counts + 1), sw, j->tc_ta, j->tc_tb,
-                                              &b->stats.p[j->slot].flags, b->tcst[si]);
-            CK(cudaEventRecord(j->tc_ev1, b->tcst[si]));
-            j->tc_block = j->tc_blocks;
         }
         CK(cudaGetLastError());
     }
@@ -952,18 +967,20 @@ uint32_t build_tasks(pfc_batch *b) {
     const double budget = per_iter * 6.0;   // candidate-steps -> multiplies
     b->iter_budget = budget;
     const double cta_share = budget / (3.0 * b->ctx->sms);
-    for (BatchJob *j : b->running) {   // tensor-core setups that have finished
-        if (!j->tc_wait) continue;
-        if (!j->tc_ev1) {   // chunks: done once the iteration that ran the last ones has finished
-            if (j->tc_block >= j->tc_blocks && b->iterations > j->tc_iter) j->tc_wait = false;
-            continue;
+    for (BatchJob *j : b->running)   // tensor-core setups that have finished
+        for (int k = 0; k < 2; ++k) {
+            if (!j->tc_wait[k]) continue;
+            if (!j->tc_ev1[k]) {   // chunks: done once the iteration that ran the last ones has finished
+                if (j->tc_block[k] >= j->tc_blocks[k] && b->iterations > j->tc_iter[k]) j->tc_wait[k] = false;
+                continue;
+            }
+            const cudaError_t q = cudaEventQuery(j->tc_ev1[k]);
+            if (q == cudaErrorNotReady) continue;
+            float ms = 0;
+            if (q == cudaSuccess && cudaEventElapsedTime(&ms, j->tc_ev0[k], j->tc_ev1[k]) == cudaSuccess)
+                b->tc_s += ms * 1e-3;
+            j->tc_wait[k] = false;   // an error surfaces at the next synchronisation
         }
-        const cudaError_t q = cudaEventQuery(j->tc_ev1);
-        if (q == cudaErrorNotReady) continue;
-        float ms = 0;
-        if (q == cudaSuccess && cudaEventElapsedTime(&ms, j->tc_ev0, j->tc_ev1) == cudaSuccess) b->tc_s += ms * 1e-3;
-        j->tc_wait = false;   // an error surfaces at the next synchronisation
-    }
     std::vector<std::pair<double, BatchJob *>> order;
     order.reserve(b->running.size());
     for (BatchJob *j : b->running) {
@@ -978,12 +995,12 @@ uint32_t build_tasks(pfc_batch *b) {
         BatchJob *j = o.second;
         const PosCost c32 = pos_cost(j, false), c64 = pos_cost(j, true);
         double jrate = 0, worst = 0;
-        if (j->pos32 < j->tot32) {
+        if (j->pos32 < j->tot32 && !j->tc_wait[0]) {
             jrate += j->n32 * (j->pos32 < j->nsetup32 ? c32.setup : c32.walk);
             worst = std::max(worst, std::max(per_cta(j, false, kSetupTask) * c32.setup,
                                              per_cta(j, false, kWalkTask) * c32.walk));
         }
-        if (j->pos64 < j->tot64 && !j->tc_wait) {
+        if (j->pos64 < j->tot64 && !j->tc_wait[1]) {
             jrate += j->n64 * (j->pos64 < j->nsetup64 ? c64.setup : c64.walk);
             worst = std::max(worst, per_cta(j, true, kSetupTask) * std::max(c64.setup, c64.walk));
         }
@@ -1019,7 +1036,7 @@ uint32_t build_tasks(pfc_batch *b) {
         for (int cls = 0; cls < 2; ++cls) {
             const uint32_t pos = cls ? j->pos64 : j->pos32, tot = cls ? j->tot64 : j->tot32;
             const uint32_t ns = cls ? j->nsetup64 : j->nsetup32, n = cls ? j->n64 : j->n32;
-            if (pos >= tot || n == 0 || j->wait || (cls && j->tc_wait)) continue;
+            if (pos >= tot || n == 0 || j->wait || j->tc_wait[cls]) continue;
             uint32_t hi = (uint32_t)std::min<uint64_t>((uint64_t)pos + (j->win ? j->win : L), tot);
             // a window that reaches the end of the setup stops there: the walk
             // starts in the next iteration, in the walk kernel, and the general
@@ -1071,7 +1088,8 @@ static void launch_list(pfc_batch *b, int l, const JobDev<typename T::W> *jobs, 
 
 bool tc_chunks_pending(const pfc_batch *b) {
     for (const BatchJob *j : b->running)
-        if (j->tc_wait && !j->tc_ev1 && j->tc_block < j->tc_blocks) return true;
+        for (int k = 0; k < 2; ++k)
+            if (j->tc_wait[k] && !j->tc_ev1[k] && j->tc_block[k] < j->tc_blocks[k]) return true;
     return false;
 }
 
@@ -1088,23 +1106,30 @@ int launch_iteration(pfc_batch *b) {
     // latency policy: chunks of pending tensor-core setups, smallest first,
     // ahead of the iteration's windows on the context stream
     if (tc_chunks_pending(b)) {
-        std::vector<std::pair<double, BatchJob *>> pend;
+        struct Pend {
+            double cost;
+            BatchJob *j;
+            int cls;
+        };
+        std::vector<Pend> pend;
         for (BatchJob *j : b->running)
-            if (j->tc_wait && !j->tc_ev1 && j->tc_block < j->tc_blocks)
-                pend.push_back({(j->tc_blocks - j->tc_block) * j->tc_block_cost, j});
-        std::sort(pend.begin(), pend.end(), [](const auto &x, const auto &y) { return x.first < y.first; });
+            for (int k = 0; k < 2; ++k)
+                if (j->tc_wait[k] && !j->tc_ev1[k] && j->tc_block[k] < j->tc_blocks[k])
+                    pend.push_back({(j->tc_blocks[k] - j->tc_block[k]) * j->tc_block_cost[k], j, k});
+        std::sort(pend.begin(), pend.end(), [](const Pend &x, const Pend &y) { return x.cost < y.cost; });
         double left = b->iter_budget * kTcChunkShare;
         CK(cudaEventRecord(b->ev_ck0, c->st));
-        for (auto &pj : pend) {
-            BatchJob *j = pj.second;
+        for (const Pend &pj : pend) {
+            BatchJob *j = pj.j;
+            const int k = pj.cls;
             if (left <= 0) break;
-            const double fit = std::floor(left / std::max(j->tc_block_cost, 1.0));
-            const uint32_t n = (uint32_t)std::min<double>(j->tc_blocks - j->tc_block, std::max<double>(fit, c->sms));
-            c->launches += launch_setup64w_tc(j->c64.view(b->stats.p[j->slot].counts + 1), j->tc_args, j->tc_ta,
-                                              j->tc_tb, &b->stats.p[j->slot].flags, c->st, j->tc_block, n);
-            j->tc_block += n;
-            if (j->tc_block >= j->tc_blocks) j->tc_iter = b->iterations;
-            left -= n * j->tc_block_cost;
+            const double fit = std::floor(left / std::max(j->tc_block_cost[k], 1.0));
+            const uint32_t n =
+                (uint32_t)std::min<double>(j->tc_blocks[k] - j->tc_block[k], std::max<double>(fit, c->sms));
+            c->launches += tc_launch(b, j, k, c->st, j->tc_block[k], n);
+            j->tc_block[k] += n;
+            if (j->tc_block[k] >= j->tc_blocks[k]) j->tc_iter[k] = b->iterations;
+            left -= n * j->tc_block_cost[k];
         }
         CK(cudaEventRecord(b->ev_ck1, c->st));
         b->ck_pending = true;
@@ -1395,7 +1420,7 @@ extern "C" int pfc_batch_step(pfc_batch *b, uint32_t *active, uint32_t *queued) 
             // returns after a short pause (searches submitted meanwhile are
             // admitted by the next call) instead of blocking on one setup
             for (BatchJob *j : b->running)
-                if (j->tc_wait) {
+                if (j->tc_wait[0] || j->tc_wait[1]) {
                     std::this_thread::sleep_for(std::chrono::microseconds(200));
                     break;
                 }

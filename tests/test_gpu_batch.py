@@ -89,12 +89,17 @@ def test_batch_matches_oracle_on_small_cases(ctx):
 TC_MIX = [MIX[2], MIX[5], MIX[10], MIX[11],
           (5, 30000, 33000, 2**45, 2**45 + 2 * 10**6),
           (4, 101, 50000, 2**55, 2**55 + 10**6),
-          (2, 60000, 60300, 2**50, 2**50 + 10**6)]   # a primorial n range without primes: setup windows
+          (2, 60000, 60300, 2**50, 2**50 + 10**6),   # a primorial n range without primes: setup windows
+          # class 32, and both classes in one search
+          (1, 300000, 300200, 10**9, 10**9 + 10**6),
+          (5, 200000, 200100, 2**31 - 10**6, 2**31 - 10),
+          (4, 100000, 100100, 2**31 - 10**5, 2**31 + 10**5)]
 
 
 def test_batch_tensor_core_setup_equals_the_integer_setup(ctx):
-    """Searches of the lazy class-64 range in a batch whose context sets them
-    up on the tensor cores give exactly what they give alone with the
+    """Searches of class 32 and of the lazy class-64 range in a batch whose
+    context sets them up on the tensor cores give exactly what they give
+    alone with the
     integer-pipe setup."""
     with pfc.Context(0) as ref:
         ref.set_setup_tc(False)
@@ -110,7 +115,7 @@ def test_batch_tensor_core_setup_equals_the_integer_setup(ctx):
 
 def test_batch_tensor_core_setup_matches_the_oracle(ctx):
     cases = [(1, 3000, 3400, 2**40, 2**40 + 2 * 10**5), (5, 1500, 1800, 2**47, 2**47 + 10**5),
-             (2, 4000, 4600, 2**61, 2**61 + 10**5)]
+             (2, 4000, 4600, 2**61, 2**61 + 10**5), (1, 3000, 3400, 10**8, 10**8 + 2 * 10**5)]
     with pfc.Batch(ctx) as b:
         ids = [b.submit(*c) for c in cases]
         b.run()

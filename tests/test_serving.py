@@ -86,18 +86,19 @@ def test_batched_roofline_counts():
     w1, s1 = pfc.setup_program_size(1, 5000)
     w4, s4 = pfc.setup_program_size(4, 5000)
     w2, s2 = pfc.setup_program_size(2, 5000, wide=False)
-    for setup_tc, word64 in ((False, 76), (True, 10)):
-        # with the tensor-core setup the class-64 word's fold leaves the
-        # integer pipe (10 IMAD.WIDE + 3 IMAD remain) and its GPU span joins
+    for setup_tc, word32, word64 in ((False, 36 * w + 2, 76 * w + 3), (True, 1.5 * w + 1, 5 * w + 1.5)):
+        # with the tensor-core setup the words' fold leaves the integer pipe
+        # (half a reduction and half a product per 896-bit word remain)
         tc_s = 0.5 if setup_tc else 0.0
         r = bench.mixed_roofline(jobs, out, 2.0, peaks, tc_s=tc_s, setup_tc=setup_tc)
-        want = (100 * (w1 * (36 * w + 2) + s1 * (w + 1 + h) + 1000 * (2 * w + 1))
-                + 101 * (w4 * (word64 * w + 3) + s4 * (8 * w + 2) + (1000 - primes) * (4 * w + 1))
+        want = (100 * (w1 * word32 + s1 * (w + 1 + h) + 1000 * (2 * w + 1))
+                + 101 * (w4 * word64 + s4 * (8 * w + 2) + (1000 - primes) * (4 * w + 1))
                 + 102 * (w2 * (8 * w + 2) + s2 * (8 * w + 2) + primes * (7 * w + 2)))
         assert abs(r["alg_ops"] - want) < 1e-6 * want
         assert abs(r["frac"] - want / 2.0 / 20e12) < 1e-9
         if setup_tc:
-            assert r["tensor_setup"]["flops"] == 2 * 101 * w4 * 112 * 8
-            assert abs(r["tensor_setup"]["achieved_tflops"] - 2 * 101 * w4 * 112 * 8 / 2.0 / 1e12) < 1e-12
+            flops = 2 * (100 * w1 * 112 * 4 + 101 * w4 * 112 * 8)
+            assert r["tensor_setup"]["flops"] == flops
+            assert abs(r["tensor_setup"]["achieved_tflops"] - flops / 2.0 / 1e12) < 1e-12
         else:
             assert r["tensor_setup"] is None
