@@ -267,7 +267,13 @@ __device__ void run_task(const JobDev<typename T::W> &J, const Task &t, const Hi
         } else {
             a.type = PFC_TYPE_FACTORIAL;
         }
-        walk_streams<T, NC, FUSED>(m, x, act, a, h);
+        // the lazy class-64 walk kind in blocks of 32, as the per-job default
+        // (fewer block restores; 75.4 against 76.9 ms per-job on the
+        // primorial near 2^62); the others in the class's default blocks
+        constexpr int WB = (KIND == kWalkTask && std::is_same<T, Cls64L>::value && !FUSED)
+                               ? 32
+                               : (FUSED ? T::B_FUSED : T::B);
+        walk_streams<T, NC, FUSED, WB>(m, x, act, a, h);
         if (!FUSED && NC > 1) {
             // walked counts are equal for the candidates of one thread
         }
