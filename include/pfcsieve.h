@@ -107,15 +107,18 @@ int pfc_ctx_set_graphs(pfc_ctx *ctx, int on);
  * every candidate in one chain.  Results are identical. */
 int pfc_ctx_set_split(pfc_ctx *ctx, int on);
 
-/* Tensor-core setup.  The setup of class-64 candidates below 2^64/3 folds
- * each 896-bit table word against the candidate's position residues; this
- * exact integer contraction runs on the tensor cores (tcgen05, bf16 byte
- * planes with fp32 sums below 2^23, so exact) and the CUDA cores do the
- * Montgomery products, with the same result as the integer-pipe setup.  No
- * counterpart in the reference, whose setup multiplies its power and
- * product tables one entry at a time (kernels/setup.cl:49-288).  On by
- * default; off (`on` = 0, or PFCSIEVE_SETUP_TC=0 in the environment when the
- * context is created) uses the integer-pipe fold.  Results are identical. */
+/* Tensor-core setup.  The setup of class-32 candidates and of class-64
+ * candidates below 2^64/3 folds each table word against the candidate's
+ * position residues; this exact integer contraction runs on the tensor cores
+ * (tcgen05, fp16 byte planes with fp32 sums kept below 2^24, so exact), on
+ * 1792-bit words that are products of pairs of the program's 896-bit words,
+ * and the CUDA cores do the Montgomery products, with the same result as the
+ * integer-pipe setup.  No counterpart in the reference, whose setup
+ * multiplies its power and product tables one entry at a time
+ * (kernels/setup.cl:49-288).  On by default, in pfc_segment, the stage calls
+ * and the batch; off (`on` = 0, or PFCSIEVE_SETUP_TC=0 in the environment
+ * when the context is created) uses the integer-pipe fold.  Results are
+ * identical. */
 int pfc_ctx_set_setup_tc(pfc_ctx *ctx, int on);
 
 /* Number of kernels this context has launched so far. */
