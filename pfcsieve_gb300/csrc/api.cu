@@ -43,6 +43,7 @@ struct pfc_job {
     // the tensor-core setup: aw, bw in their paired form (TcProg), packed into
     // fp16 tiles on first use
     TcProg tcp[2];
+    uint64_t tc_words = 0;        // 896-bit words of the search's programs (both)
     DArr<uint8_t> tct;
     DArr<uint32_t> tc_src, tc_groups;
     Prog<WideWord> tc_view[2] = {};
@@ -367,7 +368,9 @@ extern "C" int pfc_job_create(pfc_ctx *c, unsigned mode, uint32_t nmin, uint32_t
     j->setup_mulmods32 = a32.mulmods() + b32.mulmods();
     j->setup_mulmods64 = need64 ? a64.mulmods() + b64.mulmods() : aw.mulmods() + bw.mulmods();
 
-    if (needw || need32) {   // the tensor-core setups of both classes use the paired form
+    j->tc_words = ps->wa.words.size() + ps->wb.words.size();
+    if ((needw && j->tc_words >= kTcMinWords64) || (need32 && j->tc_words >= kTcMinWords32)) {
+        // the tensor-core setups of both classes use the paired form
         const HostProg<WideWord> *wide[2] = {needw ? &aw : &a32, needw ? &bw : &b32};
         for (int k = 0; k < 2; ++k) {
             if (!build_tc_prog(*wide[k], j->tcp[k])) {
@@ -522,8 +525,12 @@ static int tc_prepare(pfc_job *j) {
     return PFC_OK;
 }
 
-static bool tc_setup_applies(const pfc_job *j) { return j->use64 && j->seg_hi <= kLazyEnd && j->ctx->setup_tc; }
-static bool tc_setup32_applies(const pfc_job *j) { return j->use32 && j->ctx->setup_tc; }
+static bool tc_setup_applies(const pfc_job *j) {
+    return j->use64 && j->seg_hi <= kLazyEnd && j->ctx->setup_tc && j->tc_words >= kTcMinWords64;
+}
+static bool tc_setup32_applies(const pfc_job *j) {
+    return j->use32 && j->ctx->setup_tc && j->tc_words >= kTcMinWords32;
+}
 
 static int enqueue_setup(pfc_job *j) {
     pfc_ctx *c = j->ctx;

@@ -719,7 +719,9 @@ int upload_job(pfc_batch *b, BatchJob *j) {
     cudaError_t e = j->d_words32.upload(c, j->words32);
     if (e == cudaSuccess) e = j->d_words64.upload(c, j->words64);
     if (e == cudaSuccess) e = j->d_wordsw.upload(c, j->wordsw);
-    const bool tc = j->tc && (j->use64 || j->use32) && c->setup_tc;
+    const uint64_t words = (uint64_t)j->tc_nw[0] + j->tc_nw[1];
+    const bool tc = j->tc && c->setup_tc &&
+                    ((j->use64 && words >= kTcMinWords64) || (j->use32 && words >= kTcMinWords32));
     const size_t tb = tc_tile_bytes(), nt = (size_t)j->tc_ntiles[0] + j->tc_ntiles[1];
     if (e == cudaSuccess && tc) e = j->d_tcgroups.upload(c, j->tcgroups);
     if (e == cudaSuccess && tc) e = j->d_tcsrc.upload(c, j->tcsrc);
@@ -874,9 +876,11 @@ int admit_prepared(pfc_batch *b) {
             }
             j->tc_ta = TcTiles{j->d_tct.p, j->tc_ntiles[0]};
             j->tc_tb = TcTiles{j->d_tct.p + (size_t)j->tc_ntiles[0] * tc_tile_bytes(), j->tc_ntiles[1]};
+            const uint64_t words = (uint64_t)j->tc_nw[0] + j->tc_nw[1];
             for (int cls = 0; cls < 2; ++cls) {
                 const uint32_t n = cls ? j->n64 : j->n32;
-                if (!n) continue;
+                // small programs keep their setup windows (kernels.cuh kTcMinWords*)
+                if (!n || words < (cls ? kTcMinWords64 : kTcMinWords32)) continue;
                 j->tc_blocks[cls] = cls ? tc_setup_blocks(n) : tc_setup_blocks32(n);
                 j->tc_block_cost[cls] = kTcTileCost * ((double)j->tc_ntiles[0] + j->tc_ntiles[1]);
                 (cls ? j->pos64 : j->pos32) = cls ? j->nsetup64 : j->nsetup32;

@@ -90,10 +90,13 @@ TC_MIX = [MIX[2], MIX[5], MIX[10], MIX[11],
           (5, 30000, 33000, 2**45, 2**45 + 2 * 10**6),
           (4, 101, 50000, 2**55, 2**55 + 10**6),
           (2, 60000, 60300, 2**50, 2**50 + 10**6),   # a primorial n range without primes: setup windows
+          # programs above the tensor-core thresholds (kernels.cuh): class 64,
           # class 32, and both classes in one search
+          (1, 300000, 300100, 2**45, 2**45 + 2 * 10**6),
+          (5, 200000, 200100, 2**50, 2**50 + 10**6),
           (1, 300000, 300200, 10**9, 10**9 + 10**6),
           (5, 200000, 200100, 2**31 - 10**6, 2**31 - 10),
-          (4, 100000, 100100, 2**31 - 10**5, 2**31 + 10**5)]
+          (4, 300000, 300100, 2**31 - 10**5, 2**31 + 10**5)]
 
 
 def test_batch_tensor_core_setup_equals_the_integer_setup(ctx):
@@ -114,8 +117,9 @@ def test_batch_tensor_core_setup_equals_the_integer_setup(ctx):
 
 
 def test_batch_tensor_core_setup_matches_the_oracle(ctx):
-    cases = [(1, 3000, 3400, 2**40, 2**40 + 2 * 10**5), (5, 1500, 1800, 2**47, 2**47 + 10**5),
-             (2, 4000, 4600, 2**61, 2**61 + 10**5), (1, 3000, 3400, 10**8, 10**8 + 2 * 10**5)]
+    # programs above the tensor-core thresholds (kTcMinWords64 = 128, kTcMinWords32 = 384 words)
+    cases = [(1, 60000, 60400, 2**40, 2**40 + 10**5), (5, 60000, 60300, 2**47, 2**47 + 10**5),
+             (2, 120000, 120600, 2**61, 2**61 + 10**5), (1, 200000, 200400, 10**8, 10**8 + 10**5)]
     with pfc.Batch(ctx) as b:
         ids = [b.submit(*c) for c in cases]
         b.run()
