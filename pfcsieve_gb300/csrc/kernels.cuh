@@ -157,14 +157,15 @@ int launch_setup64w_tc(const ClassBuf<uint64_t> &c, const SetupArgs<WideWord> &a
 // class 32 on the same tiles (the class-32 and lazy class-64 programs are the same)
 uint32_t tc_setup_blocks32(uint32_t cands);
 // Smallest programs (896-bit words, both programs of the search) set up on the
-// tensor cores: below them the kernel's fixed cost per candidate (224
-// position residues, the final power of R, TMEM and barriers: about 320
-// SM cycles) outweighs what it saves per word (class 32 about 1.0 of 1.4
-// cycles per word and candidate, class 64 2.8 of 3.7); measured on GB300, a
-// combined search from n0 = 101 took 4.9 ms on the tensor cores against
-// 0.2 ms on the integer pipe.
-constexpr uint64_t kTcMinWords32 = 384;
-constexpr uint64_t kTcMinWords64 = 128;
+// tensor cores: below them the kernel's fixed cost per CTA (the 224 position
+// residues, TMEM, the first tile's copy and products, the final squarings and
+// tree, tens of thousands of cycles) outweighs what it saves per word.
+// Measured on GB300 (factorial searches, 4e6-wide p ranges), integer pipe
+// against tensor cores: class 32 at 460 words 0.41 / 0.46 ms, at 687 words
+// 0.60 / 0.54 ms; class 64 at 687 words 1.17 / 1.19 ms, at 20,330 words
+// 33.4 / 8.4 ms.
+constexpr uint64_t kTcMinWords32 = 640;
+constexpr uint64_t kTcMinWords64 = 768;
 int launch_setup32_tc(const ClassBuf<uint32_t> &c, const SetupArgs<WideWord> &a, const TcTiles &ta,
                       const TcTiles &tb, uint32_t *err, cudaStream_t st, uint32_t block0 = 0, uint32_t nblocks = 0);
 // start residues of a split walk: boundary k's into s0/s1 + (k-1) * c.cap

@@ -221,7 +221,13 @@ struct TcLayout {
     static constexpr int kParts = kTcThreads / kCands;         // threads per candidate in the products
     static constexpr uint32_t kOffPart = kOffU + kCands * kUStride * sizeof(W);   // running products [parts][cands]
     static constexpr uint32_t kOffCand = kOffPart + kParts * kCands * sizeof(W);  // p (W) and q (u32) per candidate
-    static constexpr uint32_t kOffMisc = (kOffCand + kCands * 12 + 15) & ~15u;    // 2 mbarriers, TMEM address, flag
+    static constexpr uint32_t kOffCorr = (kOffCand + kCands * 12 + 7) & ~7u;      // Mont(R^corr) [2 programs][cands]
+    static constexpr uint32_t kOffMisc = (kOffCorr + 2 * kCands * sizeof(W) + 15) & ~15u;   // 2 mbarriers, TMEM address, flag
+    // parts that build byte planes; the first one after them computes the
+    // programs' power-of-R corrections meanwhile
+    static constexpr uint32_t kChunk = (kTcBytes / 8 + kParts - 1) / kParts;
+    static constexpr uint32_t kBusy = (kTcBytes / 8 + kChunk - 1) / kChunk;
+    static_assert(kBusy < (uint32_t)kParts, "a part left for the corrections");
     static constexpr uint32_t kSmemBytes = kOffMisc + 64;
     static_assert(kSmemBytes <= 227 * 1024, "setup_tc shared memory");
     static_assert(kCands % 32 == 0 && (kParts & (kParts - 1)) == 0,
@@ -294,6 +300,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     uint64_t *mbar_load = reinterpret_cast<uint64_t *>(sm + Lay::kOffMisc + 8);
     uint32_t *taddr_slot = reinterpret_cast<uint32_t *>(sm + Lay::kOffMisc + 16);
     uint32_t *timeout = reinterpret_cast<uint32_t *>(sm + Lay::kOffMisc + 20);
+    W *corr_pow = reinterpret_cast<W *>(sm + Lay::kOffCorr);
 
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(taddr_slot)),
@@ -335,7 +342,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     // square-and-multiply; the plane order is rotated by the candidate so
     // that a warp's stores spread over the banks)
     {
-        constexpr uint32_t kChunk = (kTcBytes / 8 + kParts - 1) / kParts;
+        constexpr uint32_t kChunk = Lay::kChunk;
         const uint32_t k8a = min(prt * kChunk, (uint32_t)(kTcBytes / 8)),
                        k8b = min(k8a + kChunk, (uint32_t)(kTcBytes / 8));
         const W c256 = m.to_mont(256);
@@ -365,6 +372,13 @@ __global__ void __launch_bounds__(kTcThreads, 1)
             }
         }
     }
+
+    // the power-of-R corrections Mont(R^corr) of the programs, on the part(s)
+    // that build no byte planes (read by part 0 at the end of each program)
+    const int nprog0 = a.mode == (PFC_FACTORIAL | PFC_COMPOSITORIAL) ? 2 : 1;
+    for (int pi = 0; pi < nprog0; ++pi)
+        if (prt == Lay::kBusy + ((uint32_t)pi % (kParts - Lay::kBusy)))
+            corr_pow[pi * kCands + cl] = m.mont_R_pow((pi == 0 ? a.a : a.b).corr);
 
     const uint32_t quad = warp % 4, wgroup = warp / 4;      // TMEM lane quadrant, warp group
     const uint32_t word = quad * 32 + (tid % 32);           // this thread's word of a tile
@@ -468,7 +482,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
             for (; g < pg.ngroups; ++g)
                 for (uint32_t k = __ldg(pg.groups + 3 * g + 2); k > 0; --k) acc = C::sq(m, acc);
             for (uint32_t k = 0; k < pg.final_sq; ++k) acc = C::sq(m, acc);
-            acc = m.mul(acc, m.mont_R_pow(pg.corr));
+            acc = m.mul(acc, corr_pow[pi * kCands + cl]);
             if (nprog == 2 && pi == 0) s1 = acc;
             else s0 = acc;
             P[0] = acc;

@@ -92,11 +92,11 @@ TC_MIX = [MIX[2], MIX[5], MIX[10], MIX[11],
           (2, 60000, 60300, 2**50, 2**50 + 10**6),   # a primorial n range without primes: setup windows
           # programs above the tensor-core thresholds (kernels.cuh): class 64,
           # class 32, and both classes in one search
-          (1, 300000, 300100, 2**45, 2**45 + 2 * 10**6),
-          (5, 200000, 200100, 2**50, 2**50 + 10**6),
+          (1, 400000, 400100, 2**45, 2**45 + 2 * 10**6),
+          (5, 300000, 300100, 2**50, 2**50 + 10**6),
           (1, 300000, 300200, 10**9, 10**9 + 10**6),
-          (5, 200000, 200100, 2**31 - 10**6, 2**31 - 10),
-          (4, 300000, 300100, 2**31 - 10**5, 2**31 + 10**5)]
+          (5, 300000, 300100, 2**31 - 10**6, 2**31 - 10),
+          (4, 600000, 600100, 2**31 - 10**5, 2**31 + 10**5)]
 
 
 def test_batch_tensor_core_setup_equals_the_integer_setup(ctx):
@@ -117,9 +117,9 @@ def test_batch_tensor_core_setup_equals_the_integer_setup(ctx):
 
 
 def test_batch_tensor_core_setup_matches_the_oracle(ctx):
-    # programs above the tensor-core thresholds (kTcMinWords64 = 128, kTcMinWords32 = 384 words)
-    cases = [(1, 60000, 60400, 2**40, 2**40 + 10**5), (5, 60000, 60300, 2**47, 2**47 + 10**5),
-             (2, 120000, 120600, 2**61, 2**61 + 10**5), (1, 200000, 200400, 10**8, 10**8 + 10**5)]
+    # programs above the tensor-core thresholds (kTcMinWords64 = 768, kTcMinWords32 = 640 words)
+    cases = [(1, 400000, 400400, 2**40, 2**40 + 3 * 10**4), (5, 300000, 300300, 2**47, 2**47 + 3 * 10**4),
+             (2, 600000, 600600, 2**61, 2**61 + 3 * 10**4), (1, 300000, 300400, 10**8, 10**8 + 3 * 10**4)]
     with pfc.Batch(ctx) as b:
         ids = [b.submit(*c) for c in cases]
         b.run()

@@ -351,19 +351,19 @@ def test_split_walk_matches_the_oracle():
 # tensor-core setup (class 64 below 2^64/3): programs of one tile and of many
 # (group boundaries inside tiles), both programs of the combined search, a
 # product program without squarings, p just above 2^31 and near 2^64/3
-# programs at or above the tensor-core thresholds (kernels.cuh: 128 words in
-# class 64, 384 in class 32; smaller ones keep the integer setup)
+# programs at or above the tensor-core thresholds (kernels.cuh: 768 words in
+# class 64, 640 in class 32; smaller ones keep the integer setup)
 TC_CASES = [
-    (1, 60000, 60100, 2**40, 2**40 + 20000),            # 145 words
-    (1, 300000, 300100, 2**50, 2**50 + 20000),          # 687
-    (5, 200000, 200050, 2**62, 2**62 + 20000),          # 600
-    (2, 100000, 100050, 2**31 + 10, 2**31 + 40000),     # 162
-    (4, 150000, 150050, 6 * 10**18, 6 * 10**18 + 40000),   # 209
+    (1, 400000, 400100, 2**40, 2**40 + 20000),          # 910 words
+    (1, 500000, 500100, 2**50, 2**50 + 20000),          # 1138
+    (5, 300000, 300050, 2**62, 2**62 + 20000),          # 895
+    (2, 600000, 600050, 2**31 + 10, 2**31 + 40000),     # 975
+    (4, 600000, 600050, 6 * 10**18, 6 * 10**18 + 40000),   # 805
     # class 32 (four byte planes, 64 candidates per CTA), and both classes in one segment
-    (1, 200000, 200100, 10**9, 10**9 + 200000),         # 460
-    (5, 150000, 150050, 2**31 - 100000, 2**31 - 10),    # 452
+    (1, 400000, 400100, 10**9, 10**9 + 200000),         # 910
+    (5, 300000, 300050, 2**31 - 40000, 2**31 - 10),     # 895
     (2, 400000, 400100, 10**7, 10**7 + 200000),         # 650
-    (4, 300000, 300100, 2**31 - 100000, 2**31 + 100000),   # 408
+    (4, 600000, 600100, 2**31 - 100000, 2**31 + 100000),   # 805
     # below the thresholds: the integer setup, through the same switch
     (1, 20000, 20100, 2**40, 2**40 + 20000),            # 56
     (1, 40000, 40100, 10**9, 10**9 + 200000),           # 101
