@@ -40,9 +40,10 @@
 //      into their running products, two independent chains per thread (two
 //      lazy rounds per product; a product lowers the power of R by one, as a
 //      word on the integer pipe does).  At a group start that carries
-//      squarings (Horner over exponent bits) and at the end of a program the
-//      products are combined into the accumulator (a tree over the sixteen
-//      threads), which is then squared.
+//      squarings (Horner over exponent bits) every thread squares each of its
+//      running products (squaring distributes over their Montgomery product);
+//      at the end of a program they are combined into the accumulator (a tree
+//      over the threads of the candidate).
 // Class 32 (p < 2^31) runs the same kernel with 4 byte planes, 64 candidates
 // per CTA (N = 64 x 4 = 256 again), T < 2^47 reduced by one 32-bit round and
 // one Montgomery product (R = 2^32) per word.  The result equals
@@ -555,10 +556,14 @@ __global__ void __launch_bounds__(kTcThreads, 1)
             for (;;) {
                 uint32_t k = 0;
                 for (; g < pg.ngroups && __ldg(pg.groups + 3 * g) <= s; ++g) k += __ldg(pg.groups + 3 * g + 2);
-                if (k) {
-                    combine();
-                    if (prt == 0)
-                        for (; k > 0; --k) P[0] = C::sq(m, P[0]);
+                // a group start's squarings, applied by every thread to each of
+                // its running products: the accumulator is their Montgomery
+                // product A = P_0 (x) ... (x) P_{n-1} = (prod P) R^-(n-1), and
+                // squaring each, P (x) P = P^2 R^-1, gives (prod P)^2 R^-(2n-1)
+                // = A (x) A, so no combining is needed until the program ends
+                for (; k > 0; --k) {
+#pragma unroll
+                    for (int c2 = 0; c2 < kTcChains; ++c2) P[c2] = C::sq(m, P[c2]);
                 }
                 // the words go to parts 1.. : part 0 is warp 0, whose first
                 // thread has just issued the next tile's products (it waits
