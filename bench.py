@@ -484,6 +484,12 @@ def hit_order(f):
     return f[np.lexsort((f["nc"], f["type"], np.abs(f["nc"].astype(np.int64)), f["p"]))]
 
 
+# programs below these sizes (896-bit words, both programs of a search) keep the
+# integer-pipe setup when the tensor-core setup is on: kTcMinWords32 and
+# kTcMinWords64 of pfcsieve_gb300/csrc/kernels.cuh
+TC_MIN_WORDS = {32: 448, 64: 480}
+
+
 def mixed_roofline(jobs, outcomes, seconds, peaks, tc_s=0.0, setup_tc=True):
     """Multiply-pipe roofline of a batched run: the algorithmic multiplies of
     every search (per candidate: its setup program's table words and squarings
@@ -500,7 +506,8 @@ def mixed_roofline(jobs, outcomes, seconds, peaks, tc_s=0.0, setup_tc=True):
     half the two-round product), with the fold's 112 x 4 (class 32) or 112 x 8
     (class 64) byte-plane multiply-adds per 896-bit word on the tensor pipe,
     reported apart against the measured dense bf16 peak (fp16 runs at the same
-    rate); 64-bit
+    rate), for programs of at least TC_MIN_WORDS words (smaller ones keep the
+    integer-pipe setup); 64-bit
     word and class-64 squaring 8 IMAD.WIDE + 2 IMAD; class-32 squaring
     IMAD.WIDE + IMAD + IMAD.HI; walk steps as step_recipe.  Restores,
     corrections and replays are overhead, as in the single-search roofline.
@@ -510,9 +517,8 @@ def mixed_roofline(jobs, outcomes, seconds, peaks, tc_s=0.0, setup_tc=True):
     w = peaks["imad"] / peaks["imad_wide"]
     h = peaks["imad"] / peaks["mul_hi"]
     lazy_end = 0x5555555555555556
-    unit = {32: ((1.5 * w + 1) if setup_tc else (36 * w + 2), w + 1 + h),
-            64: ((5 * w + 1.5) if setup_tc else (76 * w + 3), 8 * w + 2),
-            65: (8 * w + 2, 8 * w + 2)}
+    unit = {32: (36 * w + 2, w + 1 + h), 64: (76 * w + 3, 8 * w + 2), 65: (8 * w + 2, 8 * w + 2)}
+    tc_word = {32: 1.5 * w + 1, 64: 5 * w + 1.5}
     tc_macs = 0.0
     top = max(s.nmax for s in jobs) + 1
     isp = np.ones(top, dtype=bool)
@@ -535,9 +541,11 @@ def mixed_roofline(jobs, outcomes, seconds, peaks, tc_s=0.0, setup_tc=True):
         recipe = step_recipe(cls == 32, cls == 64)
         step = sum(k * peaks["imad"] / peaks[name] for name, k in recipe.items())
         cw, cs = unit[cls]
-        total += outcomes[i].primecount * (words * cw + sq * cs + steps * step)
-        if cls in (32, 64) and setup_tc:
+        tc = setup_tc and cls in (32, 64) and words >= TC_MIN_WORDS[cls]
+        if tc:
+            cw = tc_word[cls]
             tc_macs += outcomes[i].primecount * words * 112 * (8 if cls == 64 else 4)
+        total += outcomes[i].primecount * (words * cw + sq * cs + steps * step)
     achieved = total / seconds
     return {"bound": "int (multiply pipe)", "achieved": achieved / 1e12, "peak": peaks["imad"] / 1e12,
             "unit": "Tops/s IMAD-equivalent (IMAD.WIDE, IMAD.HI weighted by measured rates)",

@@ -158,14 +158,14 @@ int launch_setup64w_tc(const ClassBuf<uint64_t> &c, const SetupArgs<WideWord> &a
 uint32_t tc_setup_blocks32(uint32_t cands);
 // Smallest programs (896-bit words, both programs of the search) set up on the
 // tensor cores: below them the kernel's fixed cost per CTA (the 224 position
-// residues, TMEM, the first tile's copy and products, the final squarings and
-// tree, tens of thousands of cycles) outweighs what it saves per word.
-// Measured on GB300 (factorial searches, 4e6-wide p ranges), integer pipe
-// against tensor cores: class 32 at 460 words 0.41 / 0.46 ms, at 687 words
-// 0.60 / 0.54 ms; class 64 at 687 words 1.17 / 1.19 ms, at 20,330 words
-// 33.4 / 8.4 ms.
-constexpr uint64_t kTcMinWords32 = 640;
-constexpr uint64_t kTcMinWords64 = 768;
+// residues, TMEM, the first tile's copy and products, the final tree, tens of
+// thousands of cycles) outweighs what it saves per word.  Measured on GB300
+// (factorial searches, 4e6-wide p ranges), integer pipe against tensor cores:
+// class 32 at 235 words 0.22 / 0.33 ms, at 460 words 0.41 / 0.40 ms; class 64
+// at 460 words 0.79 / 0.80 ms, at 687 words 1.16 / 0.92 ms, at 20,330 words
+// 33.4 / 8.0 ms.
+constexpr uint64_t kTcMinWords32 = 448;
+constexpr uint64_t kTcMinWords64 = 480;
 int launch_setup32_tc(const ClassBuf<uint32_t> &c, const SetupArgs<WideWord> &a, const TcTiles &ta,
                       const TcTiles &tb, uint32_t *err, cudaStream_t st, uint32_t block0 = 0, uint32_t nblocks = 0);
 // start residues of a split walk: boundary k's into s0/s1 + (k-1) * c.cap

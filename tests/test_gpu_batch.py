@@ -117,7 +117,7 @@ def test_batch_tensor_core_setup_equals_the_integer_setup(ctx):
 
 
 def test_batch_tensor_core_setup_matches_the_oracle(ctx):
-    # programs above the tensor-core thresholds (kTcMinWords64 = 768, kTcMinWords32 = 640 words)
+    # programs above the tensor-core thresholds (kTcMinWords64 = 480, kTcMinWords32 = 448 words)
     cases = [(1, 400000, 400400, 2**40, 2**40 + 3 * 10**4), (5, 300000, 300300, 2**47, 2**47 + 3 * 10**4),
              (2, 600000, 600600, 2**61, 2**61 + 3 * 10**4), (1, 300000, 300400, 10**8, 10**8 + 3 * 10**4)]
     with pfc.Batch(ctx) as b:

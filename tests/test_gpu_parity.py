@@ -351,8 +351,8 @@ def test_split_walk_matches_the_oracle():
 # tensor-core setup (class 64 below 2^64/3): programs of one tile and of many
 # (group boundaries inside tiles), both programs of the combined search, a
 # product program without squarings, p just above 2^31 and near 2^64/3
-# programs at or above the tensor-core thresholds (kernels.cuh: 768 words in
-# class 64, 640 in class 32; smaller ones keep the integer setup)
+# programs at or above the tensor-core thresholds (kernels.cuh: 480 words in
+# class 64, 448 in class 32; smaller ones keep the integer setup)
 TC_CASES = [
     (1, 400000, 400100, 2**40, 2**40 + 20000),          # 910 words
     (1, 500000, 500100, 2**50, 2**50 + 20000),          # 1138
@@ -364,9 +364,14 @@ TC_CASES = [
     (5, 300000, 300050, 2**31 - 40000, 2**31 - 10),     # 895
     (2, 400000, 400100, 10**7, 10**7 + 200000),         # 650
     (4, 600000, 600100, 2**31 - 100000, 2**31 + 100000),   # 805
+    # just above the thresholds
+    (1, 210000, 210100, 2**40, 2**40 + 20000),          # 483
+    (1, 200000, 200100, 10**9, 10**9 + 200000),         # 460
     # below the thresholds: the integer setup, through the same switch
     (1, 20000, 20100, 2**40, 2**40 + 20000),            # 56
     (1, 40000, 40100, 10**9, 10**9 + 200000),           # 101
+    (1, 200000, 200100, 2**40, 2**40 + 20000),          # 460 (class 64)
+    (1, 190000, 190100, 10**9, 10**9 + 200000),         # 439 (class 32)
 ]
 
 
