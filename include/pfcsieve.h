@@ -116,9 +116,11 @@ int pfc_ctx_set_split(pfc_ctx *ctx, int on);
  * integer-pipe setup.  No counterpart in the reference, whose setup
  * multiplies its power and product tables one entry at a time
  * (kernels/setup.cl:49-288).  On by default, in pfc_segment, the stage calls
- * and the batch; off (`on` = 0, or PFCSIEVE_SETUP_TC=0 in the environment
- * when the context is created) uses the integer-pipe fold.  Results are
- * identical. */
+ * and the batch, for searches whose setup programs hold at least 448
+ * (class 32) or 480 (class 64) 896-bit words (pfc_setup_program_size);
+ * smaller programs, and every program when off (`on` = 0, or
+ * PFCSIEVE_SETUP_TC=0 in the environment when the context is created), use
+ * the integer-pipe fold.  Results are identical. */
 int pfc_ctx_set_setup_tc(pfc_ctx *ctx, int on);
 
 /* Number of kernels this context has launched so far. */
