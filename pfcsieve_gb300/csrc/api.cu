@@ -257,11 +257,12 @@ static bool build_progs(unsigned mode, uint32_t startN, const std::vector<uint32
     return build_power_prog(startN, 1, primes, a) && build_product_prog(below, b);
 }
 
-// primes up to lim from the context's list (grown when a larger limit is
-// asked for; callers bound every use by value)
-static const std::vector<uint32_t> &ctx_primes(pfc_ctx *c, uint32_t lim) {
-    if (lim > c->primes_lim || c->primes.empty()) {
-        c->primes = primes_between(2, lim);
+// the context's prime list, covering at least [2, lim] (replaced by a longer
+// one when a larger limit is asked for; callers bound every use by value and
+// hold the pointer while they use the list)
+static std::shared_ptr<const std::vector<uint32_t>> ctx_primes(pfc_ctx *c, uint32_t lim) {
+    if (!c->primes || lim > c->primes_lim) {
+        c->primes = std::make_shared<const std::vector<uint32_t>>(primes_between(2, lim));
         c->primes_lim = lim;
     }
     return c->primes;
@@ -276,7 +277,8 @@ static std::shared_ptr<const ProgSet> ctx_progs(pfc_ctx *c, unsigned mode, uint3
     if (ps && (!wide || ps->has_wide) && (!narrow || ps->has_narrow)) return ps;
     auto fresh = std::make_shared<ProgSet>(ps ? *ps : ProgSet());
     if ((wide && !fresh->has_wide) || (narrow && !fresh->has_narrow)) {
-        const std::vector<uint32_t> &primes = ctx_primes(c, std::max<uint32_t>(startN, 2));
+        const std::shared_ptr<const std::vector<uint32_t>> plist = ctx_primes(c, std::max<uint32_t>(startN, 2));
+        const std::vector<uint32_t> &primes = *plist;
         const std::vector<uint32_t> below(primes.begin(), std::upper_bound(primes.begin(), primes.end(), startN));
         if (wide && !fresh->has_wide) {
             if (!build_progs(mode, startN, primes, below, fresh->wa, fresh->wb)) return nullptr;
@@ -350,7 +352,8 @@ extern "C" int pfc_job_create(pfc_ctx *c, unsigned mode, uint32_t nmin, uint32_t
 
     const uint32_t startN = nmin - 1;
     const uint32_t plim = (mode & PFC_COMPOSITORIAL) ? nmax : std::max(startN, nmax - 1);
-    const std::vector<uint32_t> &primes = ctx_primes(c, plim);
+    const std::shared_ptr<const std::vector<uint32_t>> plist = ctx_primes(c, plim);
+    const std::vector<uint32_t> &primes = *plist;
     const bool need32 = pmin < kClassSplit;
     const bool needw = pmax > kClassSplit && pmin < kLazyEnd;
     const bool need64 = pmax > kLazyEnd;

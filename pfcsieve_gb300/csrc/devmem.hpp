@@ -43,8 +43,10 @@ struct pfc_ctx {
     // host tables kept between the context's jobs: the primes up to the
     // largest limit asked for so far, and the setup programs per (mode,
     // startN), oldest dropped first beyond kProgCacheBytes (searches of one n
-    // range over many p ranges, and the split walks' boundaries, reuse them)
-    std::vector<uint32_t> primes;
+    // range over many p ranges, and the split walks' boundaries, reuse them);
+    // the prime list is shared, so a caller's copy of the pointer stays valid
+    // when a later call replaces it with a longer one
+    std::shared_ptr<const std::vector<uint32_t>> primes;
     uint32_t primes_lim = 0;
     std::map<std::pair<unsigned, uint32_t>, std::shared_ptr<pfc::ProgSet>> progs;
     std::deque<std::pair<unsigned, uint32_t>> prog_order;
