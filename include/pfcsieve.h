@@ -265,6 +265,19 @@ int pfc_verify_factors_device(pfc_ctx *ctx, unsigned mode, uint32_t nmax, const 
  * run; no counterpart in the reference. */
 int pfc_setup_program_size(unsigned mode, uint32_t nmin, int wide, uint64_t *words, uint64_t *squarings);
 
+/* Host replay of a search's setup programs for one odd p (host only, no
+ * GPU): the programs pfc_job_create builds, run as the device runs them
+ * (each squaring and each product with a table word lowers the power of R,
+ * the final correction restores it) in exact modular arithmetic, giving the
+ * starting residues the setup must produce: *s0 = (nmin-1)!, (nmin-1)# or
+ * (nmin-1)!/(nmin-1)# mod p, and for the combined search also
+ * *s1 = (nmin-1)!/(nmin-1)# (else 0).  form 0: 64-bit words; 1: 896-bit
+ * words; 2: 896-bit words multiplied in pairs as the tensor-core setup takes
+ * them.  A check of the host-built programs against the definition
+ * (kernels/setup.cl:49-288 computes the same residues); not used by the
+ * sieve. */
+int pfc_setup_program_eval(unsigned mode, uint32_t nmin, int form, uint64_t p, uint64_t *s0, uint64_t *s1);
+
 /* Deterministic primality for 64-bit p (verifyprime.cpp:157-195). */
 int pfc_is_prime(uint64_t p);
 

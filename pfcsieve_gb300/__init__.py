@@ -102,6 +102,7 @@ def lib():
                                                     ctypes.c_int, P(sz), P(u64)]),
             "pfc_verify_factors_device": (ctypes.c_int, [vp, ctypes.c_uint, u32, vp, sz, vp, P(sz)]),
             "pfc_setup_program_size": (ctypes.c_int, [ctypes.c_uint, u32, ctypes.c_int, P(u64), P(u64)]),
+            "pfc_setup_program_eval": (ctypes.c_int, [ctypes.c_uint, u32, ctypes.c_int, u64, P(u64), P(u64)]),
             "pfc_is_prime": (ctypes.c_int, [u64]),
             "pfc_format_factor": (ctypes.c_int, [vp, ctypes.c_char_p, sz]),
             "pfc_status_string": (ctypes.c_char_p, [ctypes.c_int]),
@@ -465,6 +466,20 @@ def setup_program_size(mode, nmin, wide=True):
     _ck(lib().pfc_setup_program_size(mode, nmin, int(bool(wide)), ctypes.byref(w), ctypes.byref(q)),
         "pfc_setup_program_size")
     return w.value, q.value
+
+
+SETUP_FORMS = {"narrow": 0, "wide": 1, "paired": 2}
+
+
+def setup_program_eval(mode, nmin, p, form="wide"):
+    """(s0, s1): the starting residues a search's setup programs give for p,
+    replayed on the host as the device runs them (pfc_setup_program_eval);
+    form "narrow" (64-bit words), "wide" (896-bit words) or "paired" (the
+    tensor-core setup's pairs of 896-bit words)."""
+    s0, s1 = ctypes.c_uint64(0), ctypes.c_uint64(0)
+    _ck(lib().pfc_setup_program_eval(mode, nmin, SETUP_FORMS[form], int(p), ctypes.byref(s0), ctypes.byref(s1)),
+        "pfc_setup_program_eval")
+    return s0.value, s1.value
 
 
 def is_prime(p):

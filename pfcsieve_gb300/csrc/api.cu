@@ -330,6 +330,105 @@ extern "C" int pfc_setup_program_size(unsigned mode, uint32_t nmin, int wide, ui
     return PFC_OK;
 }
 
+namespace {
+// host replay of a setup program, the way the device runs it: the
+// accumulator holds x R^d, a squaring and a product with a table word each
+// lower d by one (a*b*R^-1), and the end multiplies by Mont(R^corr); exact
+// 128-bit modular arithmetic, R = 2^64 mod p
+typedef unsigned __int128 u128e;
+struct HostMont {
+    uint64_t p, rinv;
+    uint64_t mul(uint64_t a, uint64_t b) const { return (uint64_t)((u128e)a * b % p); }
+    uint64_t redc(uint64_t a, uint64_t b) const { return mul(mul(a, b), rinv); }
+};
+uint64_t host_word(const HostMont &m, uint64_t w) { return w % m.p; }
+uint64_t host_word(const HostMont &m, const WideWord &w) {
+    uint64_t z = 0;   // sum of limb_k 2^(28 k), from the top limb
+    for (int k = kWideLimbs - 1; k >= 0; --k)
+        z = (uint64_t)((((u128e)z << kWideRadixBits) + w.limb[k]) % m.p);
+    return z;
+}
+// a^-1 mod p for gcd(a, p) = 1 (extended Euclid)
+uint64_t host_inv(uint64_t a, uint64_t p) {
+    __int128 r0 = p, r1 = a % p, t0 = 0, t1 = 1;
+    while (r1) {
+        const __int128 q = r0 / r1, r2 = r0 - q * r1, t2 = t0 - q * t1;
+        r0 = r1, r1 = r2, t0 = t1, t1 = t2;
+    }
+    if (r0 != 1) return 0;
+    return (uint64_t)(t0 < 0 ? t0 + p : t0);
+}
+uint64_t host_pow(const HostMont &m, uint64_t b, uint64_t e) {
+    uint64_t r = 1 % m.p;
+    for (; e; e >>= 1, b = m.mul(b, b))
+        if (e & 1) r = m.mul(r, b);
+    return r;
+}
+// groups of (first word, end word, squarings before the group) over words
+// given by value(i)
+template <class F>
+uint64_t host_run(const HostMont &m, const std::vector<uint32_t> &groups, uint32_t final_sq, uint64_t corr,
+                  uint64_t acc, F value) {
+    for (size_t g = 0; g + 2 < groups.size(); g += 3) {
+        for (uint32_t k = 0; k < groups[g + 2]; ++k) acc = m.redc(acc, acc);
+        for (uint32_t i = groups[g]; i < groups[g + 1]; ++i) acc = m.redc(acc, value(i));
+    }
+    for (uint32_t k = 0; k < final_sq; ++k) acc = m.redc(acc, acc);
+    const uint64_t R = (uint64_t)(((u128e)1 << 64) % m.p);
+    return m.redc(acc, host_pow(m, R, corr + 1));   // Mont(R^corr) = R^(corr+1)
+}
+template <class W>
+uint64_t host_prog(const HostMont &m, const HostProg<W> &pg, uint64_t acc) {
+    return host_run(m, pg.groups, pg.final_sq, pg.corr, acc, [&](uint32_t i) { return host_word(m, pg.words[i]); });
+}
+uint64_t host_tc_prog(const HostMont &m, const HostProg<WideWord> &pg, uint64_t acc) {
+    TcProg tp;
+    if (!build_tc_prog(pg, tp)) return ~0ull;
+    return host_run(m, tp.groups, tp.final_sq, tp.corr, acc, [&](uint32_t i) {
+        const uint32_t s = tp.src[i] & 0x7FFFFFFFu;
+        const uint64_t z = host_word(m, pg.words[s]);
+        return (tp.src[i] & 0x80000000u) ? m.mul(z, host_word(m, pg.words[s + 1])) : z;
+    });
+}
+}  // namespace
+
+extern "C" int pfc_setup_program_eval(unsigned mode, uint32_t nmin, int form, uint64_t p, uint64_t *s0,
+                                      uint64_t *s1) {
+    if (!s0 || !s1 || p < 3 || !(p & 1) || form < 0 || form > 2) return PFC_ERR_ARG;
+    const bool valid_mode = mode == PFC_FACTORIAL || mode == PFC_PRIMORIAL || mode == PFC_COMPOSITORIAL ||
+                            mode == (PFC_FACTORIAL | PFC_COMPOSITORIAL);
+    if (!valid_mode || nmin < 101 || nmin > 0x7FFFFFFFu) return PFC_ERR_ARG;
+    const uint32_t startN = nmin - 1;
+    const std::vector<uint32_t> primes = primes_between(2, startN);
+    HostMont m;
+    m.p = p;
+    const uint64_t R = (uint64_t)(((u128e)1 << 64) % p);
+    m.rinv = host_inv(R, p);   // p odd: 2^64 is invertible
+    uint64_t a = 0, b = 0;
+    bool ok;
+    if (form == 0) {
+        HostProg<uint64_t> pa, pb;
+        ok = build_progs(mode, startN, primes, primes, pa, pb);
+        if (ok) {
+            a = host_prog(m, pa, R);   // Mont(1) = R
+            b = host_prog(m, pb, a);   // the combined search continues from the first result
+        }
+    } else {
+        HostProg<WideWord> pa, pb;
+        ok = build_progs(mode, startN, primes, primes, pa, pb);
+        if (ok) {
+            a = form == 1 ? host_prog(m, pa, R) : host_tc_prog(m, pa, R);
+            b = form == 1 ? host_prog(m, pb, a) : host_tc_prog(m, pb, a);
+            ok = a != ~0ull && b != ~0ull;
+        }
+    }
+    if (!ok) return PFC_ERR_ARG;
+    const bool two = mode == (PFC_FACTORIAL | PFC_COMPOSITORIAL);
+    *s0 = m.mul(two ? b : a, m.rinv);   // plain residues
+    *s1 = two ? m.mul(a, m.rinv) : 0;
+    return PFC_OK;
+}
+
 extern "C" int pfc_job_create(pfc_ctx *c, unsigned mode, uint32_t nmin, uint32_t nmax, uint64_t pmin,
                               uint64_t pmax, pfc_job **out) {
     if (!c || !out) return PFC_ERR_ARG;

@@ -172,3 +172,53 @@ def _program_model(mode, nmin):
 @pytest.mark.parametrize("mode,nmin", [(1, 101), (1, 5000), (2, 5000), (4, 5000), (5, 20011), (1, 65537)])
 def test_setup_program_size_matches_the_definition(pfc, mode, nmin):
     assert pfc.setup_program_size(mode, nmin) == _program_model(mode, nmin)
+
+
+def _start_residues(nmin, ps):
+    """(n-1)!, (n-1)# and (n-1)!/(n-1)# mod each p, n = nmin: the starting
+    residues the reference's setup computes (kernels/setup.cl:49-288), from
+    their definition."""
+    N = nmin - 1
+    isp = np.ones(N + 1, dtype=bool)
+    isp[:2] = False
+    for i in range(2, int(N ** 0.5) + 1):
+        if isp[i]:
+            isp[i * i::i] = False
+    out = {}
+    for p in ps:
+        f = pr = c = 1
+        for n in range(2, N + 1):
+            f = f * n % p
+            if isp[n]:
+                pr = pr * n % p
+            else:
+                c = c * n % p
+        out[p] = (f, pr, c)
+    return out
+
+
+# programs below and above the tensor-core setup's thresholds (kTcMinWords32/64):
+# 7, 214 and 460 896-bit words for the factorial
+@pytest.mark.parametrize("nmin", [101, 90001, 200001])
+def test_setup_programs_replayed_on_the_host_give_the_start_residues(pfc, nmin):
+    """Every form of the host-built setup programs -- 64-bit words, 896-bit
+    words, and the tensor-core setup's pairs of 896-bit words with their own
+    groups and power-of-R correction -- replayed as the device runs them
+    gives the definition's starting residues, for p in every size class and a
+    composite candidate (a base-2 pseudoprime)."""
+    ps = [int(o.candidates(10**9, 10**9 + 200)[0]), 2**31 - 1, int(o.candidates(2**40, 2**40 + 200)[0]),
+          int(o.candidates(2**62, 2**62 + 400)[0]), 2**64 - 59, 4294967297]
+    want = _start_residues(nmin, ps)
+    for p in ps:
+        f, pr, c = want[p]
+        for form in ("narrow", "wide", "paired"):
+            assert pfc.setup_program_eval(1, nmin, p, form) == (f, 0), (p, form)
+            assert pfc.setup_program_eval(2, nmin, p, form) == (pr, 0), (p, form)
+            assert pfc.setup_program_eval(4, nmin, p, form) == (c, 0), (p, form)
+            assert pfc.setup_program_eval(5, nmin, p, form) == (f, c), (p, form)
+
+
+def test_setup_program_eval_rejects_bad_arguments(pfc):
+    for mode, nmin, p in [(3, 101, 10**9 + 7), (1, 100, 10**9 + 7), (1, 101, 10**9 + 8), (1, 101, 1)]:
+        with pytest.raises(pfc.PFCError):
+            pfc.setup_program_eval(mode, nmin, p)
