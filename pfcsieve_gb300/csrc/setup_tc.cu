@@ -1,5 +1,7 @@
-// setup_tc.cu -- the setup of class-64 candidates below 2^64/3 (the lazy
-// class) with the table-word fold on the tensor cores (tcgen05).
+// setup_tc.cu -- the setup of class-32 candidates and of class-64 candidates
+// below 2^64/3 (the lazy class) with the table-word fold on the tensor cores
+// (tcgen05), for programs of at least kTcMinWords32 / kTcMinWords64 words
+// (kernels.cuh).  The description below is of class 64; class 32 follows it.
 //
 // The setup evaluates a program of table words Z (products of primes,
 // kernels.cuh Prog) into each candidate's residue.  The costly part on the
