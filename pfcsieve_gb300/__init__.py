@@ -202,7 +202,8 @@ class Context:
         _ck(lib().pfc_ctx_set_split(self.h, int(bool(on))), "pfc_ctx_set_split")
 
     def set_setup_tc(self, on):
-        """Fold the lazy class-64 setup's table words on the tensor cores (default on)."""
+        """Fold the setup's table words on the tensor cores (class 32 and class 64
+        below 2^64/3, programs above the word thresholds; default on)."""
         _ck(lib().pfc_ctx_set_setup_tc(self.h, int(bool(on))), "pfc_ctx_set_setup_tc")
         self.setup_tc = bool(on)
 

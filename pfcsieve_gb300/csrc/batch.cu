@@ -392,8 +392,8 @@ struct BatchJob {
     std::vector<WideWord> wordsw;      // class 64 below 2^64/3
     std::vector<SetupSeg> segs32, segs64;
     uint32_t nsetup32 = 0, nsetup64 = 0;
-    // class 64 below 2^64/3 on the tensor cores: the wide programs' groups
-    // (first program's, then the second's) and their shapes
+    // class 32 and class 64 below 2^64/3 on the tensor cores: the wide
+    // programs' groups (first program's, then the second's) and their shapes
     bool tc = false;
     // per size class (0: class 32, 1: class 64 below 2^64/3)
     bool tc_wait[2] = {false, false};    // its setup is still running (no window of the class yet)
