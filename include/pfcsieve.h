@@ -233,8 +233,9 @@ int pfc_job_verify_tables(pfc_job *job, uint64_t *table_bytes);
 
 /* Sort hits by (p, |n|, type), re-verify each on the CPU with naive products
  * when `verify` is set (verifyprime.cpp:199-268, OpenMP with `threads`),
- * drop hits whose p is not prime (7-base Miller-Rabin, verifyprime.cpp:
- * 157-195) and add n+c of every kept factor to *checksum
+ * drop hits whose p is not prime (exact Miller-Rabin with the same
+ * verdicts as the reference's 7 bases, verifyprime.cpp:157-195; below 2^32
+ * the bases 2, 7, 61) and add n+c of every kept factor to *checksum
  * (cl_sieve.cpp:496-589).  Kept factors are compacted to the front of f;
  * *kept receives their count. */
 int pfc_finalize_factors(unsigned mode, uint32_t nmax, pfc_factor *f, size_t n,

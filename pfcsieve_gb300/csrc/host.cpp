@@ -265,7 +265,32 @@ struct HMont {
     uint64_t add(uint64_t a, uint64_t b) const { return (a >= p - b) ? a + b - p : a + b; }
 };
 
-static bool sprp_base(const HMont &m, uint32_t base, int t, uint64_t d) {
+// the same for p < 2^32 with R = 2^32: values below p held in 64-bit words,
+// every product a plain 64-bit multiply (a b < p^2 < 2^64)
+struct HMont32 {
+    uint64_t p, one, r2;
+    uint32_t q;   // p^-1 mod 2^32
+    explicit HMont32(uint64_t p_) : p(p_) {
+        uint32_t x = (uint32_t)p;
+        for (int i = 0; i < 5; ++i) x *= 2u - (uint32_t)p * x;
+        q = x;
+        one = (1ull << 32) % p;
+        r2 = one * one % p;
+    }
+    // a b 2^-32 mod p for a b < 2^32 p: m p = t (mod 2^32), so t - m p is
+    // (hi(t) - hi(m p)) 2^32 exactly, with hi(t) - hi(m p) in (-p, p)
+    uint64_t mul(uint64_t a, uint64_t b) const {
+        const uint64_t t = a * b;
+        const uint32_t m = (uint32_t)t * q;
+        const uint64_t th = t >> 32, uh = ((uint64_t)m * p) >> 32;
+        return th >= uh ? th - uh : th + p - uh;
+    }
+    uint64_t to(uint64_t x) const { return mul(x, r2); }   // x < 2^32
+    uint64_t add(uint64_t a, uint64_t b) const { return (a >= p - b) ? a + b - p : a + b; }
+};
+
+template <class M>
+static bool sprp_base(const M &m, uint32_t base, int t, uint64_t d) {
     const uint64_t nmo = m.p - m.one;
     const uint64_t b = m.to(base);
     uint64_t a = m.one;
@@ -281,12 +306,9 @@ static bool sprp_base(const HMont &m, uint32_t base, int t, uint64_t d) {
     return false;
 }
 
-bool is_prime_u64(uint64_t p) {
-    static const uint32_t bases[7] = {2, 325, 9375, 28178, 450775, 9780504, 1795265022};
-    if (p < 2) return false;
-    if (!(p & 1)) return p == 2;
-    if (p < 9) return p > 1;
-    const HMont m(p);
+template <class M, size_t K>
+static bool sprp_bases(uint64_t p, const uint32_t (&bases)[K]) {
+    const M m(p);
     const int t = __builtin_ctzll(p - 1);
     const uint64_t d = (p - 1) >> t;
     for (uint32_t b : bases) {
@@ -300,6 +322,20 @@ bool is_prime_u64(uint64_t p) {
     return true;
 }
 
+// Exact primality, the reference's verdict (verifyprime.cpp:157-195 tests
+// the seven bases below, a set with no strong pseudoprime under 2^64).
+// Below 2^32 the bases 2, 7, 61 decide it as well (no composite under
+// 4,759,123,141 is a strong probable prime to all three; Jaeschke 1993), so
+// the verdict is the same with three 32-bit tests instead of seven 64-bit.
+bool is_prime_u64(uint64_t p) {
+    static const uint32_t bases64[7] = {2, 325, 9375, 28178, 450775, 9780504, 1795265022};
+    static const uint32_t bases32[3] = {2, 7, 61};
+    if (p < 2) return false;
+    if (!(p & 1)) return p == 2;
+    if (p < 9) return p > 1;
+    return p < (1ull << 32) ? sprp_bases<HMont32>(p, bases32) : sprp_bases<HMont>(p, bases64);
+}
+
 // starting products of verifyprime.cpp:205,222,241: 34!, 101#, 44!/44#
 static const u128 kStart[3] = {
     ((u128)0xde1bc4d19efcac82ull << 64) | 0x445da75b00000000ull,
@@ -309,7 +345,8 @@ static const u128 kStart[3] = {
 // r * (cur+1) * ... * n in Montgomery form: eight interleaved chains (one
 // chain is latency-bound; eight ran 2.7x faster than one on x86), the last
 // steps one at a time
-static uint64_t mul_range(const HMont &m, uint64_t r, uint64_t cur, uint64_t n) {
+template <class M>
+static uint64_t mul_range(const M &m, uint64_t r, uint64_t cur, uint64_t n) {
     if (n >= cur + 16) {
         const uint64_t step = m.to(8 % m.p);
         uint64_t a[8], x[8];
@@ -330,7 +367,8 @@ static uint64_t mul_range(const HMont &m, uint64_t r, uint64_t cur, uint64_t n) 
 
 // r * prod list[i], i in [b, e): four interleaved chains (the conversions
 // to Montgomery form are independent work between them)
-static uint64_t mul_list(const HMont &m, uint64_t r, const uint32_t *list, size_t b, size_t e) {
+template <class M>
+static uint64_t mul_list(const M &m, uint64_t r, const uint32_t *list, size_t b, size_t e) {
     uint64_t a[4] = {r, m.one, m.one, m.one};
     for (; b + 4 <= e; b += 4)
         for (int j = 0; j < 4; ++j) a[j] = m.mul(a[j], m.to(list[b + j]));
@@ -340,9 +378,10 @@ static uint64_t mul_list(const HMont &m, uint64_t r, const uint32_t *list, size_
 
 // One walk per (p, type) over the hits of one prime (sorted by |n|):
 // the value of verifyprime.cpp:199-268 for each hit.
-static bool verify_group(const pfc_factor *h, size_t cnt, const uint32_t *list, size_t listsize) {
+template <class M>
+static bool verify_group_m(const pfc_factor *h, size_t cnt, const uint32_t *list, size_t listsize) {
     const uint64_t p = h[0].p;
-    const HMont m(p);
+    const M m(p);
     const uint64_t nmo = p - m.one;
     for (int type = 0; type < 3; ++type) {
         bool init = false;
@@ -373,6 +412,13 @@ static bool verify_group(const pfc_factor *h, size_t cnt, const uint32_t *list, 
     return true;
 }
 
+// p < 2^32 in 32-bit Montgomery arithmetic (R = 2^32), else R = 2^64: the
+// products are the same residues either way
+static bool verify_group(const pfc_factor *h, size_t cnt, const uint32_t *list, size_t listsize) {
+    return h[0].p < (1ull << 32) ? verify_group_m<HMont32>(h, cnt, list, listsize)
+                                 : verify_group_m<HMont>(h, cnt, list, listsize);
+}
+
 uint64_t verify_start(int type, uint64_t p) { return (uint64_t)(kStart[type] % p); }
 
 bool verify_factor(uint64_t p, uint32_t n, int32_t c, int32_t type, const uint32_t *list, size_t listsize) {
@@ -401,6 +447,14 @@ extern "C" int pfc_finalize_factors(unsigned mode, uint32_t nmax, pfc_factor *f,
                                     int verify, size_t *kept, uint64_t *checksum) {
     if ((!f && n) || !kept || !checksum) return PFC_ERR_ARG;
     std::sort(f, f + n, factor_less);
+    // the hits of one p are adjacent: one verification walk and one
+    // primality verdict per group
+    std::vector<size_t> grp;
+    for (size_t i = 0; i < n; ++i)
+        if (i == 0 || f[i].p != f[i - 1].p) grp.push_back(i);
+    grp.push_back(n);
+    const int64_t ngrp = (int64_t)grp.size() - 1;
+    std::vector<uint8_t> good((size_t)std::max<int64_t>(ngrp, 0), 0);
     if (verify && n) {
         // verification lists (cl_sieve.cpp:1468-1492)
         std::vector<uint32_t> list;
@@ -417,33 +471,29 @@ extern "C" int pfc_finalize_factors(unsigned mode, uint32_t nmax, pfc_factor *f,
                 list.push_back(v);
             }
         }
-        std::vector<size_t> grp;
-        for (size_t i = 0; i < n; ++i)
-            if (i == 0 || f[i].p != f[i - 1].p) grp.push_back(i);
-        grp.push_back(n);
         int bad = 0;
 #ifdef _OPENMP
         if (threads > 0) omp_set_num_threads(threads);
 #else
         (void)threads;
 #endif
-        const int64_t ngrp = (int64_t)grp.size() - 1;
 #pragma omp parallel for schedule(dynamic, 1)
         for (int64_t g = 0; g < ngrp; ++g) {
             if (!verify_group(f + grp[g], grp[g + 1] - grp[g], list.data(), list.size())) {
 #pragma omp atomic write
                 bad = 1;
             }
+            good[g] = is_prime_u64(f[grp[g]].p);
         }
         if (bad) return PFC_ERR_VERIFY;
+    } else {
+        for (int64_t g = 0; g < ngrp; ++g) good[g] = is_prime_u64(f[grp[g]].p);
     }
     // drop 2-PRP factors, fold n+c into the checksum (cl_sieve.cpp:555-589)
     size_t k = 0;
-    uint64_t lastgood = 0;
-    for (size_t i = 0; i < n; ++i) {
-        const uint64_t p = f[i].p;
-        if (p == lastgood || is_prime_u64(p)) {
-            lastgood = p;
+    for (int64_t g = 0; g < ngrp; ++g) {
+        if (!good[g]) continue;
+        for (size_t i = grp[g]; i < grp[g + 1]; ++i) {
             const uint32_t fn = (uint32_t)(f[i].nc < 0 ? -f[i].nc : f[i].nc);
             const int32_t fc = f[i].nc < 0 ? -1 : 1;
             *checksum += (uint32_t)(fn + (uint32_t)fc);

@@ -76,6 +76,21 @@ def test_is_prime_matches_oracle(pfc):
         assert pfc.is_prime(x) == o.is_prime(x), x
 
 
+def test_is_prime_below_2_32_matches_oracle(pfc):
+    """Below 2^32 the host test takes three 32-bit bases: its verdicts equal
+    the reference's seven-base test (the oracle) on dense windows at 2^31
+    and below 2^32, random 32-bit values, and every base-2 strong
+    pseudoprime under 10^6 (they pass the first base)."""
+    rng = np.random.default_rng(5)
+    xs = list(range(2**31 - 20001, 2**31 + 20001, 2)) + list(range(2**32 - 40001, 2**32, 2))
+    xs += [int(x) | 1 for x in rng.integers(3, 2**32, size=20000, dtype=np.uint64)]
+    spsp = [x for x in range(3, 10**6, 2) if o.strong_prp_two(x) and not o.is_prime(x)]
+    assert 2047 in spsp and len(spsp) > 40
+    xs += spsp + [3215031751, 4759123141, 2**32 - 5, 2**32 + 15]
+    for x in xs:
+        assert pfc.is_prime(x) == o.is_prime(x), x
+
+
 @pytest.mark.parametrize("mode,nmin,nmax,pmin,pmax", [
     (1, 101, 200000, 101, 20000), (2, 101, 200000, 101, 20000),
     (4, 101, 200000, 101, 20000), (5, 101, 50000, 3, 30000),
