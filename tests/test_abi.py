@@ -106,6 +106,44 @@ def test_finalize_matches_oracle_job(pfc, mode, nmin, nmax, pmin, pmax):
     assert np.array_equal(o.sort_factors(kept), o.sort_factors(ofac))
 
 
+@pytest.mark.parametrize("p", [1000003, 16777259, 33554467])
+def test_finalize_accepts_wilson_hits_over_long_ranges(pfc, p):
+    """(p-1)! = -1 (mod p) (Wilson): the record (p, +(p-1), factorial) is a
+    true hit and the other sign is not; the re-verification walks up to 3.4e7
+    consecutive terms (the block-product path)."""
+    assert o.is_prime(p)
+    rec = np.zeros(1, dtype=pfc.FACTOR_DTYPE)
+    rec[0] = (p, p - 1, 0)
+    kept, _ = pfc.finalize(1, 2**31 - 1, rec, threads=1)
+    assert len(kept) == 1
+    rec[0] = (p, -(p - 1), 0)
+    with pytest.raises(pfc.PFCError):
+        pfc.finalize(1, 2**31 - 1, rec, threads=1)
+
+
+def test_finalize_accepts_true_hits_above_2_32(pfc):
+    """True hits of every type with p above 2^32 (the 64-bit arithmetic of
+    the re-verification), found by the oracle (tests/golden/make_verify_hits.py):
+    all are kept, and copies with the sign flipped, n moved by one or p moved
+    to the next odd number fail as the reference's check would fail them."""
+    d = np.load(os.path.join(ROOT, "tests", "golden", "verify_hits_64.npz"))
+    types = set()
+    for i in range(2):
+        mode, nmin, nmax, pmin, pmax = [int(x) for x in d["s%d_params" % i]]
+        hits = d["s%d_hits" % i]
+        assert len(hits) > 10 and (hits["p"] > 2**32).all()
+        types |= set(int(t) for t in hits["type"])
+        kept, add = pfc.finalize(mode, nmax, hits.copy(), threads=2)
+        assert len(kept) == len(hits)
+        assert add == sum(abs(int(x)) + (1 if x > 0 else -1) for x in hits["nc"]) % 2**64
+        for r in hits:
+            flipped = np.array([r], dtype=pfc.FACTOR_DTYPE)
+            flipped["nc"] = -flipped["nc"]
+            with pytest.raises(pfc.PFCError):
+                pfc.finalize(mode, nmax, flipped, threads=1)
+    assert types == {0, 1, 2}
+
+
 def test_finalize_rejects_false_hit(pfc):
     bad = np.zeros(1, dtype=pfc.FACTOR_DTYPE)
     bad[0] = (1000003, -1000, 0)   # 1000003 does not divide 1000!-1
