@@ -434,15 +434,26 @@ static uint64_t mul_list(const M &m, uint64_t r, const uint32_t *list, size_t b,
 
 // One walk per (p, type) over the hits of one prime (sorted by |n|):
 // the value of verifyprime.cpp:199-268 for each hit.
+// Mont(x^-1) from Mont(x) for prime p: Mont(x)^(p-2) in Montgomery form;
+// 0 when the product check fails (p composite, or x = 0 mod p)
 template <class M>
-static bool verify_group_m(const pfc_factor *h, size_t cnt, const uint32_t *list, size_t listsize) {
+static uint64_t mont_inverse(const M &m, uint64_t xm) {
+    uint64_t y = m.one, b = xm;
+    for (uint64_t e = m.p - 2; e; e >>= 1, b = m.mul(b, b))
+        if (e & 1) y = m.mul(y, b);
+    return m.mul(y, xm) == m.one ? y : 0;
+}
+
+template <class M>
+static bool verify_group_m(const pfc_factor *h, size_t cnt, const uint32_t *list, size_t listsize,
+                           const uint32_t *primes, size_t nprimes) {
     const uint64_t p = h[0].p;
     const M m(p);
     const uint64_t nmo = p - m.one;
     for (int type = 0; type < 3; ++type) {
         bool init = false;
         uint64_t r = 0;   // Montgomery running product
-        uint64_t cur = 34;
+        uint64_t cur = type == 2 ? 44 : 34;   // last integer multiplied in (types 0 and 2)
         size_t li = 0;
         for (size_t k = 0; k < cnt; ++k) {
             if (h[k].type != type) continue;
@@ -459,8 +470,20 @@ static bool verify_group_m(const pfc_factor *h, size_t cnt, const uint32_t *list
                 }
             } else {
                 const size_t e = (size_t)(std::upper_bound(list + li, list + listsize, n) - list);
-                r = mul_list(m, r, list, li, e);
+                // the composites of (cur, n] are its integers over its primes: a
+                // long range with n < p (no term 0 mod p) as a block product and
+                // the inverse of the primes' product, else term by term
+                uint64_t inv = 0, prm = m.one;
+                if (type == 2 && primes && n < p && cur < n && n - cur >= 4096) {
+                    const size_t pb = (size_t)(std::upper_bound(primes, primes + nprimes, (uint32_t)cur) - primes);
+                    const size_t pe = (size_t)(std::upper_bound(primes, primes + nprimes, n) - primes);
+                    prm = mul_list(m, m.one, primes, pb, pe);
+                    inv = mont_inverse(m, prm);
+                }
+                if (inv) r = m.mul(mul_range(m, r, cur, n), inv);
+                else r = mul_list(m, r, list, li, e);
                 li = e;
+                if (type == 2 && cur < n) cur = n;
             }
             if (!((r == m.one && c == -1) || (r == nmo && c == 1))) return false;
         }
@@ -470,9 +493,11 @@ static bool verify_group_m(const pfc_factor *h, size_t cnt, const uint32_t *list
 
 // p < 2^32 in 32-bit Montgomery arithmetic (R = 2^32), else R = 2^64: the
 // products are the same residues either way
-static bool verify_group(const pfc_factor *h, size_t cnt, const uint32_t *list, size_t listsize) {
-    return h[0].p < (1ull << 32) ? verify_group_m<HMont32>(h, cnt, list, listsize)
-                                 : verify_group_m<HMont>(h, cnt, list, listsize);
+// (primes: those of [45, nmax] for the compositorial, else null)
+static bool verify_group(const pfc_factor *h, size_t cnt, const uint32_t *list, size_t listsize,
+                         const uint32_t *primes = nullptr, size_t nprimes = 0) {
+    return h[0].p < (1ull << 32) ? verify_group_m<HMont32>(h, cnt, list, listsize, primes, nprimes)
+                                 : verify_group_m<HMont>(h, cnt, list, listsize, primes, nprimes);
 }
 
 uint64_t verify_start(int type, uint64_t p) { return (uint64_t)(kStart[type] % p); }
@@ -513,11 +538,11 @@ extern "C" int pfc_finalize_factors(unsigned mode, uint32_t nmax, pfc_factor *f,
     std::vector<uint8_t> good((size_t)std::max<int64_t>(ngrp, 0), 0);
     if (verify && n) {
         // verification lists (cl_sieve.cpp:1468-1492)
-        std::vector<uint32_t> list;
+        std::vector<uint32_t> list, pr;
         if (mode & PFC_PRIMORIAL) {
             list = primes_between(103, nmax);
         } else if (mode & PFC_COMPOSITORIAL) {
-            const std::vector<uint32_t> pr = primes_between(45, nmax);
+            pr = primes_between(45, nmax);
             size_t i = 0;
             for (uint32_t v = 45; v < nmax; ++v) {
                 if (i < pr.size() && pr[i] == v) {
@@ -535,7 +560,8 @@ extern "C" int pfc_finalize_factors(unsigned mode, uint32_t nmax, pfc_factor *f,
 #endif
 #pragma omp parallel for schedule(dynamic, 1)
         for (int64_t g = 0; g < ngrp; ++g) {
-            if (!verify_group(f + grp[g], grp[g + 1] - grp[g], list.data(), list.size())) {
+            if (!verify_group(f + grp[g], grp[g + 1] - grp[g], list.data(), list.size(),
+                              pr.empty() ? nullptr : pr.data(), pr.size())) {
 #pragma omp atomic write
                 bad = 1;
             }
