@@ -85,8 +85,6 @@ struct Mont32 {
         }
         return acc;
     }
-    // value with R = 2^64 Montgomery scaling: x*2^64 mod p, from x*2^32 mod p
-    __device__ __forceinline__ uint64_t mont32_to_mont64(uint32_t xm) const { return mul(xm, r2); }
 };
 
 // ------------------------------------------------------------------ class 64
