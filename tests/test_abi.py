@@ -144,6 +144,28 @@ def test_finalize_accepts_true_hits_above_2_32(pfc):
     assert types == {0, 1, 2}
 
 
+@pytest.mark.parametrize("name", ["cfg1", "cfg2"])
+def test_finalize_keeps_the_reference_programs_factors(pfc, name):
+    """The factors.txt the reference's own OpenCL program wrote for two
+    benchmark searches (tests/golden/ref_opencl_*_factors.txt), read back as
+    records: the host re-verification and 2-PRP filter keep every one, and
+    they format to the same lines (cl_sieve.cpp:565-581)."""
+    g = np.load(os.path.join(ROOT, "tests", "golden", "configs.npz"))
+    mode, nmin, nmax = (int(x) for x in g[name + "_params"][:3])
+    lines = open(os.path.join(ROOT, "tests", "golden", "ref_opencl_%s_factors.txt" % name)).read().splitlines()
+    body = [x for x in lines[:-1] if x != "no factors"]
+    recs = np.zeros(len(body), dtype=pfc.FACTOR_DTYPE)
+    for i, line in enumerate(body):
+        ps, rest = line.split(" | ")
+        m = re.match(r"(\d+)(!/#|!|#)([+-]1)$", rest)
+        n, typ, c = int(m.group(1)), {"!": 0, "#": 1, "!/#": 2}[m.group(2)], int(m.group(3))
+        recs[i] = (int(ps), c * n if c > 0 else -n, typ)
+    kept, add = pfc.finalize(mode, nmax, recs.copy(), threads=4)
+    assert len(kept) == len(body) > 200
+    assert add == sum(abs(int(x)) + (1 if x > 0 else -1) for x in recs["nc"]) % 2**64
+    assert sorted(pfc.format_factor(f) for f in kept) == sorted(body)
+
+
 def test_finalize_rejects_false_hit(pfc):
     bad = np.zeros(1, dtype=pfc.FACTOR_DTYPE)
     bad[0] = (1000003, -1000, 0)   # 1000003 does not divide 1000!-1
